@@ -1,0 +1,32 @@
+#!/usr/bin/env bash
+# Builds oracle/_ref/libref_kernels.so: the reference's own OpenCL kernels
+# (kernels/grid.cl, wcsph.cl, normals.cl, pcisph.cl, boundary.cl and their headers)
+# compiled for the CPU through oracle/ref_shim/clshim.hpp.  Used only to pin the oracle
+# and to generate tests/golden/ fixtures, in a container where the reference is mounted.
+#
+# The one source transformation rewrites OpenCL vector literals "(int4)(" / "(float4)("
+# into function calls, on copies written under oracle/_ref/src (never committed).
+#
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+set -euo pipefail
+here="$(cd "$(dirname "$0")" && pwd)"
+ref="${1:-/root/reference}"
+if [ ! -d "$ref/kernels" ]; then
+    echo "build_ref: no reference kernels under $ref; skipped" >&2
+    exit 0
+fi
+out="$here/_ref"
+mkdir -p "$out/src" "$out/obj"
+for f in "$ref"/kernels/*.cl "$ref"/kernels/*.h; do
+    sed -E 's/\((int4|float4)\)[[:space:]]*\(/make_\1(/g' "$f" > "$out/src/$(basename "$f")"
+done
+CXX="${CXX:-g++}"
+flags=(-O1 -std=c++17 -fPIC -ffp-contract=off -Wall -Wno-sign-compare -Wno-unused -I "$here/ref_shim" -I "$out/src")
+pids=()
+for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary; do
+    "$CXX" "${flags[@]}" -c "$here/ref_shim/$u.cpp" -o "$out/obj/$u.o" &
+    pids+=($!)
+done
+for p in "${pids[@]}"; do wait "$p"; done
+"$CXX" -shared -o "$out/libref_kernels.so" "$out"/obj/*.o
+echo "build_ref: built $out/libref_kernels.so"

@@ -1,0 +1,200 @@
+"""ctypes wrapper of oracle/_ref/libref_kernels.so -- the reference's own OpenCL kernels
+compiled for the CPU (TEST INFRASTRUCTURE; pins the oracle; available only where the
+reference is mounted and ``oracle/build_ref.sh`` has run)."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_ref", "libref_kernels.so")
+REFERENCE_ROOT = "/root/reference"
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB) or os.path.isdir(os.path.join(REFERENCE_ROOT, "kernels"))
+
+
+def build(force=False):
+    if os.path.exists(LIB) and not force:
+        return LIB
+    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "kernels")):
+        return None
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
+    return LIB if os.path.exists(LIB) else None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if build() is None:
+            raise RuntimeError("reference kernels unavailable")
+        _lib = C.CDLL(LIB)
+    return _lib
+
+
+def P(a):
+    """Pointer to a contiguous numpy array (or NULL)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+def f(x):
+    return C.c_float(float(x))
+
+
+def i(x):
+    return C.c_int(int(x))
+
+
+def compute_hashes(pos4, size, h, cps):
+    n = len(pos4)
+    hs = np.zeros(n, np.uint32)
+    mk = np.zeros(n, np.int32)
+    lib().ref_compute_hashes(P(pos4), i(n), f(size), f(h), i(cps), P(hs), P(mk))
+    return hs, mk
+
+
+def compute_cell_intervals(spos4, hashes, size, h, cps):
+    iv = np.zeros(2 * cps ** 3, np.int32)
+    lib().ref_compute_cell_intervals(P(spos4), P(hashes), i(len(spos4)), f(size), f(h), i(cps), P(iv))
+    return iv
+
+
+def compute_neigh_list(ref_pos4, neigh_pos4, intervals, size, h, h_define, cps, cap=50):
+    n = len(ref_pos4)
+    lst = np.zeros(cap * max(n, 1), np.int32)
+    ln = np.zeros(n, np.int32)
+    lib().ref_compute_neigh_list(P(ref_pos4), i(n), P(neigh_pos4), P(intervals), f(size), f(h), f(h_define),
+                                 i(cps), P(lst), P(ln))
+    return lst, ln
+
+
+def wc_density_pressure(spos4, flist, flen, bpos4, bphi, blist, blen, mass, h, gas_k, rho0, poly6, h_define):
+    n = len(spos4)
+    d = np.zeros(n, np.float32)
+    p = np.zeros(n, np.float32)
+    lib().ref_wc_density_pressure(P(spos4), i(n), P(d), P(p), f(mass), f(h), f(gas_k), f(rho0), f(poly6),
+                                  P(flen), P(flist), P(blist), P(blen), P(bpos4), P(bphi), f(h_define))
+    return d, p
+
+
+def wc_acceleration(spos4, svel4, nrm4, dens, pres, flist, flen, bpos4, bphi, blist, blen, g, mass, h, mu, sigma,
+                    rho0, sc9, st_main, st_term, h_define):
+    n = len(spos4)
+    acc = np.zeros((n, 4), np.float32)
+    g4 = np.array([0.0, -g, 0.0, 0.0], np.float32)
+    sc = np.ascontiguousarray(sc9, np.float32)
+    lib().ref_wc_acceleration(P(spos4), P(svel4), P(nrm4), P(dens), P(pres), P(acc), i(n), P(g4), f(mass), f(h),
+                              f(h * h), f(mu), f(sigma), f(rho0), P(sc), P(flen), P(flist), P(blist), P(blen),
+                              P(bpos4), P(bphi), f(st_main), f(st_term), f(h_define))
+    return acc
+
+
+def wc_integrate(spos4, svel4, svh4, acc4, dt, max_vel, limits, h_define):
+    n = len(spos4)
+    op, ov, ovh = (np.zeros((n, 4), np.float32) for _ in range(3))
+    lim = np.array(list(limits) + [0.0], np.float32)
+    lib().ref_wc_integrate(P(spos4), P(svel4), P(svh4), P(acc4), i(n), f(dt), P(op), P(ov), P(ovh), f(max_vel),
+                           P(lim), f(h_define))
+    return op, ov, ovh
+
+
+def compute_normals(spos4, dens, flist, flen, w_grad, mass_define, h_define, local_size=64):
+    n = len(spos4)
+    nrm = np.zeros((n, 4), np.float32)
+    lib().ref_compute_normals(P(spos4), P(dens), P(nrm), i(n), P(flen), P(flist), f(w_grad), f(mass_define),
+                              f(h_define), i(local_size))
+    return nrm
+
+
+def pci_initial_density(spos4, flist, flen, bpos4, bphi, blist, blen, w_eval, h_def, m_def, rho_def, local_size=64):
+    n = len(spos4)
+    d = np.zeros(n, np.float32)
+    lib().ref_pci_initial_density(P(spos4), P(d), i(n), P(flen), P(flist), P(blist), P(blen), P(bpos4), P(bphi),
+                                  f(w_eval), f(h_def), f(m_def), f(rho_def), i(local_size))
+    return d
+
+
+def pci_initial_forces(spos4, svel4, dens, nrm4, flist, flen, mu, sigma, visc_lapl, st_main, st_term, h_def, m_def,
+                       rho_def, local_size=64):
+    n = len(spos4)
+    fo = np.zeros((n, 4), np.float32)
+    lib().ref_pci_initial_forces(P(spos4), P(svel4), P(dens), P(nrm4), P(fo), i(n), f(mu), f(sigma), P(flen),
+                                 P(flist), f(visc_lapl), f(st_main), f(st_term), f(h_def), f(m_def), f(rho_def),
+                                 i(local_size))
+    return fo
+
+
+def pci_predict_pos(spos4, svel4, fo4, fp4, dt, g, max_vel, limits, h_def, m_def, rho_def):
+    n = len(spos4)
+    pred = np.zeros((n, 4), np.float32)
+    g4 = np.array([0.0, -g, 0.0, 0.0], np.float32)
+    lim = np.array(list(limits) + [0.0], np.float32)
+    lib().ref_pci_predict_pos(P(spos4), P(svel4), P(fo4), P(fp4), P(pred), i(n), f(dt), P(g4), f(max_vel), P(lim),
+                              f(h_def), f(m_def), f(rho_def))
+    return pred
+
+
+def pci_update_pressure(pred4, pres, delta, flist, flen, bpos4, bphi, blist, blen, w_eval, h_def, m_def, rho_def,
+                        local_size=64):
+    n = len(pred4)
+    dv = np.zeros(n, np.float32)
+    p = np.ascontiguousarray(pres, np.float32).copy()
+    lib().ref_pci_update_pressure(P(pred4), P(dv), P(p), i(n), f(delta), P(flen), P(flist), P(blist), P(blen),
+                                  P(bpos4), P(bphi), f(w_eval), f(h_def), f(m_def), f(rho_def), i(local_size))
+    return dv, p
+
+
+def pci_pressure_force(spos4, dens, pres, size, h, cps, flist, flen, bpos4, bphi, blist, blen, w_grad, h_def, m_def,
+                       rho_def, local_size=64):
+    n = len(spos4)
+    fp = np.zeros((n, 4), np.float32)
+    lib().ref_pci_pressure_force(P(spos4), P(dens), P(pres), P(fp), i(n), f(size), f(h), i(cps), P(flen), P(flist),
+                                 P(blist), P(blen), P(bpos4), P(bphi), f(w_grad), f(h_def), f(m_def), f(rho_def),
+                                 i(local_size))
+    return fp
+
+
+def pci_integrate(spos4, svel4, fo4, fp4, dt, g, max_vel, limits, h_def, m_def, rho_def):
+    n = len(spos4)
+    op, ov = np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32)
+    g4 = np.array([0.0, -g, 0.0, 0.0], np.float32)
+    lim = np.array(list(limits) + [0.0], np.float32)
+    lib().ref_pci_integrate(P(spos4), P(svel4), P(fo4), P(fp4), P(op), P(ov), i(n), f(dt), P(g4), f(max_vel),
+                            P(lim), f(h_def), f(m_def), f(rho_def))
+    return op, ov
+
+
+def boundary_phi(pos4, rho0, w_eval, phi_coeff, h_define):
+    n = len(pos4)
+    phi = np.zeros(n, np.float32)
+    lib().ref_boundary_phi(P(pos4), P(phi), i(n), f(rho0), f(w_eval), f(phi_coeff), f(h_define))
+    return phi
+
+
+def transform_particles(raw4, rot3x4, lin, ang):
+    n = len(raw4)
+    out, vel = np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32)
+    r = np.asarray(rot3x4, np.float32).reshape(3, 4)
+    m = [np.array([r[k, 0], r[k, 1], r[k, 2], 0.0], np.float32) for k in range(3)]
+    cm = np.array([r[0, 3], r[1, 3], r[2, 3], 1.0], np.float32)
+    li = np.array(list(lin)[:3] + [0.0], np.float32)
+    an = np.array(list(ang)[:3] + [0.0], np.float32)
+    lib().ref_transform_particles(P(raw4), P(out), P(vel), P(m[0]), P(m[1]), P(m[2]), P(li), P(an), P(cm), i(n))
+    return out, vel
+
+
+def fluid_force(bpos4, bphi, fpos4, fdens, fpres, intervals, mass, spiky_grad, size, h, cps, center, fvel4, bvel4,
+                visc_lapl, h_define):
+    n = len(bpos4)
+    force, torque = np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32)
+    c4 = np.array(list(center)[:3] + [1.0], np.float32)
+    lib().ref_fluid_force(P(bpos4), P(bphi), P(fpos4), P(fdens), P(fpres), P(intervals), f(mass), f(spiky_grad),
+                          f(size), f(h), i(cps), i(n), P(force), P(torque), P(c4), P(fvel4), P(bvel4), f(visc_lapl),
+                          f(h_define))
+    return force, torque
