@@ -1,0 +1,295 @@
+"""ctypes binding of the C ABI in include/sph_capi.h (libsph_gb300.so).
+
+This is the Python face of the drop-in boundary: every call goes through the exported
+``extern "C"`` entry points.  The library must exist (``fluids_gb300.build()``); on a
+machine with a GPU there is no fallback -- a missing library or device raises.
+"""
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+_lock = threading.Lock()
+_lib = None
+
+SPH_WCSPH, SPH_PCISPH = 0, 1
+SPH_MODE_COMPAT, SPH_MODE_PHYSICS = 0, 1
+SPH_NEIGH_SCAN, SPH_NEIGH_LIST = 0, 1
+FLAGS = dict(NAN=1, ESCAPED=2, TIMEOUT=4, OVERFLOW=8, NONCONVERGED=16)
+STATUS = {0: "SPH_OK", 1: "SPH_E_INVALID", 2: "SPH_E_CUDA", 3: "SPH_E_NONCONVERGED", 4: "SPH_E_ESCAPED",
+          5: "SPH_E_NAN", 6: "SPH_E_TIMEOUT", 7: "SPH_E_OVERFLOW", 8: "SPH_E_STATE", 9: "SPH_E_NOMEM"}
+STAGES = dict(BOUNDARY_SYNC=0, HASHES=1, SORT=2, SHUFFLE=3, CELL_INTERVALS=4, NEIGH_LIST=5, SB_NEIGH_LIST=6,
+              WC_DENSITY=7, NORMALS=8, WC_ACCEL=9, WC_INTEGRATE=10, PCI_INIT_DENSITY=11, PCI_INIT_FORCES=12,
+              PCI_LOOP=13, PCI_INTEGRATE=14, BOUNDARY_FORCES=15)
+FIELDS = dict(POS=0, VEL=1, VEL_HALF=2, POS_SORTED=3, VEL_SORTED=4, VEL_HALF_SORTED=5, HASHES=6, MASK=7,
+              CELL_INTERVALS=8, NEIGH_LIST=9, NEIGH_LEN=10, SB_NEIGH_LIST=11, SB_NEIGH_LEN=12, DENSITY=13,
+              PRESSURE=14, NORMAL=15, ACCEL=16, POS_PRED=17, FORCE_OTHER=18, FORCE_PRESSURE=19, DENS_VAR=20,
+              BPOS_SORTED=21, BPHI_SORTED=22, BCELL_INTERVALS=23, BHASHES=24, BMASK=25, BPHI=26, BPOS=27,
+              BODY_FORCE=28, BODY_TORQUE=29, PCI_ITERS=30, PCI_MAXERR=31, ID=32)
+_KIND = {0: np.float32, 1: np.int32, 2: np.uint32}
+
+# Every symbol include/sph_capi.h declares (checked by tests/test_capi_symbols.py).
+EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", "sph_reset", "sph_set_stream",
+           "sph_set_rect_limits", "sph_add_volume", "sph_add_boundary", "sph_set_body_transform",
+           "sph_particle_count", "sph_boundary_particle_count", "sph_simulate", "sph_run_stage",
+           "sph_synchronize", "sph_device_flags", "sph_field_elems", "sph_field_kind", "sph_get_field",
+           "sph_set_field", "sph_field_device_ptr", "sph_body_forces", "sph_stats", "sph_sort_pairs",
+           "sph_scene_box_volume", "sph_scene_fishtank", "sph_scene_cube", "sph_jitter", "sph_cuda_available",
+           "sph_describe"]
+
+
+class SphParams(C.Structure):
+    _fields_ = [("method", C.c_int), ("mode", C.c_int), ("time_step", C.c_float), ("max_vel", C.c_float),
+                ("particle_radius", C.c_float), ("support_radius", C.c_float),
+                ("pcisph_min_iterations", C.c_int), ("pcisph_max_iterations", C.c_int),
+                ("pcisph_error_ratio", C.c_float), ("pcisph_relax_max_iterations", C.c_int),
+                ("rest_density", C.c_float), ("k_viscosity", C.c_float), ("gravity", C.c_float),
+                ("gas_stiffness", C.c_float), ("surface_tension", C.c_float), ("grid_size", C.c_float),
+                ("grid_margin", C.c_float), ("boundary_phi_coeff", C.c_float), ("neigh_cap", C.c_int),
+                ("relax_on_add", C.c_int), ("neighbor_mode", C.c_int), ("use_graph", C.c_int),
+                ("block_size", C.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class SphDerived(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("mass", "mass_def", "h", "h_def", "rest_density_def", "poly6_eval",
+                                          "poly6_grad", "spiky_grad", "visc_lapl", "st_main", "st_term",
+                                          "default_eval", "boundary_eval", "pci_delta")] + \
+               [("grid_origin", C.c_float * 3), ("grid_dims", C.c_int * 3), ("grid_wrap", C.c_int),
+                ("key_bits", C.c_int)]
+
+    def as_dict(self):
+        d = {n: getattr(self, n) for n, _ in self._fields_}
+        d["grid_origin"] = list(self.grid_origin)
+        d["grid_dims"] = list(self.grid_dims)
+        return d
+
+
+class SphError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+def lib():
+    """Loads libsph_gb300.so (building it in-tree if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            _build.build()
+        L = C.CDLL(LIB_PATH)
+        vp, ip, fp, cp = C.c_void_p, C.c_int, C.c_void_p, C.c_char_p
+        PP = C.POINTER(SphParams)
+        sig = {
+            "sph_default_params": (None, [ip, PP]),
+            "sph_create": (ip, [PP, C.POINTER(vp)]),
+            "sph_destroy": (ip, [vp]),
+            "sph_last_error": (cp, [vp]),
+            "sph_reset": (ip, [vp, PP]),
+            "sph_set_stream": (ip, [vp, vp]),
+            "sph_set_rect_limits": (ip, [vp, C.c_float, C.c_float, C.c_float]),
+            "sph_add_volume": (ip, [vp, fp, fp, ip]),
+            "sph_add_boundary": (ip, [vp, fp, ip, ip, fp, fp, fp, C.c_float]),
+            "sph_set_body_transform": (ip, [vp, ip, fp, fp, fp]),
+            "sph_particle_count": (ip, [vp]),
+            "sph_boundary_particle_count": (ip, [vp]),
+            "sph_simulate": (ip, [vp, ip]),
+            "sph_run_stage": (ip, [vp, ip]),
+            "sph_synchronize": (ip, [vp]),
+            "sph_device_flags": (ip, [vp, C.POINTER(C.c_uint), ip]),
+            "sph_field_elems": (C.c_longlong, [vp, ip]),
+            "sph_field_kind": (ip, [ip]),
+            "sph_get_field": (ip, [vp, ip, vp, C.c_size_t]),
+            "sph_set_field": (ip, [vp, ip, vp, C.c_size_t]),
+            "sph_field_device_ptr": (ip, [vp, ip, C.POINTER(vp)]),
+            "sph_body_forces": (ip, [vp, fp, fp, ip]),
+            "sph_stats": (ip, [vp, C.POINTER(C.c_double)]),
+            "sph_sort_pairs": (ip, [vp, vp, ip, ip, vp]),
+            "sph_scene_box_volume": (ip, [fp, fp, C.c_float, fp, ip]),
+            "sph_scene_fishtank": (ip, [C.c_float, C.c_float, C.c_float, C.c_float, fp, ip]),
+            "sph_scene_cube": (ip, [C.c_float, C.c_float, fp, ip]),
+            "sph_jitter": (None, [fp, ip, C.c_float, C.c_uint64]),
+            "sph_cuda_available": (ip, []),
+            "sph_describe": (ip, [PP, fp, C.POINTER(SphDerived)]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+        return L
+
+
+def ptr(a):
+    """Address of a contiguous numpy array (None for None)."""
+    if a is None:
+        return None
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data
+
+
+def f4(a):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if a.ndim == 1:
+        a = a.reshape(-1, 4)
+    if a.ndim != 2 or a.shape[1] != 4:
+        raise ValueError("expected an (n, 4) float32 array, got shape %r" % (a.shape,))
+    return a
+
+
+def default_params(method=SPH_WCSPH):
+    p = SphParams()
+    lib().sph_default_params(int(method), C.byref(p))
+    return p
+
+
+def make_params(method=SPH_WCSPH, **kw):
+    p = default_params(method)
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError("unknown parameter %r" % k)
+        setattr(p, k, v)
+    return p
+
+
+def describe(params, container=(0.0, 0.0, 0.0)):
+    """Constants and grid a context derives (sph_describe; host only)."""
+    c = np.ascontiguousarray(container, np.float32)
+    d = SphDerived()
+    check(lib().sph_describe(C.byref(params), ptr(c), C.byref(d)))
+    return d.as_dict()
+
+
+def cuda_available():
+    return bool(lib().sph_cuda_available())
+
+
+def last_error(handle=None):
+    s = lib().sph_last_error(handle)
+    return s.decode() if s else ""
+
+
+def check(rc, handle=None):
+    if rc != 0:
+        raise SphError(rc, last_error(handle))
+    return rc
+
+
+class Context:
+    """Owns one ``sph_ctx``.  Thin: each method is one C-ABI call."""
+
+    def __init__(self, params):
+        self._lib = lib()
+        h = C.c_void_p()
+        check(self._lib.sph_create(C.byref(params), C.byref(h)))
+        self.h = h
+        self.params = params
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.sph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, rc):
+        return check(rc, self.h)
+
+    def set_rect_limits(self, w, h, d):
+        self._c(self._lib.sph_set_rect_limits(self.h, w, h, d))
+
+    def add_volume(self, pos4, vel4=None):
+        p = f4(pos4)
+        v = None if vel4 is None else f4(vel4)
+        self._c(self._lib.sph_add_volume(self.h, ptr(p), ptr(v), len(p)))
+
+    def add_boundary(self, pos4, can_move=False, rot3x4=None, lin=None, ang=None, mass=0.0):
+        p = f4(pos4)
+        r = None if rot3x4 is None else np.ascontiguousarray(rot3x4, np.float32).reshape(12)
+        li = None if lin is None else np.ascontiguousarray(lin, np.float32).reshape(4)
+        an = None if ang is None else np.ascontiguousarray(ang, np.float32).reshape(4)
+        self._c(self._lib.sph_add_boundary(self.h, ptr(p), len(p), int(bool(can_move)), ptr(r), ptr(li), ptr(an),
+                                           float(mass)))
+
+    def set_body_transform(self, body, rot3x4=None, lin=None, ang=None):
+        r = None if rot3x4 is None else np.ascontiguousarray(rot3x4, np.float32).reshape(12)
+        li = None if lin is None else np.ascontiguousarray(lin, np.float32).reshape(4)
+        an = None if ang is None else np.ascontiguousarray(ang, np.float32).reshape(4)
+        self._c(self._lib.sph_set_body_transform(self.h, int(body), ptr(r), ptr(li), ptr(an)))
+
+    def reset(self, params):
+        self.params = params
+        self._c(self._lib.sph_reset(self.h, C.byref(params)))
+
+    def simulate(self, steps=1):
+        self._c(self._lib.sph_simulate(self.h, int(steps)))
+
+    def stage(self, name):
+        s = STAGES[name] if isinstance(name, str) else int(name)
+        self._c(self._lib.sph_run_stage(self.h, s))
+
+    def synchronize(self):
+        self._c(self._lib.sph_synchronize(self.h))
+
+    def device_flags(self, clear=False):
+        f = C.c_uint()
+        self._c(self._lib.sph_device_flags(self.h, C.byref(f), int(bool(clear))))
+        return int(f.value)
+
+    def particle_count(self):
+        return int(self._lib.sph_particle_count(self.h))
+
+    def boundary_particle_count(self):
+        return int(self._lib.sph_boundary_particle_count(self.h))
+
+    def get(self, field):
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        n = self._lib.sph_field_elems(self.h, fid)
+        if n < 0:
+            raise SphError(1, "bad field %r" % (field,))
+        out = np.empty(int(n), dtype=_KIND[self._lib.sph_field_kind(fid)])
+        self._c(self._lib.sph_get_field(self.h, fid, out.ctypes.data, out.nbytes))
+        return out
+
+    def set(self, field, arr):
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        a = np.ascontiguousarray(arr, dtype=_KIND[self._lib.sph_field_kind(fid)]).reshape(-1)
+        self._c(self._lib.sph_set_field(self.h, fid, a.ctypes.data, a.nbytes))
+
+    def device_ptr(self, field):
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        p = C.c_void_p()
+        self._c(self._lib.sph_field_device_ptr(self.h, fid, C.byref(p)))
+        return int(p.value or 0)
+
+    def body_forces(self, nbodies):
+        f = np.zeros((nbodies, 4), np.float32)
+        t = np.zeros((nbodies, 4), np.float32)
+        self._c(self._lib.sph_body_forces(self.h, ptr(f), ptr(t), int(nbodies)))
+        return f, t
+
+    def stats(self):
+        out = (C.c_double * 8)()
+        self._c(self._lib.sph_stats(self.h, out))
+        keys = ["mean_compression", "mean_abs_density_error", "max_density_error", "kinetic", "potential",
+                "com_x", "com_y", "com_z"]
+        return dict(zip(keys, list(out)))
+
+
+def sort_pairs_device(d_keys, d_vals, n, key_bits=32, stream=None):
+    """sph_sort_pairs on device addresses (ints)."""
+    check(lib().sph_sort_pairs(C.c_void_p(d_keys), C.c_void_p(d_vals), int(n), int(key_bits),
+                               C.c_void_p(stream or 0)))

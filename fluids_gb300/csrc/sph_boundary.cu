@@ -1,0 +1,218 @@
+/*
+ * sph_boundary.cu -- boundary-particle coupling (kernels/boundary.cl) and device statistics.
+ *
+ *   k_bnd_transform  transform_particles (boundary.cl:33-59): x = R x_raw + c, boundary
+ *                    velocity v = v_lin + w*(x - c) componentwise in COMPAT (the kernel
+ *                    text), w x (x - c) in PHYSICS (P6).  Uncontracted arithmetic, so the
+ *                    positions (and the Morton keys built from them) equal the oracle's.
+ *   k_bnd_phi        compute_boundary_phi (boundary.cl:4-31): Psi_b = rho0 / (W_sum w) / coeff
+ *                    over the particles of the same body.  The reference loops over every
+ *                    particle of the body (O(n^2)); here the sorted boundary cell table gives
+ *                    the same set (r^2 < h^2) in O(n), summed in cell order.
+ *   k_bnd_forces     compute_fluid_force (boundary.cl:61-118) + clsum (clreduce.h:74-86): the
+ *                    pressure force of the fluid on each particle of a body with mass > 0 and
+ *                    its torque about the body centre, reduced per body with warp shuffles and
+ *                    one atomic per warp (no host read per body as in
+ *                    boundaryhandler.cpp:338-346).
+ *   k_stats          density error, kinetic/potential energy and centre of mass.
+ */
+#include "sph_kernels.cuh"
+
+namespace sph {
+
+__global__ void k_bnd_transform(int nb, const float4* __restrict__ raw, const int32_t* __restrict__ body,
+                                const float* __restrict__ xf, const int32_t* __restrict__ range, int compat,
+                                int only_movable, float4* __restrict__ pos, float4* __restrict__ vel) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const int bi = body[i];
+    if (only_movable && range[4 * bi + 2] == 0) return;
+    const float* t = xf + 20 * bi;
+    const float4 r = raw[i];
+    /* dot(m_k, p) over (x, y, z, w) with m_k.w = 0: ((a+b)+c)+0 */
+    const float px = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(t[0], r.x), __fmul_rn(t[1], r.y)), __fmul_rn(t[2], r.z)), 0.f);
+    const float py = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(t[4], r.x), __fmul_rn(t[5], r.y)), __fmul_rn(t[6], r.z)), 0.f);
+    const float pz = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(t[8], r.x), __fmul_rn(t[9], r.y)), __fmul_rn(t[10], r.z)), 0.f);
+    const float x = __fadd_rn(px, t[3]), y = __fadd_rn(py, t[7]), z = __fadd_rn(pz, t[11]);
+    pos[i] = make_float4(x, y, z, 1.f);
+    const float rx = __fsub_rn(x, t[3]), ry = __fsub_rn(y, t[7]), rz = __fsub_rn(z, t[11]);
+    const float ax = t[16], ay = t[17], az = t[18];
+    float vx, vy, vz;
+    if (compat) {
+        vx = __fadd_rn(t[12], __fmul_rn(ax, rx));
+        vy = __fadd_rn(t[13], __fmul_rn(ay, ry));
+        vz = __fadd_rn(t[14], __fmul_rn(az, rz));
+    } else {
+        vx = t[12] + (ay * rz - az * ry);
+        vy = t[13] + (az * rx - ax * rz);
+        vz = t[14] + (ax * ry - ay * rx);
+    }
+    vel[i] = make_float4(vx, vy, vz, 0.f);
+}
+
+__global__ void k_bnd_phi(Const c, int nb, const float4* __restrict__ bpos_s, const int32_t* __restrict__ body_s,
+                          const int2* __restrict__ btab, const int32_t* __restrict__ bmask_s, float phi_coeff,
+                          float* __restrict__ bphi_s, float* __restrict__ bphi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const float4 pi = bpos_s[i];
+    const int bi = body_s[i];
+    const float H = c.h_def, HH = H * H;
+    Const cu = c;
+    cu.cap = 0x7fffffff;
+    cu.h2_list = HH;
+    float del = 0.f;
+    scan_neighbors(cu, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float dx, float dy, float dz) {
+        if (__ldg(&body_s[j]) == bi) {
+            const float t = HH - r2_exact(dx, dy, dz);
+            del += (t * t) * t;
+        }
+    });
+    const float phi = (c.rho0 / (del * c.boundary_eval)) / phi_coeff;
+    bphi_s[i] = phi;
+    bphi[bmask_s[i]] = phi;
+}
+
+__global__ void k_bnd_forces(Const c, int nb, const float4* __restrict__ bpos, const float* __restrict__ bphi,
+                             const int32_t* __restrict__ body, const int32_t* __restrict__ range,
+                             const float* __restrict__ xf, const float4* __restrict__ spos,
+                             const float* __restrict__ dens, const float* __restrict__ pres,
+                             const int2* __restrict__ tab, float4* __restrict__ body_force,
+                             float4* __restrict__ body_torque) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < nb;
+    int bi = -1;
+    float fx = 0.f, fy = 0.f, fz = 0.f, tx = 0.f, ty = 0.f, tz = 0.f;
+    if (live) {
+        bi = body[i];
+        if (range[4 * bi + 3] == 0) bi = -1;
+    }
+    if (bi >= 0) {
+        const float4 pi = bpos[i];
+        const float H = c.h_def;
+        int cx, cy, cz;
+        cell_of(c, pi.x, pi.y, pi.z, cx, cy, cz);
+        int cnt = 0;
+        for (int o = 0; cnt < c.cap && o < 27; ++o) {
+            int ox, oy, oz;
+            neigh_offset(o, ox, oy, oz);
+            long long id;
+            if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) continue;
+            const int2 rg = tab[id];
+            for (int j = rg.x; cnt < c.cap && j < rg.y; ++j) {
+                const float4 pj = spos[j];
+                const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
+                const float rn = sqrtf(rx * rx + ry * ry + rz * rz);
+                if (rn < H) {
+                    const float dj = dens[j];
+                    const float C = pres[j] / (dj * dj);
+                    ++cnt;
+                    const float s = c.bforce_spiky / rn, t = (H - rn) * (H - rn);
+                    fx += (((rx * s) * t) * 2.0f) * C;
+                    fy += (((ry * s) * t) * 2.0f) * C;
+                    fz += (((rz * s) * t) * 2.0f) * C;
+                }
+            }
+        }
+        const float k = c.mass * bphi[i];
+        fx *= k; fy *= k; fz *= k;
+        const float* t = xf + 20 * bi;
+        const float ex = pi.x - t[3], ey = pi.y - t[7], ez = pi.z - t[11];
+        tx = ey * fz - ez * fy;
+        ty = ez * fx - ex * fz;
+        tz = ex * fy - ey * fx;
+    }
+    /* warp reduction when the warp's particles belong to one body, else one atomic each */
+    const unsigned active = __activemask();
+    const int b0 = __shfl_sync(active, bi, __ffs(active) - 1);
+    const bool uniform = __all_sync(active, bi == b0);
+    if (uniform) {
+        if (b0 < 0) return;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o);
+            fz += __shfl_xor_sync(0xffffffffu, fz, o);
+            tx += __shfl_xor_sync(0xffffffffu, tx, o);
+            ty += __shfl_xor_sync(0xffffffffu, ty, o);
+            tz += __shfl_xor_sync(0xffffffffu, tz, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            float* f = reinterpret_cast<float*>(&body_force[b0]);
+            float* q = reinterpret_cast<float*>(&body_torque[b0]);
+            atomicAdd(f, fx); atomicAdd(f + 1, fy); atomicAdd(f + 2, fz);
+            atomicAdd(q, tx); atomicAdd(q + 1, ty); atomicAdd(q + 2, tz);
+        }
+    } else if (bi >= 0) {
+        float* f = reinterpret_cast<float*>(&body_force[bi]);
+        float* q = reinterpret_cast<float*>(&body_torque[bi]);
+        atomicAdd(f, fx); atomicAdd(f + 1, fy); atomicAdd(f + 2, fz);
+        atomicAdd(q, tx); atomicAdd(q + 1, ty); atomicAdd(q + 2, tz);
+    }
+}
+
+/* stats[0..7]: sum max(e,0), sum |e|, max e (as ordered bits), KE, PE, sum x, y, z */
+__global__ void k_stats(Const c, const float* __restrict__ dens, const float4* __restrict__ pos,
+                        const float4* __restrict__ vel, double* __restrict__ out) {
+    double a[7] = {0, 0, 0, 0, 0, 0, 0};
+    float mx = -3.0e38f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.n; i += gridDim.x * blockDim.x) {
+        const float e = (dens[i] - c.rho0) / c.rho0;
+        a[0] += e > 0.f ? e : 0.f;
+        a[1] += fabsf(e);
+        mx = fmaxf(mx, e);
+        const float4 p = pos[i], v = vel[i];
+        a[2] += 0.5 * (double)c.mass * (double)(v.x * v.x + v.y * v.y + v.z * v.z);
+        a[3] += (double)c.mass * (double)(-c.g) * (double)p.y;
+        a[4] += p.x; a[5] += p.y; a[6] += p.z;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 7; ++k) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out[0], a[0]);
+        atomicAdd(&out[1], a[1]);
+        atomicAdd(&out[3], a[2]);
+        atomicAdd(&out[4], a[3]);
+        atomicAdd(&out[5], a[4]);
+        atomicAdd(&out[6], a[5]);
+        atomicAdd(&out[7], a[6]);
+        /* order-preserving map of the float max into an unsigned slot (out[2] bits) */
+        unsigned u = __float_as_uint(mx);
+        u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        atomicMax(reinterpret_cast<unsigned long long*>(&out[2]), (unsigned long long)u);
+    }
+}
+
+static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
+
+void launch_bnd_transform(cudaStream_t s, const Bufs& b, int nbodies, int nb, bool compat, bool only_movable,
+                          int bs) {
+    if (nb <= 0 || nbodies <= 0) return;
+    k_bnd_transform<<<nblk(nb, bs), bs, 0, s>>>(nb, b.braw, b.bbody, b.body_xf, b.body_range, compat ? 1 : 0,
+                                                only_movable ? 1 : 0, b.bpos, b.bvel);
+}
+void launch_bnd_phi(cudaStream_t s, const Const& c, const Bufs& b, float phi_coeff, int bs) {
+    if (c.nb <= 0) return;
+    k_bnd_phi<<<nblk(c.nb, bs), bs, 0, s>>>(c, c.nb, b.bpos_s, b.bbody_s, b.btab, b.bmask_sorted, phi_coeff,
+                                            b.bphi_s, b.bphi);
+}
+void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs) {
+    if (c.nb <= 0 || nbodies <= 0) return;
+    cudaMemsetAsync(b.body_force, 0, sizeof(float4) * nbodies, s);
+    cudaMemsetAsync(b.body_torque, 0, sizeof(float4) * nbodies, s);
+    k_bnd_forces<<<nblk(c.nb, bs), bs, 0, s>>>(c, c.nb, b.bpos, b.bphi, b.bbody, b.body_range, b.body_xf, b.pos_s,
+                                               b.density, b.pressure, b.tab, b.body_force, b.body_torque);
+}
+void launch_stats(cudaStream_t s, const Const& c, const Bufs& b) {
+    cudaMemsetAsync(b.stats, 0, 8 * sizeof(double), s);
+    if (c.n <= 0) return;
+    int g = nblk(c.n, 256);
+    if (g > 1024) g = 1024;
+    k_stats<<<g, 256, 0, s>>>(c, b.density, b.pos, b.vel, b.stats);
+}
+
+}  // namespace sph

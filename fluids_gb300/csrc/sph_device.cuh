@@ -1,0 +1,196 @@
+/*
+ * sph_device.cuh -- device-side building blocks shared by the SPH kernels (sm_103a).
+ *
+ * Data layout in HBM (one context): structure-of-arrays, particle i of every array is the
+ * same particle, arrays indexed in Morton order of the current step:
+ *   float4 pos/vel/vel_half (x, y, z, w; w = 1 for positions, 0 otherwise), float density,
+ *   pressure, int cell table int2[cells] = [start, end) into the sorted arrays.
+ * The cell coordinate, Morton key and linear cell id follow kernels/grid.h:7-13,74-108 and
+ * kernels/morton.h:37-56; the neighbour traversal order follows grid.h:15-49 (own cell
+ * first, then the 26 offsets), ascending particle index inside a cell, with the
+ * NEIGH_LIST_MAX_LENGTH cap of grid.cl:163-177.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sph {
+
+/* Kernel constants derived on the host (sph_context.cu: derive_constants). */
+struct Const {
+    /* grid: origin, cell size, dimensions; wrap = 1 reproduces grid.h:82-88 */
+    float ox, oy, oz, cell;
+    int nx, ny, nz, wrap;
+    long long ncells;
+    float h2_list;       /* CELL_SIZE^2 of grid.cl:3 (6-decimal -D rounding in COMPAT) */
+    int n, nb, cap, compat;
+    float h, h_def;      /* kernel argument h; SUPPORT_RADIUS -D constant */
+    float mass, mass_def, rho0, rho0_def, kgas, mu, sigma, g;
+    float poly6_eval, poly6_grad, spiky_grad, visc_lapl, st_main, st_term;
+    float default_eval, boundary_eval, delta, bforce_spiky;
+    float dt, vmax, lim_x, lim_y, lim_z;
+    float pci_eta;
+    int pci_min_iter, pci_max_iter;
+    int key_bits;
+    float rmin_wc;       /* largest float <= 1e-5: wcsph.cl:152 compares r > 0.00001 (a double) */
+};
+
+constexpr unsigned kFlagNan = 1u, kFlagEscaped = 2u, kFlagTimeout = 4u, kFlagOverflow = 8u,
+                   kFlagNonconverged = 16u;
+
+/* ---- IEEE helpers that the compiler may not contract into FMAs ---------------------- */
+__device__ __forceinline__ float r2_exact(float dx, float dy, float dz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+/* kernels/morton.h:37-56 with OpenCL C semantics (shift by 32 is a shift by 0; 64-bit
+ * masks truncated to 32 bits). */
+__host__ __device__ __forceinline__ uint32_t split_by_3(uint32_t a) {
+    uint32_t x = a & 0x1fffffu;
+    x = x & 0x0000ffffu;
+    x = (x | (x << 16)) & 0xff0000ffu;
+    x = (x | (x << 8)) & 0x0f00f00fu;
+    x = (x | (x << 4)) & 0xc30c30c3u;
+    x = (x | (x << 2)) & 0x49249249u;
+    return x;
+}
+__host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return (split_by_3(x) | (split_by_3(y) << 1)) | (split_by_3(z) << 2);
+}
+
+/* One axis of get_grid_coordinates (grid.h:74-91): floor((p - origin) / h) with IEEE
+ * subtraction and division; COMPAT wraps modulo n, PHYSICS clamps into [0, n). */
+__device__ __forceinline__ int axis_cell(float p, float o, float h, int n, int wrap) {
+    float f = floorf(__fdiv_rn(__fsub_rn(p, o), h));
+    if (wrap) {
+        if (!(f > -1e9f && f < 1e9f)) f = 0.f;
+        int c = (int)f + n;
+        return c % n;
+    }
+    if (!(f >= 0.f)) return 0;
+    if (f > (float)(n - 1)) return n - 1;
+    return (int)f;
+}
+__device__ __forceinline__ void cell_of(const Const& c, float x, float y, float z, int& cx, int& cy, int& cz) {
+    cx = axis_cell(x, c.ox, c.cell, c.nx, c.wrap);
+    cy = axis_cell(y, c.oy, c.cell, c.ny, c.wrap);
+    cz = axis_cell(z, c.oz, c.cell, c.nz, c.wrap);
+}
+/* CELL_ID (grid.h:7): x + nx * (y + ny * z). */
+__device__ __forceinline__ long long cell_lin(const Const& c, int x, int y, int z) {
+    return (long long)x + (long long)c.nx * ((long long)y + (long long)c.ny * (long long)z);
+}
+/* Linear id of a neighbour cell, false when it is outside the table.  COMPAT keeps the
+ * reference's unchecked linear arithmetic (a -1 / n coordinate reads the adjacent row)
+ * and only rejects ids outside [0, cells); PHYSICS rejects coordinates outside the grid. */
+__device__ __forceinline__ bool neigh_cell(const Const& c, int x, int y, int z, long long& id) {
+    if (c.wrap) {
+        id = cell_lin(c, x, y, z);
+        return id >= 0 && id < c.ncells;
+    }
+    if ((unsigned)x >= (unsigned)c.nx || (unsigned)y >= (unsigned)c.ny || (unsigned)z >= (unsigned)c.nz)
+        return false;
+    id = cell_lin(c, x, y, z);
+    return true;
+}
+/* CELL_NEIGH_OFFSET (grid.h:15-49): o = 0 is the own cell; o = 1..26 enumerate
+ * (dx, dy, dz) in {-1,0,1}^3 \ {0} with dx slowest, dz fastest. */
+__device__ __forceinline__ void neigh_offset(int o, int& dx, int& dy, int& dz) {
+    if (o == 0) { dx = dy = dz = 0; return; }
+    int t = o - 1;
+    t += (t >= 13) ? 1 : 0;
+    dx = t / 9 - 1;
+    dy = (t / 3) % 3 - 1;
+    dz = t % 3 - 1;
+}
+
+/* Visits the neighbours j of a point (px, py, pz) among the particles npos[] binned in
+ * table tab, in the reference's list order, keeping at most c.cap with r^2 < h2_list.
+ * f(j, pj, dx, dy, dz) receives the neighbour and d = p - pj (IEEE, uncontracted). */
+template <class F>
+__device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py, float pz,
+                                              const int2* __restrict__ tab, const float4* __restrict__ npos,
+                                              F&& f) {
+    int cx, cy, cz;
+    cell_of(c, px, py, pz, cx, cy, cz);
+    int cnt = 0;
+#pragma unroll 1
+    for (int o = 0; o < 27 && cnt < c.cap; ++o) {
+        int ox, oy, oz;
+        neigh_offset(o, ox, oy, oz);
+        long long id;
+        if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) continue;
+        const int2 r = __ldg(&tab[id]);
+#pragma unroll 1
+        for (int j = r.x; j < r.y && cnt < c.cap; ++j) {
+            const float4 pj = __ldg(&npos[j]);
+            const float dx = __fsub_rn(px, pj.x), dy = __fsub_rn(py, pj.y), dz = __fsub_rn(pz, pj.z);
+            if (r2_exact(dx, dy, dz) < c.h2_list) {
+                f(j, pj, dx, dy, dz);
+                ++cnt;
+            }
+        }
+    }
+    return cnt;
+}
+
+/* Visits the materialised list of particle i (column-major list[k * n + i], grid.cl:174). */
+template <class F>
+__device__ __forceinline__ void list_neighbors(int i, int n, const int* __restrict__ list, int len,
+                                               const float4* __restrict__ npos, float px, float py, float pz,
+                                               F&& f) {
+#pragma unroll 1
+    for (int k = 0; k < len; ++k) {
+        const int j = __ldg(&list[(size_t)k * n + i]);
+        const float4 pj = __ldg(&npos[j]);
+        f(j, pj, __fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
+    }
+}
+
+/* Neighbour source: either the cell scan or the materialised list, same order. */
+template <bool LIST>
+struct Neigh {
+    const int2* tab;
+    const int* list;
+    const int* len;
+    const float4* npos;
+    template <class F>
+    __device__ __forceinline__ void visit(const Const& c, int i, float px, float py, float pz, F&& f) const {
+        if (LIST) list_neighbors(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
+        else scan_neighbors(c, px, py, pz, tab, npos, f);
+    }
+};
+
+/* pown(x, n) restated as left-to-right repeated multiplication. */
+__device__ __forceinline__ float pown2(float x) { return x * x; }
+__device__ __forceinline__ float pown3(float x) { return (x * x) * x; }
+__device__ __forceinline__ float pown7(float x) {
+    float r = x * x;
+    r = r * x; r = r * x; r = r * x; r = r * x; r = r * x;
+    return r;
+}
+/* kernels/surface_tension.h:23-50 */
+__device__ __forceinline__ float st_corr(float rho0, float di, float dj) { return 2.0f * rho0 / (di + dj); }
+__device__ __forceinline__ float st_kernel(float r, float h, float c) {
+    if (r <= 0.5f * h) {
+        float t1 = h - r;
+        float t2 = (t1 * t1 * t1) * (r * r * r);
+        return 2.0f * t2 - c;
+    } else if (r <= h) {
+        float t1 = h - r;
+        return (t1 * t1 * t1) * (r * r * r);
+    }
+    return 0.0f;
+}
+/* OpenCL clamp = fmin(fmax(x, lo), hi) and sign(). */
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+__device__ __forceinline__ float signf(float x) {
+    if (x > 0.f) return 1.f;
+    if (x < 0.f) return -1.f;
+    if (x != x) return 0.f;
+    return x;
+}
+__device__ __forceinline__ float len3(float x, float y, float z) { return sqrtf(x * x + y * y + z * z); }
+
+
+}  // namespace sph

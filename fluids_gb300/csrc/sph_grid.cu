@@ -1,0 +1,147 @@
+/*
+ * sph_grid.cu -- uniform-grid binning kernels.
+ *
+ *   k_hashes      compute_hashes (kernels/grid.cl:20-39): Morton key + identity mask; also
+ *                 clears the cell-table entries the previous step wrote, so the table never
+ *                 needs the O(cells) fill of fluid/simulation/grid.cpp:41.
+ *   k_gather      clshuffle (opencl/algorithms/clshuffle.h:12-58) for every fluid array in
+ *                 one pass: dst[i] = src[mask[i]].
+ *   k_cell_ranges compute_cell_intervals (kernels/grid.cl:60-123): [start, end) per occupied
+ *                 cell from adjacent sorted keys (neighbours read from L1, no local-memory
+ *                 staging or barrier needed on this hardware).
+ *   k_neigh_lists compute_neigh_list (kernels/grid.cl:145-182) for the fluid and the boundary
+ *                 tables in one launch, column-major list[k * n + i].
+ * All are HBM-streaming kernels (bytes per particle listed in the design doc).
+ */
+#include "sph_kernels.cuh"
+
+namespace sph {
+
+__global__ void k_hashes(Const c, const float4* __restrict__ pos, int n, uint32_t* __restrict__ keys,
+                         int32_t* __restrict__ mask, int2* __restrict__ tab, const int32_t* __restrict__ cell_prev,
+                         unsigned* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (cell_prev) {
+        const int pc = cell_prev[i];
+        if (pc >= 0) tab[pc] = make_int2(0, 0);
+    }
+    const float4 p = pos[i];
+    int cx, cy, cz;
+    cell_of(c, p.x, p.y, p.z, cx, cy, cz);
+    keys[i] = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+    mask[i] = i;
+    if (!c.wrap) {
+        /* PHYSICS grid clamps: report particles outside it (informational) */
+        const float fx = floorf(__fdiv_rn(__fsub_rn(p.x, c.ox), c.cell));
+        const float fy = floorf(__fdiv_rn(__fsub_rn(p.y, c.oy), c.cell));
+        const float fz = floorf(__fdiv_rn(__fsub_rn(p.z, c.oz), c.cell));
+        const bool out = !(fx >= 0.f && fx < (float)c.nx && fy >= 0.f && fy < (float)c.ny && fz >= 0.f &&
+                           fz < (float)c.nz);
+        if (out) atomicOr(flags, kFlagEscaped);
+    }
+}
+
+__global__ void k_gather(int n, const int32_t* __restrict__ perm, const float4* __restrict__ a,
+                         float4* __restrict__ as, const float4* __restrict__ b, float4* __restrict__ bs,
+                         const float4* __restrict__ c3, float4* __restrict__ cs, const int32_t* __restrict__ ids,
+                         int32_t* __restrict__ ids_s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int src = perm[i];
+    as[i] = __ldg(&a[src]);
+    bs[i] = __ldg(&b[src]);
+    if (c3) cs[i] = __ldg(&c3[src]);
+    if (ids) ids_s[i] = __ldg(&ids[src]);
+}
+
+__global__ void k_gather_boundary(int n, const int32_t* __restrict__ perm, const float4* __restrict__ pos,
+                                  float4* __restrict__ pos_s, const int32_t* __restrict__ body,
+                                  int32_t* __restrict__ body_s, const float* __restrict__ phi,
+                                  float* __restrict__ phi_s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int src = perm[i];
+    pos_s[i] = pos[src];
+    body_s[i] = body[src];
+    if (phi) phi_s[i] = phi[src];
+}
+
+__global__ void k_cell_ranges(Const c, const float4* __restrict__ spos, const uint32_t* __restrict__ keys, int n,
+                              int2* __restrict__ tab, int32_t* __restrict__ cell_out, unsigned* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int* t = reinterpret_cast<int*>(tab);
+    const float4 p0 = spos[i];
+    int x, y, z;
+    cell_of(c, p0.x, p0.y, p0.z, x, y, z);
+    const long long id0 = cell_lin(c, x, y, z);
+    const bool ok0 = id0 >= 0 && id0 < c.ncells;
+    if (!ok0) atomicOr(flags, kFlagEscaped);
+    cell_out[i] = ok0 ? (int)id0 : -1;
+    if (i == n - 1) {
+        if (ok0) t[2 * id0 + 1] = i + 1;
+    } else {
+        const uint32_t h0 = keys[i], h1 = keys[i + 1];
+        if (h0 < h1) {
+            const float4 p1 = spos[i + 1];
+            cell_of(c, p1.x, p1.y, p1.z, x, y, z);
+            const long long id1 = cell_lin(c, x, y, z);
+            if (ok0) t[2 * id0 + 1] = i + 1;
+            if (id1 >= 0 && id1 < c.ncells) t[2 * id1] = i + 1;
+        }
+    }
+}
+
+__global__ void k_neigh_lists(Const c, const float4* __restrict__ spos, const int2* __restrict__ tab,
+                              const float4* __restrict__ bpos_s, const int2* __restrict__ btab, int* __restrict__ nlist,
+                              int* __restrict__ nlen, int* __restrict__ sblist, int* __restrict__ sblen) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const float4 pi = spos[i];
+    const size_t n = (size_t)c.n;
+    int k = 0;
+    scan_neighbors(c, pi.x, pi.y, pi.z, tab, spos, [&](int j, float4, float, float, float) {
+        nlist[(size_t)k * n + i] = j;
+        ++k;
+    });
+    nlen[i] = k;
+    int kb = 0;
+    if (c.nb > 0) {
+        scan_neighbors(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float, float, float) {
+            sblist[(size_t)kb * n + i] = j;
+            ++kb;
+        });
+    }
+    sblen[i] = kb;
+}
+
+static inline int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+void launch_hashes(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int32_t* mask,
+                   int2* tab, const int32_t* cell_prev, unsigned* flags, int bs) {
+    if (n <= 0) return;
+    k_hashes<<<blocks_for(n, bs), bs, 0, s>>>(c, pos, n, keys, mask, tab, cell_prev, flags);
+}
+void launch_gather(cudaStream_t s, int n, const int32_t* perm, const float4* a, float4* as, const float4* b,
+                   float4* bs_, const float4* c3, float4* cs, const int32_t* ids, int32_t* ids_s, int bs) {
+    if (n <= 0) return;
+    k_gather<<<blocks_for(n, bs), bs, 0, s>>>(n, perm, a, as, b, bs_, c3, cs, ids, ids_s);
+}
+void launch_gather_boundary(cudaStream_t s, int n, const int32_t* perm, const float4* pos, float4* pos_s,
+                            const int32_t* body, int32_t* body_s, const float* phi, float* phi_s, int bs) {
+    if (n <= 0) return;
+    k_gather_boundary<<<blocks_for(n, bs), bs, 0, s>>>(n, perm, pos, pos_s, body, body_s, phi, phi_s);
+}
+void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, const uint32_t* keys, int n,
+                        int2* tab, int32_t* cell_out, unsigned* flags, int bs) {
+    if (n <= 0) return;
+    k_cell_ranges<<<blocks_for(n, bs), bs, 0, s>>>(c, spos, keys, n, tab, cell_out, flags);
+}
+void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, const int2* tab, const float4* bpos_s,
+                        const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs) {
+    if (c.n <= 0) return;
+    k_neigh_lists<<<blocks_for(c.n, bs), bs, 0, s>>>(c, spos, tab, bpos_s, btab, nlist, nlen, sblist, sblen);
+}
+
+}  // namespace sph

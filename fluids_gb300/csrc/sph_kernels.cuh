@@ -1,0 +1,91 @@
+/*
+ * sph_kernels.cuh -- host-side launchers of the SPH kernels (one per reference launch point).
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+/* Device buffers of one context, passed to the launchers. */
+struct Bufs {
+    /* fluid */
+    float4 *pos, *vel, *vhalf;             /* state between steps */
+    float4 *pos_s, *vel_s, *vhalf_s;       /* this step's sorted copies */
+    float4 *normal, *accel, *pos_pred, *f_other, *f_press;
+    float *density, *pressure, *dens_var;
+    uint32_t *keys, *keys_alt;
+    int32_t *mask, *mask_alt;
+    uint32_t* keys_sorted;                 /* where the sort left the keys */
+    int32_t* mask_sorted;
+    int32_t *ids, *ids_s;
+    int2* tab;                             /* fluid cell table */
+    int32_t* cell_prev;                    /* cell id of each sorted particle (sparse clear) */
+    int32_t *nlist, *nlen, *sblist, *sblen;
+    void* sort_ws;
+    /* boundary */
+    float4 *braw, *bpos, *bvel, *bpos_s;
+    float *bphi, *bphi_s;
+    int32_t *bbody, *bbody_s;
+    uint32_t *bkeys, *bkeys_alt;
+    int32_t *bmask, *bmask_alt;
+    uint32_t* bkeys_sorted;
+    int32_t* bmask_sorted;
+    int2* btab;
+    int32_t* bcell_prev;
+    void* bsort_ws;
+    /* per-body data (device) */
+    float* body_xf;                        /* 20 floats per body: rot3x4, lin4, ang4 */
+    int32_t* body_range;                   /* origin, count, can_move, has_mass per body */
+    float4 *body_force, *body_torque;
+    /* status */
+    unsigned* flags;
+    int32_t* pci_iters;
+    float* pci_maxerr;
+    unsigned* barrier;
+    double* stats;
+};
+
+/* sph_sort.cu */
+int sort_passes(int key_bits);
+size_t sort_workspace_bytes(int n, int key_bits);
+void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t* v1, int n, int key_bits,
+                void* ws, unsigned* flags, int num_sms, uint32_t** kres, int32_t** vres);
+
+/* sph_grid.cu */
+void launch_hashes(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int32_t* mask,
+                   int2* tab, const int32_t* cell_prev, unsigned* flags, int bs);
+void launch_gather(cudaStream_t s, int n, const int32_t* perm, const float4* a, float4* as, const float4* b,
+                   float4* bs_, const float4* c3, float4* cs, const int32_t* ids, int32_t* ids_s, int bs);
+void launch_gather_boundary(cudaStream_t s, int n, const int32_t* perm, const float4* pos, float4* pos_s,
+                            const int32_t* body, int32_t* body_s, const float* phi, float* phi_s, int bs);
+void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, const uint32_t* keys, int n,
+                        int2* tab, int32_t* cell_out, unsigned* flags, int bs);
+void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, const int2* tab, const float4* bpos_s,
+                        const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs);
+
+/* sph_wcsph.cu */
+void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);
+void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);
+void launch_wc_forces(cudaStream_t s, const Const& c, const Bufs& b, bool lists, bool fuse_integrate,
+                      bool write_acc, int bs);
+void launch_wc_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+
+/* sph_pcisph.cu */
+void launch_pci_init_density(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+void launch_pci_init_forces(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+int pci_loop_blocks(int num_sms, int bs);
+cudaError_t launch_pci_loop(cudaStream_t s, const Const& c, const Bufs& b, int min_iter, int max_iter, int blocks,
+                            int bs, bool fuse_integrate);
+void launch_pci_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+
+/* sph_boundary.cu */
+void launch_bnd_transform(cudaStream_t s, const Bufs& b, int nbodies, int nb, bool compat, bool only_movable,
+                          int bs);
+void launch_bnd_phi(cudaStream_t s, const Const& c, const Bufs& b, float phi_coeff, int bs);
+void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs);
+void launch_stats(cudaStream_t s, const Const& c, const Bufs& b);
+
+}  // namespace sph

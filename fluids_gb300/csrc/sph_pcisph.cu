@@ -1,0 +1,334 @@
+/*
+ * sph_pcisph.cu -- PCISPH passes (kernels/pcisph.cl) over the materialised neighbour lists.
+ *
+ *   k_pci_init_density  fill p = 0 (pcisphsimluation.cpp:118) + compute_initial_density
+ *                       (pcisph.cl:33-102)
+ *   k_pci_init_forces   fill F_p = 0 (pcisphsimluation.cpp:126) + compute_initial_forces
+ *                       (pcisph.cl:134-222): viscosity + Akinci surface tension
+ *   k_pci_loop          the whole predict-correct loop of pcisphsimluation.cpp:129-148 in ONE
+ *                       persistent cooperative kernel: predict_pos (pcisph.cl:302-344),
+ *                       update_pressure (:349-418) with a fused block max of the density
+ *                       error (replacing clmax, clreduce.h:54-62, and its blocking read per
+ *                       iteration), compute_pressure_force (:420-504).  The stop test runs on
+ *                       the device after a grid barrier, so no host round trip per iteration.
+ *                       Optionally the final predict_vel_n_pos (:240-284) is fused after it.
+ *   k_pci_integrate     predict_vel_n_pos (pcisph.cl:240-284)
+ * The grid barrier spins on a generation counter with a bounded poll count; on timeout the
+ * kernel sets SPH_FLAG_TIMEOUT and every CTA returns (the launch is cooperative, so all CTAs
+ * are co-resident and the wait ends in practice).
+ */
+#include "sph_kernels.cuh"
+
+namespace sph {
+
+namespace {
+constexpr long long kBarrierSpinLimit = 1LL << 24;
+
+/* Grid-wide barrier: bar[0] = arrivals, bar[1] = generation.  Returns false on timeout. */
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* flags) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        int ok = 1;
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == gen) {
+                if (++spins > kBarrierSpinLimit) {
+                    atomicOr(flags, kFlagTimeout);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ float block_max(float v) {
+    __shared__ float s_w[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) s_w[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? s_w[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
+/* container clamp of both PCISPH integrators */
+__device__ __forceinline__ void pci_advance(const Const& c, float4 p, float4 v, float4 fo, float4 fp, float& px,
+                                            float& py, float& pz, float& vx, float& vy, float& vz, float& cx,
+                                            float& cy, float& cz, float& d, float& vn) {
+    const float md = c.mass_def, dt = c.dt, vm = c.vmax;
+    const float ax = (fp.x + fo.x) / md, ay = c.g + (fp.y + fo.y) / md, az = (fp.z + fo.z) / md;
+    vx = v.x + clampf(ax * dt, -vm, vm);
+    vy = v.y + clampf(ay * dt, -vm, vm);
+    vz = v.z + clampf(az * dt, -vm, vm);
+    px = p.x + vx * dt;
+    py = p.y + vy * dt;
+    pz = p.z + vz * dt;
+    vn = len3(vx, vy, vz);
+    cx = clampf(px, (-c.lim_x) / 2.0f, c.lim_x / 2.0f);
+    cy = clampf(py, (-c.lim_y) / 2.0f, 10.0f);
+    cz = clampf(pz, (-c.lim_z) / 2.0f, c.lim_z / 2.0f);
+    d = len3(cx - px, cy - py, cz - pz);
+}
+
+__device__ __forceinline__ void pci_predict_one(const Const& c, const Bufs& b, int i) {
+    float px, py, pz, vx, vy, vz, cx, cy, cz, d, vn;
+    pci_advance(c, __ldg(&b.pos_s[i]), __ldg(&b.vel_s[i]), b.f_other[i], b.f_press[i], px, py, pz, vx, vy, vz, cx,
+                cy, cz, d, vn);
+    if (d > 0.f && vn > 0.f) { px = cx; py = cy; pz = cz; }
+    b.pos_pred[i] = make_float4(px, py, pz, 1.f);
+}
+
+__device__ __forceinline__ void pci_integrate_one(const Const& c, const Bufs& b, int i) {
+    float px, py, pz, vx, vy, vz, cx, cy, cz, d, vn;
+    pci_advance(c, __ldg(&b.pos_s[i]), __ldg(&b.vel_s[i]), b.f_other[i], b.f_press[i], px, py, pz, vx, vy, vz, cx,
+                cy, cz, d, vn);
+    if (d > 0.f && vn > 0.f) {
+        float sx = signf(cx - px), sy = signf(cy - py), sz = signf(cz - pz);
+        const float sl = len3(sx, sy, sz);
+        sx /= sl; sy /= sl; sz /= sl;
+        const float rest = d / (c.dt * vn);
+        const float k = (1.0f + rest) * (vx * sx + vy * sy + vz * sz);
+        vx -= k * sx; vy -= k * sy; vz -= k * sz;
+        px = cx; py = cy; pz = cz;
+    }
+    b.pos[i] = make_float4(px, py, pz, 1.f);
+    b.vel[i] = make_float4(vx, vy, vz, 0.f);
+    b.ids[i] = b.ids_s[i];
+    const bool bad = !(isfinite(px) && isfinite(py) && isfinite(pz) && isfinite(vx) && isfinite(vy) && isfinite(vz));
+    if (bad) atomicOr(b.flags, kFlagNan);
+}
+
+/* update_pressure for one particle: predicted density from the fixed lists at x*. */
+template <bool COMPAT>
+__device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, int i) {
+    const float4 pi = b.pos_pred[i];
+    const float H = c.h_def, HH = H * H;
+    const size_t n = (size_t)c.n;
+    float pd = 0.f, pdb = 0.f;
+    const int len = __ldg(&b.nlen[i]);
+    for (int k = 0; k < len; ++k) {
+        const int j = __ldg(&b.nlist[k * n + i]);
+        const float4 pj = b.pos_pred[j];
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (COMPAT || r2 < HH) { const float t = HH - r2; pd += (t * t) * t; }
+    }
+    pd *= c.default_eval * c.mass_def;
+    const int blen = __ldg(&b.sblen[i]);
+    for (int k = 0; k < blen; ++k) {
+        const int j = __ldg(&b.sblist[k * n + i]);
+        const float4 pj = __ldg(&b.bpos_s[j]);
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (COMPAT || r2 < HH) { const float t = HH - r2; pdb += ((t * t) * t) * __ldg(&b.bphi_s[j]); }
+    }
+    pdb *= c.default_eval;
+    const float e = pd + pdb - c.rho0_def;
+    const float dv = (0.f < e) ? e : 0.f;
+    b.dens_var[i] = dv;
+    b.pressure[i] += dv * c.delta;
+    return dv;
+}
+
+/* compute_pressure_force for one particle (initial density, updated pressure). */
+__device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Bufs& b, int i) {
+    const float4 pi = __ldg(&b.pos_s[i]);
+    const float H = c.h_def;
+    const size_t n = (size_t)c.n;
+    const float di = __ldg(&b.density[i]), p_i = b.pressure[i];
+    const float C = p_i / (di * di);
+    float fx = 0.f, fy = 0.f, fz = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+    const int len = __ldg(&b.nlen[i]);
+    for (int k = 0; k < len; ++k) {
+        const int j = __ldg(&b.nlist[k * n + i]);
+        const float4 pj = __ldg(&b.pos_s[j]);
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float l = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (l >= 1e-5f) {
+            const float dj = __ldg(&b.density[j]);
+            const float q = C + b.pressure[j] / (dj * dj);
+            const float il = 1.0f / l, t = (H - l) * (H - l);
+            fx += q * ((dx * il) * t);
+            fy += q * ((dy * il) * t);
+            fz += q * ((dz * il) * t);
+        }
+    }
+    const float sf = (-(c.mass_def * c.mass_def)) * c.spiky_grad;
+    fx *= sf; fy *= sf; fz *= sf;
+    const int blen = __ldg(&b.sblen[i]);
+    for (int k = 0; k < blen; ++k) {
+        const int j = __ldg(&b.sblist[k * n + i]);
+        const float4 pj = __ldg(&b.bpos_s[j]);
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float l = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float q = __ldg(&b.bphi_s[j]) * (2.0f * C);
+        const float il = 1.0f / l, t = (H - l) * (H - l);
+        gx += q * ((dx * il) * t);
+        gy += q * ((dy * il) * t);
+        gz += q * ((dz * il) * t);
+    }
+    const float sb = (-c.mass_def) * c.spiky_grad;
+    b.f_press[i] = make_float4(fx + gx * sb, fy + gy * sb, fz + gz * sb, 0.f);
+}
+}  // namespace
+
+template <bool COMPAT>
+__global__ void __launch_bounds__(256) k_pci_init_density(Const c, Bufs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    b.pressure[i] = 0.f;
+    const float4 pi = __ldg(&b.pos_s[i]);
+    const float H = c.h_def, HH = H * H;
+    float di = 0.f, bdi = 0.f;
+    list_neighbors(i, c.n, b.nlist, __ldg(&b.nlen[i]), b.pos_s, pi.x, pi.y, pi.z,
+                   [&](int, float4, float dx, float dy, float dz) {
+                       const float t = HH - (dx * dx + dy * dy + dz * dz);
+                       di += (t * t) * t;
+                   });
+    list_neighbors(i, c.n, b.sblist, __ldg(&b.sblen[i]), b.bpos_s, pi.x, pi.y, pi.z,
+                   [&](int j, float4, float dx, float dy, float dz) {
+                       const float t = HH - (dx * dx + dy * dy + dz * dz);
+                       bdi += ((t * t) * t) * __ldg(&b.bphi_s[j]);
+                   });
+    b.density[i] = c.default_eval * ((di * c.mass_def) + bdi);
+}
+
+__global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    b.f_press[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 pi = __ldg(&b.pos_s[i]), vi = __ldg(&b.vel_s[i]), ni = __ldg(&b.normal[i]);
+    const float di = __ldg(&b.density[i]);
+    const float H = c.h_def;
+    float vx = 0.f, vy = 0.f, vz = 0.f, ux = 0.f, uy = 0.f, uz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f;
+    list_neighbors(i, c.n, b.nlist, __ldg(&b.nlen[i]), b.pos_s, pi.x, pi.y, pi.z,
+                   [&](int j, float4, float dx, float dy, float dz) {
+                       const float4 vj = __ldg(&b.vel_s[j]), nj = __ldg(&b.normal[j]);
+                       const float dj = __ldg(&b.density[j]);
+                       const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
+                       const float w = (H - rn) / dj;
+                       vx += (vj.x - vi.x) * w;
+                       vy += (vj.y - vi.y) * w;
+                       vz += (vj.z - vi.z) * w;
+                       const float K = st_corr(c.rho0_def, di, dj);
+                       ux += (ni.x - nj.x) * K;
+                       uy += (ni.y - nj.y) * K;
+                       uz += (ni.z - nj.z) * K;
+                       const float sk = st_kernel(rn, H, c.st_term);
+                       const float inv = rn > 0.f ? 1.0f / rn : 0.f;
+                       ox += ((dx * inv) * sk) * K;
+                       oy += ((dy * inv) * sk) * K;
+                       oz += ((dz * inv) * sk) * K;
+                   });
+    const float md = c.mass_def;
+    const float vsc = (c.mu * (md * md)) * (c.visc_lapl / di);
+    const float csc = md * c.st_main;
+    const float tsc = (-c.sigma) * md;
+    b.f_other[i] = make_float4(vx * vsc + tsc * (ux + ox * csc), vy * vsc + tsc * (uy + oy * csc),
+                               vz * vsc + tsc * (uz + oz * csc), 0.f);
+}
+
+template <bool COMPAT, bool FUSE_INTEGRATE>
+__global__ void __launch_bounds__(256) k_pci_loop(Const c, Bufs b, int min_iter, int max_iter) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    const int n = c.n;
+    int it = 1;
+    for (; it <= max_iter; ++it) {
+        for (int i = tid; i < n; i += stride) pci_predict_one(c, b, i);
+        if (!grid_barrier(b.barrier, b.flags)) return;
+        float lmax = 0.f;
+        for (int i = tid; i < n; i += stride) lmax = fmaxf(lmax, pci_update_one<COMPAT>(c, b, i));
+        lmax = block_max(lmax);
+        if (threadIdx.x == 0) atomicMax(reinterpret_cast<unsigned*>(&b.pci_maxerr[it - 1]), __float_as_uint(lmax));
+        if (!grid_barrier(b.barrier, b.flags)) return;
+        const float mx = *reinterpret_cast<volatile float*>(&b.pci_maxerr[it - 1]);
+        for (int i = tid; i < n; i += stride) pci_pressure_force_one(c, b, i);
+        bool stop = false;
+        if (it >= min_iter) {
+            const float crit = COMPAT ? (mx - c.rho0) / c.rho0 : mx / c.rho0;
+            stop = crit < c.pci_eta;
+        }
+        if (stop) break;
+    }
+    if (tid == 0) {
+        b.pci_iters[0] = it > max_iter ? max_iter : it;
+        if (it > max_iter && !COMPAT) atomicOr(b.flags, kFlagNonconverged);
+    }
+    if (FUSE_INTEGRATE) {
+        for (int i = tid; i < n; i += stride) pci_integrate_one(c, b, i);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_pci_integrate(Const c, Bufs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    pci_integrate_one(c, b, i);
+}
+
+static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
+
+void launch_pci_init_density(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    if (c.compat) k_pci_init_density<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+    else k_pci_init_density<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+}
+void launch_pci_init_forces(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    k_pci_init_forces<<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+}
+
+static void* loop_fn(bool compat, bool fuse) {
+    if (compat) return fuse ? (void*)k_pci_loop<true, true> : (void*)k_pci_loop<true, false>;
+    return fuse ? (void*)k_pci_loop<false, true> : (void*)k_pci_loop<false, false>;
+}
+
+int pci_loop_blocks(int num_sms, int bs) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pci_loop<false, true>, bs, 0);
+    int per_sm2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_pci_loop<true, false>, bs, 0);
+    per_sm = per_sm < per_sm2 ? per_sm : per_sm2;
+    if (per_sm < 1) per_sm = 1;
+    return per_sm * num_sms;
+}
+
+cudaError_t launch_pci_loop(cudaStream_t s, const Const& c, const Bufs& b, int min_iter, int max_iter, int blocks,
+                            int bs, bool fuse) {
+    if (c.n <= 0) return cudaSuccess;
+    int need = nblk(c.n, bs);
+    if (blocks > need) blocks = need;
+    if (blocks < 1) blocks = 1;
+    Const cc = c;
+    Bufs bb = b;
+    int mi = min_iter, ma = max_iter;
+    void* args[] = {&cc, &bb, &mi, &ma};
+    return cudaLaunchCooperativeKernel(loop_fn(c.compat != 0, fuse), dim3(blocks), dim3(bs), args, 0, s);
+}
+
+void launch_pci_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    k_pci_integrate<<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+}
+
+}  // namespace sph

@@ -1,0 +1,92 @@
+"""The benchmark scenes, built from seeded synthetic inputs with the shapes the benchmark
+configurations name (no dataset is involved).
+
+    dam_break_65k   WCSPH dam break, 32x64x32 lattice at dx = 0.015 m, 2x1x1 m container
+    pcisph_cube     PCISPH double block (2 x 0.5x1.0x0.7 m at dx = 0.0125 m) + rotated 0.3 m cube
+    double_dam_4m   WCSPH double dam break, 2 x 128^3 at dx = 0.005 m (4,194,304 particles)
+
+Each returns a dict: params (capi.SphParams), fluid (n, 4), velocities or None, bodies
+[(points, rot3x4, can_move, mass)], container (w, h, d), steps, plus descriptive fields.
+"""
+import numpy as np
+
+from . import capi
+from .scenes import BoxVolume, Cube, FishTank, jitter, lattice_block, rotation_y
+
+REST_DENSITY = 1000.0
+GAMMA = 7.0
+
+
+def tait_stiffness(c0, rho0=REST_DENSITY, gamma=GAMMA):
+    """Tait EOS stiffness k = rho0 c0^2 / gamma."""
+    return rho0 * c0 * c0 / gamma
+
+
+def wcsph_params(dx, dt, mode=capi.SPH_MODE_PHYSICS, c0=20.0, mu=0.01, sigma=0.001, vmax=10.0, **kw):
+    p = capi.make_params(capi.SPH_WCSPH, mode=mode, time_step=dt, max_vel=vmax, particle_radius=dx / 2.0,
+                         support_radius=2.0 * dx, rest_density=REST_DENSITY, k_viscosity=mu, gravity=9.81,
+                         gas_stiffness=tait_stiffness(c0), surface_tension=sigma)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _tank(container, dx):
+    t = FishTank(*container)
+    return (t.surface_sampling(dx), t.rot3x4(), 0, 0.0)
+
+
+def dam_break(nx, ny, nz, dx, container=(2.0, 1.0, 1.0), seed=0, amp=1e-4):
+    """A lattice block resting on the floor against the +x wall (one spacing from each)."""
+    W, H, D = container
+    lo = (W / 2 - nx * dx, -H / 2 + dx, -(nz - 1) * dx / 2)
+    return jitter(lattice_block(nx, ny, nz, dx, lo), amp, seed)
+
+
+def dam_break_65k(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=1000, **kw):
+    dx, container = 0.015, (2.0, 1.0, 1.0)
+    fluid = dam_break(32, 64, 32, dx, container, seed)
+    return dict(name="wcsph_dam_break_65536", params=wcsph_params(dx, 2e-4, mode, **kw), fluid=fluid,
+                velocities=None, bodies=[_tank(container, dx)], container=container, steps=steps, dx=dx)
+
+
+def double_dam_4m(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=200, n=128, **kw):
+    """Two n^3 blocks flush with the floor at x in [-1, -0.36] and [0.36, 1] (n = 128)."""
+    dx, container = 0.005, (2.0, 1.0, 1.0)
+    W, H, D = container
+    a = lattice_block(n, n, n, dx, (-W / 2 + dx, -H / 2 + dx, -(n - 1) * dx / 2))
+    b = lattice_block(n, n, n, dx, (W / 2 - n * dx, -H / 2 + dx, -(n - 1) * dx / 2))
+    fluid = jitter(np.concatenate([a, b]), 1e-4, seed)
+    return dict(name="wcsph_double_dam_break_%d" % len(fluid), params=wcsph_params(dx, 5e-5, mode, **kw),
+                fluid=fluid, velocities=None, bodies=[_tank(container, dx)], container=container, steps=steps,
+                dx=dx)
+
+
+def pcisph_cube(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=500, dx=0.0125, **kw):
+    """Two 0.5x1.0x0.7 m BoxVolumes at (+-0.74, dx, -0.1) (raised one spacing so the bottom
+    layer does not sit on the floor's boundary particles) and a static 0.3 m cube at
+    (0, -0.35, 0) rotated 0.5 rad about y."""
+    container = (2.0, 1.0, 1.0)
+    r = dx / 2.0
+    vols = [BoxVolume((0.5, 1.0, 0.7), (0.74, dx, -0.1)), BoxVolume((0.5, 1.0, 0.7), (-0.74, dx, -0.1))]
+    fluid = jitter(np.concatenate([v.particles(r) for v in vols]), 1e-4, seed)
+    cube = Cube(0.3, 0.0, (0.0, -0.35, 0.0), rotation_y(0.5))
+    p = capi.make_params(capi.SPH_PCISPH, mode=mode, time_step=5e-4, max_vel=20.0, particle_radius=r,
+                         support_radius=2.0 * dx, pcisph_min_iterations=3, pcisph_max_iterations=8,
+                         pcisph_error_ratio=0.01, rest_density=REST_DENSITY, k_viscosity=1.7, gravity=9.81,
+                         surface_tension=1.0, relax_on_add=0)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    bodies = [_tank(container, dx), (cube.surface_sampling(dx), cube.rot3x4(), 0, 0.0)]
+    return dict(name="pcisph_double_block_cube_%d" % len(fluid), params=p, fluid=fluid, velocities=None,
+                bodies=bodies, container=container, steps=steps, dx=dx)
+
+
+def build_context(w, params=None):
+    """Creates a context and loads a workload: limits, boundaries, then the fluid."""
+    ctx = capi.Context(params if params is not None else w["params"])
+    ctx.set_rect_limits(*w["container"])
+    for pts, rot, mv, mass in w["bodies"]:
+        ctx.add_boundary(pts, can_move=mv, rot3x4=rot, mass=mass)
+    ctx.add_volume(w["fluid"], w.get("velocities"))
+    return ctx

@@ -1,0 +1,241 @@
+/*
+ * sph_capi.h -- C ABI of the GB300 SPH particle pipeline (libsph_gb300.so).
+ *
+ * Drop-in boundary for the per-step particle pipeline of paivett/fluids: the reference's
+ * C++ solver classes (fluid/simulation/wcsphsimluation.cpp, pcisphsimluation.cpp,
+ * grid.cpp, boundaryhandler.cpp) call these entry points in place of their OpenCL kernel
+ * launches (clEnqueueNDRangeKernel / CLKernel::run), clsort, clshuffle, clmax and clsum.
+ * Plain C types only: host arrays are float[4*n] (x, y, z, w) as the reference's cl_float4
+ * buffers; device pointers are returned as void*.
+ *
+ * Every function returns SPH_OK (0) or an SPH_E_* status; sph_last_error() describes the
+ * last failure.  A context owns one CUDA stream and is not thread-safe; distinct contexts
+ * may be driven from different threads.
+ */
+#ifndef SPH_CAPI_H
+#define SPH_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_CAPI_VERSION 1
+
+/* Status codes.  Replace CLError::check's exceptions (opencl/clerror.cpp:15-19). */
+enum sph_status {
+    SPH_OK = 0,
+    SPH_E_INVALID = 1,       /* bad argument or parameter */
+    SPH_E_CUDA = 2,          /* a CUDA runtime call failed */
+    SPH_E_NONCONVERGED = 3,  /* PCISPH stopped at max iterations above the error ratio */
+    SPH_E_ESCAPED = 4,       /* a particle left the grid (PHYSICS grid clamps it) */
+    SPH_E_NAN = 5,           /* a non-finite position or velocity was produced */
+    SPH_E_TIMEOUT = 6,       /* a bounded device wait gave up */
+    SPH_E_OVERFLOW = 7,      /* a size limit was exceeded */
+    SPH_E_STATE = 8,         /* call not valid in the current state */
+    SPH_E_NOMEM = 9          /* device allocation failed */
+};
+
+/* Device status word bits (sph_device_flags). */
+enum sph_flag {
+    SPH_FLAG_NAN = 1u,
+    SPH_FLAG_ESCAPED = 2u,
+    SPH_FLAG_TIMEOUT = 4u,
+    SPH_FLAG_OVERFLOW = 8u,
+    SPH_FLAG_NONCONVERGED = 16u
+};
+
+enum sph_method { SPH_WCSPH = 0, SPH_PCISPH = 1 };
+
+/* COMPAT follows the reference kernel text (including its defects) for stage parity;
+ * PHYSICS applies the documented fixes P1..P7 (container-fitted grid, mass-consistent
+ * forces, 315 poly6 normalisation, PCISPH stop test). */
+enum sph_mode { SPH_MODE_COMPAT = 0, SPH_MODE_PHYSICS = 1 };
+
+/* Neighbour access: scan the 27 cells in every pass, or materialise per-particle lists
+ * once per step (grid.cl:145-182 layout, column-major).  PCISPH always uses lists. */
+enum sph_neighbors { SPH_NEIGH_SCAN = 0, SPH_NEIGH_LIST = 1 };
+
+/* Solver parameters: the union of SimulationSettings (settings/simulationsettings.h) and
+ * PhysicsSettings (settings/physicssettings.h) plus the grid constants the reference fixes
+ * in code (wcsphsimluation.cpp:26 grid side 5.0, common.h:4 list cap 50). */
+typedef struct sph_params {
+    int method;                      /* sph_method */
+    int mode;                        /* sph_mode */
+    float time_step;                 /* s */
+    float max_vel;                   /* m/s, per-component clamp */
+    float particle_radius;           /* m; lattice spacing = 2 * radius */
+    float support_radius;            /* h, m; also the grid cell size */
+    int pcisph_min_iterations;       /* pcisphsimluation.h:254 (3) */
+    int pcisph_max_iterations;
+    float pcisph_error_ratio;        /* eta */
+    int pcisph_relax_max_iterations; /* pcisphsimluation.cpp:549 (10000) */
+    float rest_density;              /* kg/m^3 */
+    float k_viscosity;
+    float gravity;                   /* m/s^2, acts along -y */
+    float gas_stiffness;             /* Tait k (WCSPH) */
+    float surface_tension;
+    float grid_size;                 /* COMPAT: cube side centred at the origin (5.0) */
+    float grid_margin;               /* PHYSICS: cells of margin around the container (2) */
+    float boundary_phi_coeff;        /* BoundaryHandler phi coefficient (1.0) */
+    int neigh_cap;                   /* neighbours kept per particle (50) */
+    int relax_on_add;                /* PCISPH: relaxation step then v := 0 after add_volume */
+    int neighbor_mode;               /* sph_neighbors (WCSPH only) */
+    int use_graph;                   /* capture a step in a CUDA graph (1) */
+    int block_size;                  /* threads per block of particle kernels (32..256), 0 = 256 */
+} sph_params;
+
+typedef struct sph_ctx sph_ctx;
+
+/* Field ids for sph_get_field / sph_set_field / sph_field_device_ptr.  "Sorted" arrays are in
+ * this step's Morton order; POS/VEL/VEL_HALF hold the state between steps, in the previous
+ * step's sorted order, as the reference's unsorted buffers do (wcsphsimluation.cpp:270-279). */
+enum sph_field {
+    SPH_F_POS = 0, SPH_F_VEL = 1, SPH_F_VEL_HALF = 2,
+    SPH_F_POS_SORTED = 3, SPH_F_VEL_SORTED = 4, SPH_F_VEL_HALF_SORTED = 5,
+    SPH_F_HASHES = 6, SPH_F_MASK = 7, SPH_F_CELL_INTERVALS = 8,
+    SPH_F_NEIGH_LIST = 9, SPH_F_NEIGH_LEN = 10, SPH_F_SB_NEIGH_LIST = 11, SPH_F_SB_NEIGH_LEN = 12,
+    SPH_F_DENSITY = 13, SPH_F_PRESSURE = 14, SPH_F_NORMAL = 15, SPH_F_ACCEL = 16,
+    SPH_F_POS_PRED = 17, SPH_F_FORCE_OTHER = 18, SPH_F_FORCE_PRESSURE = 19, SPH_F_DENS_VAR = 20,
+    SPH_F_BPOS_SORTED = 21, SPH_F_BPHI_SORTED = 22, SPH_F_BCELL_INTERVALS = 23,
+    SPH_F_BHASHES = 24, SPH_F_BMASK = 25, SPH_F_BPHI = 26, SPH_F_BPOS = 27,
+    SPH_F_BODY_FORCE = 28, SPH_F_BODY_TORQUE = 29, SPH_F_PCI_ITERS = 30, SPH_F_PCI_MAXERR = 31,
+    SPH_F_ID = 32, SPH_F_COUNT = 33
+};
+/* Element kinds returned by sph_field_kind. */
+enum sph_kind { SPH_KIND_F32 = 0, SPH_KIND_I32 = 1, SPH_KIND_U32 = 2 };
+
+/* Stage ids for sph_run_stage: one call per reference launch point. */
+enum sph_stage {
+    SPH_S_BOUNDARY_SYNC = 0,    /* BoundaryHandler::sync (boundaryhandler.cpp:251-294) */
+    SPH_S_HASHES = 1,           /* Grid::compute_hashes (grid.cpp:22-34; grid.cl:20-39) */
+    SPH_S_SORT = 2,             /* clsort<cl_uint,cl_int> (opencl/algorithms/clsort.h:13-35) */
+    SPH_S_SHUFFLE = 3,          /* clshuffle<cl_float4> x3 / x2 (clshuffle.h:12-58) */
+    SPH_S_CELL_INTERVALS = 4,   /* Grid::compute_cell_intervals (grid.cpp:36-55; grid.cl:60-123) */
+    SPH_S_NEIGH_LIST = 5,       /* Grid::compute_neigh_list (grid.cpp:97-115; grid.cl:145-182) */
+    SPH_S_SB_NEIGH_LIST = 6,    /* BoundaryHandler::build_neighbourhood (boundaryhandler.cpp:351-371) */
+    SPH_S_WC_DENSITY = 7,       /* compute_density_pressure (wcsph.cl:32-79) */
+    SPH_S_NORMALS = 8,          /* compute_normals (normals.cl:23-70) */
+    SPH_S_WC_ACCEL = 9,         /* compute_acceleration (wcsph.cl:81-173) */
+    SPH_S_WC_INTEGRATE = 10,    /* predict_vel_n_pos (wcsph.cl:176-224) */
+    SPH_S_PCI_INIT_DENSITY = 11,/* fill p = 0 + compute_initial_density (pcisph.cl:33-102) */
+    SPH_S_PCI_INIT_FORCES = 12, /* fill F_p = 0 + compute_initial_forces (pcisph.cl:134-222) */
+    SPH_S_PCI_LOOP = 13,        /* predict/update/force loop + clmax (pcisphsimluation.cpp:129-148) */
+    SPH_S_PCI_INTEGRATE = 14,   /* predict_vel_n_pos (pcisph.cl:240-284) */
+    SPH_S_BOUNDARY_FORCES = 15  /* BoundaryHandler::apply_fluid_forces (boundaryhandler.cpp:296-349) */
+};
+
+/* ---- parameters and lifetime ------------------------------------------------------ */
+
+/* Fills *out with the defaults of the reference's config.wc (method SPH_WCSPH) or
+ * config.pci (SPH_PCISPH) in COMPAT mode. */
+void sph_default_params(int method, sph_params* out);
+
+/* Creates a solver.  Replaces WCSPHSimulation / PCISPHSimulation construction
+ * (wcsphsimluation.cpp:15-34, pcisphsimluation.cpp:19-62, fluidsimulationfactory.h:13-40). */
+int sph_create(const sph_params* params, sph_ctx** out);
+/* Releases the context and its device memory (wcsphsimluation.cpp:284-308). */
+int sph_destroy(sph_ctx* ctx);
+/* Text of the last failure on ctx (or of the last failed sph_create when ctx is NULL). */
+const char* sph_last_error(const sph_ctx* ctx);
+/* FluidSimulation::reset (fluidsimulation.h:47-48): new parameters, particles rebuilt from
+ * the volumes and boundaries added so far. */
+int sph_reset(sph_ctx* ctx, const sph_params* params);
+/* Runs work on a caller stream (cudaStream_t) instead of the context's own stream. */
+int sph_set_stream(sph_ctx* ctx, void* cuda_stream);
+
+/* ---- scene -------------------------------------------------------------------------- */
+
+/* FluidSimulation::set_rect_limits (fluidsimulation.h:79; wcsphsimluation.cpp:407-414). */
+int sph_set_rect_limits(sph_ctx* ctx, float width, float height, float depth);
+/* FluidSimulation::add_volume (fluidsimulation.h:91): appends n particles (host pos4; vel4
+ * may be NULL for rest) and re-initialises the solver (wcsphsimluation.cpp:386-405). */
+int sph_add_volume(sph_ctx* ctx, const float* pos4, const float* vel4, int n);
+/* FluidSimulation::add_boundary (fluidsimulation.h:66-68; boundaryhandler.cpp:95-153):
+ * n sampled surface particles in body coordinates, the body's rigid transform rot3x4
+ * (row-major 3x4, NULL = identity), linear/angular velocity lin4/ang4 (NULL = 0) and mass
+ * (fluid forces are accumulated for mass > 0). */
+int sph_add_boundary(sph_ctx* ctx, const float* pos4, int n, int can_move, const float* rot3x4,
+                     const float* lin4, const float* ang4, float mass);
+/* Updates a body's transform and velocities before the next sync (RigidBody state read by
+ * boundaryhandler.cpp:259-274). */
+int sph_set_body_transform(sph_ctx* ctx, int body, const float* rot3x4, const float* lin4,
+                           const float* ang4);
+/* FluidSimulation::particle_count / boundary_particle_count (fluidsimulation.h:54,84). */
+int sph_particle_count(const sph_ctx* ctx);
+int sph_boundary_particle_count(const sph_ctx* ctx);
+
+/* ---- stepping ------------------------------------------------------------------------ */
+
+/* FluidSimulation::simulate (fluidsimulation.h:36) called nsteps times; asynchronous on the
+ * context stream (a CUDA graph per step when use_graph = 1). */
+int sph_simulate(sph_ctx* ctx, int nsteps);
+/* Runs one stage (one reference launch point) on the current state. */
+int sph_run_stage(sph_ctx* ctx, int stage);
+/* Waits for the context stream. */
+int sph_synchronize(sph_ctx* ctx);
+/* Reads (and with clear = 1 resets) the device status word; synchronises. */
+int sph_device_flags(sph_ctx* ctx, unsigned* flags, int clear);
+
+/* ---- buffers ------------------------------------------------------------------------- */
+
+/* Number of scalar elements of a field (float4 fields count 4 per particle). */
+long long sph_field_elems(const sph_ctx* ctx, int field);
+/* sph_kind of a field. */
+int sph_field_kind(int field);
+/* Copies a field to / from host memory (bytes must equal elems * 4); synchronises. */
+int sph_get_field(sph_ctx* ctx, int field, void* host, size_t bytes);
+int sph_set_field(sph_ctx* ctx, int field, const void* host, size_t bytes);
+/* Device address of a field (replaces the cl_mem / GL VBO buffers of clallocator.h). */
+int sph_field_device_ptr(sph_ctx* ctx, int field, void** dptr);
+/* Sum of fluid force / torque per body (boundaryhandler.cpp:338-346), float[4*bodies]. */
+int sph_body_forces(sph_ctx* ctx, float* force4, float* torque4, int bodies);
+/* Rollout statistics of the last step, out[8]: mean max(rho-rho0,0)/rho0, mean
+ * |rho-rho0|/rho0, max (rho-rho0)/rho0, kinetic energy, potential energy (m g y), centre
+ * of mass x, y, z.  Computed on the device; synchronises. */
+int sph_stats(sph_ctx* ctx, double* out8);
+
+/* ---- primitives ---------------------------------------------------------------------- */
+
+/* clsort<cl_uint, cl_int> (opencl/algorithms/clsort.h:13-35): stable ascending sort of n
+ * (key, value) pairs in place in device memory, on the low key_bits bits (1..32) of the
+ * key.  Scratch memory is allocated on first use and cached per device. */
+int sph_sort_pairs(uint32_t* d_keys, int32_t* d_vals, int n, int key_bits, void* cuda_stream);
+
+/* ---- scene builders (host) ------------------------------------------------------------ */
+
+/* BoxVolume::particles (fluid/simulation/boxvolume.cpp:11-40): fills out4 (capacity cap
+ * particles, may be NULL to count) and returns the particle count. */
+int sph_scene_box_volume(const float size3[3], const float center3[3], float particle_radius,
+                         float* out4, int cap);
+/* FishTank::surface_sampling (scene/fishtank.cpp:108-141): container base and four walls,
+ * open top. */
+int sph_scene_fishtank(float width, float height, float depth, float spacing, float* out4, int cap);
+/* Cube::surface_sampling (scene/cube.cpp:136-171): hollow cube shell in body coordinates. */
+int sph_scene_cube(float side, float spacing, float* out4, int cap);
+/* Adds U(-amp, amp) to x, y, z of every particle from a splitmix64 stream seeded by seed. */
+void sph_jitter(float* pos4, int n, float amp, uint64_t seed);
+
+/* Whether a CUDA device is visible (does not create a context on failure paths). */
+int sph_cuda_available(void);
+
+/* Constants a context derives from params and a container (host only, no GPU needed):
+ * the kernel constants of wcsphsimluation.cpp:165-202 / pcisphsimluation.cpp:230-278,429-469
+ * and the grid of grid.cpp:61-68 (Grid::info, grid.h:66-118). */
+typedef struct sph_derived {
+    float mass, mass_def, h, h_def, rest_density_def;
+    float poly6_eval, poly6_grad, spiky_grad, visc_lapl, st_main, st_term;
+    float default_eval, boundary_eval, pci_delta;
+    float grid_origin[3];
+    int grid_dims[3];
+    int grid_wrap;
+    int key_bits;
+} sph_derived;
+int sph_describe(const sph_params* params, const float container3[3], sph_derived* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPH_CAPI_H */

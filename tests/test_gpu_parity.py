@@ -1,0 +1,175 @@
+"""Parity of the CUDA path with the oracle, stage by stage, on the same seeded inputs.
+
+Integer stages (Morton keys, mask, sort permutation, cell ranges, neighbour lists) must be
+bit-exact; FP32 fields must agree within 1e-5 field-relative (parity_util.RTOL)."""
+import numpy as np
+import pytest
+
+from fluids_gb300 import capi
+from parity_util import assert_close, make_pair
+from scenes_np import small_scene
+
+pytestmark = pytest.mark.gpu
+
+GRID = ["BOUNDARY_SYNC", "HASHES", "SORT", "SHUFFLE", "CELL_INTERVALS"]
+
+
+def small_params(method, mode, **kw):
+    base = dict(mode=mode, time_step=2e-4 if method == 0 else 5e-4, max_vel=10.0 if method == 0 else 20.0,
+                particle_radius=0.0075, support_radius=0.03, rest_density=1000.0, k_viscosity=0.01, gravity=9.81,
+                gas_stiffness=57142.857, surface_tension=0.001 if method == 0 else 1.0,
+                pcisph_min_iterations=3, pcisph_max_iterations=3, relax_on_add=0)
+    base.update(kw)
+    return capi.make_params(method, **base)
+
+
+def scene():
+    sc = small_scene()
+    return sc["fluid"], [(sc["boundary"], None, 0, 0.0)], sc["container"]
+
+
+def check_grid(ctx, orc):
+    for s in GRID:
+        ctx.stage(s)
+        orc.stage(s)
+        if s == "HASHES":
+            assert np.array_equal(ctx.get("HASHES"), orc.get("HASHES"))
+            assert np.array_equal(ctx.get("MASK"), orc.get("MASK"))
+    assert np.array_equal(ctx.get("HASHES"), orc.get("HASHES")), "sorted keys differ"
+    assert np.array_equal(ctx.get("MASK"), orc.get("MASK")), "sort permutation differs"
+    assert np.array_equal(ctx.get("POS_SORTED"), orc.get("POS_SORTED"))
+    assert np.array_equal(ctx.get("CELL_INTERVALS"), orc.get("CELL_INTERVALS")), "cell ranges differ"
+
+
+def valid_entries(lst, ln):
+    """Column-major list[k * n + i] restricted to k < len[i] (later slots keep stale values,
+    as the reference's list buffers do)."""
+    n = len(ln)
+    cap = len(lst) // max(n, 1)
+    m = lst.reshape(cap, n)
+    keep = np.arange(cap)[:, None] < ln[None, :]
+    return np.where(keep, m, -1)
+
+
+def check_lists(ctx, orc):
+    ctx.stage("NEIGH_LIST")
+    orc.stage("NEIGH_LIST")
+    orc.stage("SB_NEIGH_LIST")
+    for lst, ln in (("NEIGH_LIST", "NEIGH_LEN"), ("SB_NEIGH_LIST", "SB_NEIGH_LEN")):
+        a_len, b_len = ctx.get(ln), orc.get(ln)
+        assert np.array_equal(a_len, b_len), ln
+        assert np.array_equal(valid_entries(ctx.get(lst), a_len), valid_entries(orc.get(lst), b_len)), lst
+
+
+def test_boundary_setup_matches_oracle(gpu_lib):
+    fluid, bodies, container = scene()
+    for mode in (0, 1):
+        ctx, orc = make_pair(small_params(0, mode), fluid, bodies, container)
+        assert np.array_equal(ctx.get("BHASHES"), orc.get("BHASHES"))
+        assert np.array_equal(ctx.get("BMASK"), orc.get("BMASK"))
+        assert np.array_equal(ctx.get("BPOS_SORTED"), orc.get("BPOS_SORTED"))
+        assert np.array_equal(ctx.get("BCELL_INTERVALS"), orc.get("BCELL_INTERVALS"))
+        assert_close("phi", ctx.get("BPHI"), orc.get("BPHI"))
+        assert_close("phi sorted", ctx.get("BPHI_SORTED"), orc.get("BPHI_SORTED"))
+        ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("lists", [0, 1])
+def test_wcsph_stages_match_oracle(gpu_lib, mode, lists):
+    fluid, bodies, container = scene()
+    ctx, orc = make_pair(small_params(0, mode, neighbor_mode=lists), fluid, bodies, container)
+    n = ctx.particle_count()
+    for step in range(3):
+        check_grid(ctx, orc)
+        check_lists(ctx, orc)
+        ctx.stage("WC_DENSITY")
+        orc.stage("WC_DENSITY")
+        assert_close("density", ctx.get("DENSITY"), orc.get("DENSITY"))
+        assert_close("pressure", ctx.get("PRESSURE"), orc.get("PRESSURE"), rtol=1e-4)
+        if mode == 0:
+            # COMPAT densities are negative (poly6 of r): drive the force branch with
+            # physical density/pressure fields on both sides.
+            d = (1000.0 + 20.0 * np.sin(np.arange(n))).astype(np.float32)
+            p = (57142.857 * ((d / 1000.0) ** 7 - 1)).clip(0).astype(np.float32)
+            for o in (ctx, orc):
+                o.set("DENSITY", d)
+                o.set("PRESSURE", p)
+        else:
+            # start both from the same fields so the force comparison isolates the kernel
+            orc.set("DENSITY", ctx.get("DENSITY"))
+            orc.set("PRESSURE", ctx.get("PRESSURE"))
+        ctx.stage("NORMALS")
+        orc.stage("NORMALS")
+        assert_close("normal", ctx.get("NORMAL"), orc.get("NORMAL"), 4)
+        orc.set("NORMAL", ctx.get("NORMAL"))
+        ctx.stage("WC_ACCEL")
+        orc.stage("WC_ACCEL")
+        assert_close("accel", ctx.get("ACCEL"), orc.get("ACCEL"), 4)
+        orc.set("ACCEL", ctx.get("ACCEL"))
+        ctx.stage("WC_INTEGRATE")
+        orc.stage("WC_INTEGRATE")
+        assert_close("pos", ctx.get("POS"), orc.get("POS"), 4, rtol=1e-6)
+        assert_close("vel", ctx.get("VEL"), orc.get("VEL"), 4)
+        assert_close("vel_half", ctx.get("VEL_HALF"), orc.get("VEL_HALF"), 4)
+        assert np.array_equal(ctx.get("ID"), orc.get("ID"))
+        # continue from identical state
+        for f in ("POS", "VEL", "VEL_HALF"):
+            orc.set(f, ctx.get(f))
+    ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_pcisph_stages_match_oracle(gpu_lib, mode):
+    fluid, bodies, container = scene()
+    ctx, orc = make_pair(small_params(1, mode, pcisph_max_iterations=4), fluid, bodies, container)
+    for step in range(2):
+        check_grid(ctx, orc)
+        check_lists(ctx, orc)
+        for s in ("PCI_INIT_DENSITY", "NORMALS", "PCI_INIT_FORCES"):
+            ctx.stage(s)
+            orc.stage(s)
+        assert_close("density", ctx.get("DENSITY"), orc.get("DENSITY"))
+        assert_close("normal", ctx.get("NORMAL"), orc.get("NORMAL"), 4)
+        assert_close("f_other", ctx.get("FORCE_OTHER"), orc.get("FORCE_OTHER"), 4)
+        for f in ("DENSITY", "NORMAL", "FORCE_OTHER"):
+            orc.set(f, ctx.get(f))
+        ctx.stage("PCI_LOOP")
+        orc.stage("PCI_LOOP")
+        assert ctx.get("PCI_ITERS")[0] == orc.get("PCI_ITERS")[0]
+        assert_close("maxerr", ctx.get("PCI_MAXERR"), orc.get("PCI_MAXERR"), rtol=1e-4)
+        assert_close("dens_var", ctx.get("DENS_VAR"), orc.get("DENS_VAR"), rtol=1e-4)
+        assert_close("pressure", ctx.get("PRESSURE"), orc.get("PRESSURE"), rtol=1e-4)
+        assert_close("f_press", ctx.get("FORCE_PRESSURE"), orc.get("FORCE_PRESSURE"), 4, rtol=1e-4)
+        orc.set("FORCE_PRESSURE", ctx.get("FORCE_PRESSURE"))
+        ctx.stage("PCI_INTEGRATE")
+        orc.stage("PCI_INTEGRATE")
+        assert_close("pos", ctx.get("POS"), orc.get("POS"), 4, rtol=1e-6)
+        assert_close("vel", ctx.get("VEL"), orc.get("VEL"), 4)
+        for f in ("POS", "VEL"):
+            orc.set(f, ctx.get(f))
+    ctx.close()
+
+
+def test_fused_graph_step_matches_stage_sequence(gpu_lib):
+    """The CUDA-graph step (fused forces + integration) equals the stage-by-stage step."""
+    fluid, bodies, container = scene()
+    a, orc = make_pair(small_params(0, 1), fluid, bodies, container)
+    b, _ = make_pair(small_params(0, 1, use_graph=0), fluid, bodies, container)
+    a.simulate(5)
+    b.simulate(5)
+    assert_close("pos graph vs direct", a.get("POS"), b.get("POS"), 4, rtol=1e-6)
+    orc.step(5)
+    assert_close("pos vs oracle (5 steps)", a.get("POS"), orc.get("POS"), 4, rtol=1e-5)
+    assert np.array_equal(a.get("ID"), orc.get("ID"))
+    assert a.device_flags() & (capi.FLAGS["NAN"] | capi.FLAGS["TIMEOUT"]) == 0
+
+
+def test_pcisph_graph_step_matches_oracle(gpu_lib):
+    fluid, bodies, container = scene()
+    ctx, orc = make_pair(small_params(1, 1, pcisph_max_iterations=8), fluid, bodies, container)
+    ctx.simulate(3)
+    orc.step(3)
+    assert ctx.get("PCI_ITERS")[0] == orc.get("PCI_ITERS")[0]
+    assert_close("pos", ctx.get("POS"), orc.get("POS"), 4, rtol=1e-5)
+    assert ctx.device_flags() & capi.FLAGS["TIMEOUT"] == 0
