@@ -1,0 +1,332 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 SPH particle pipeline: particle-updates/s.
+
+Default workload: WCSPH double dam break, 4,194,304 fluid particles (two 128^3 lattice blocks
+at dx = 0.005 m, h = 0.01 m, dt = 5e-5 s) in a 2x1x1 m container of ~321k boundary particles,
+PHYSICS mode, FP32.  A step is one sph_simulate() (one CUDA-graph replay): bin, onesweep sort,
+reorder, cell ranges, density/pressure, normals, forces with fused leapfrog integration.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
+
+Prints ONE JSON line (rank 0).  value = N_fluid x K x ranks / max-over-ranks device time of K
+steps (CUDA events on the context stream; inputs larger than L2 every step).  e2e repeats the
+metric through the C ABI with host buffers (pinned), copying the particle state in and the
+step's result out every step.  With several GPUs each rank runs an independent replica
+(the single-scene path has no data-parallel split without a halo exchange).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-updates/s (WCSPH/PCISPH @4M); batched & adjoint vs plain, same GPU"
+UNIT = "particle-updates/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+# Algorithmic HBM bytes per fluid particle of each kernel (compulsory traffic; neighbour reads
+# are assumed to hit L1/L2).  The derivation is tabulated in the design doc.
+ALG_BYTES = {
+    "k_hashes": 16 + 4 + 4 + 4 + 8,          # pos in; key, mask out; cell_prev in; clear 8 B/cell (upper bound)
+    "k_gather": 4 + 3 * 16 * 2 + 4 * 2,      # perm; pos/vel/vhalf gathered and written; ids
+    "k_cell_ranges": 16 + 8 + 4 + 8,         # sorted pos, 2 keys, cell id out, range writes (per cell)
+    "k_wc_density": 16 + 8,                  # own position; density and pressure out
+    "k_normals": 16 + 16,                    # own position; normal out
+    "k_wc_forces": 16 * 3 + 4 + 4 + 16 + 4 + 16 * 3 + 4,   # pos,vel,vhalf,rho,p,normal,id in; pos,vel,vhalf,id out
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["wcsph4m", "wcsph65k", "pcisph"], default="wcsph4m")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--neighbor-mode", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), int(
+        os.environ.get("WORLD_SIZE", "1"))
+
+
+def load_workload(name, mode, seed=0):
+    from fluids_gb300 import workloads
+    if name == "wcsph4m":
+        return workloads.double_dam_4m(mode=mode, seed=seed)
+    if name == "wcsph65k":
+        return workloads.dam_break_65k(mode=mode, seed=seed)
+    return workloads.pcisph_cube(mode=mode, seed=seed)
+
+
+def describe_workload(w, n, nb, params):
+    p = params
+    return {
+        "workload": w["name"],
+        "method": "PCISPH" if p.method == 1 else "WCSPH",
+        "particles": n,
+        "boundary_particles": nb,
+        "dx_m": w["dx"],
+        "h_m": p.support_radius,
+        "dt_s": p.time_step,
+        "container_m": list(w["container"]),
+        "mode": "physics" if p.mode == 1 else "compat",
+        "neighbors": "list" if p.neighbor_mode == 1 or p.method == 1 else "cell-scan",
+        "l2": "inputs larger than L2 every step (particle state %.0f MB > 129 MB)" % (n * 200 / 1e6),
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_hbm_peak():
+    try:
+        d = json.load(open(PEAKS_FILE))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def measured_traffic(kernel, workload):
+    """dram read+write bytes per launch of a kernel, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        f = line.split()
+        if len(f) >= 3 and f[0] == kernel and f[1] == workload:
+            return float(f[2])
+    return None
+
+
+def cpu_baseline(wl_name, mode, sample_steps, sample_desc_prefix, crop=None):
+    """Times the oracle (the CPU port of the same step) on the host cores."""
+    from oracle import Oracle, kwargs_from_params
+    w = load_workload(wl_name, mode)
+    fluid = w["fluid"]
+    if crop is not None:
+        fluid = fluid[crop]
+    threads = os.cpu_count() or 1
+    o = Oracle(threads=threads, **kwargs_from_params(w["params"], w["container"]))
+    for pts, rot, mv, mass in w["bodies"]:
+        o.add_boundary(pts, can_move=mv, rot3x4=rot, mass=mass)
+    o.set_fluid(fluid)
+    o.step(1)
+    t0 = time.perf_counter()
+    o.step(sample_steps)
+    dt = time.perf_counter() - t0
+    n = len(fluid)
+    return {"value": n * sample_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%s: %d steps of %d fluid particles (+%d boundary), %.1f s" % (
+                sample_desc_prefix, sample_steps, n, sum(len(b[0]) for b in w["bodies"]), dt)}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    from fluids_gb300 import capi
+    w = load_workload(args.workload, capi.SPH_MODE_COMPAT)
+    # bounded sample: a slab of the first block (every particle with z in the lowest eighth)
+    z = w["fluid"][:, 2]
+    crop = np.nonzero(z < np.quantile(z, 1.0 / 16))[0] if args.workload == "wcsph4m" else None
+    from oracle import Oracle, kwargs_from_params
+    fluid = w["fluid"] if crop is None else w["fluid"][crop]
+    threads = os.cpu_count() or 1
+    o = Oracle(threads=threads, **kwargs_from_params(w["params"], w["container"]))
+    for pts, rot, mv, mass in w["bodies"]:
+        o.add_boundary(pts, can_move=mv, rot3x4=rot, mass=mass)
+    o.set_fluid(fluid)
+    o.step(max(args.warmup, 0))
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    n = len(fluid)
+    v = n * args.steps / dt
+    sample = ("reference kernels' CPU port (oracle, COMPAT mode: 5 m grid, 50-entry neighbour lists), "
+              "%d fluid particles (a z-slab of the workload) + %d boundary, %d steps in %.1f s" % (
+                  n, sum(len(b[0]) for b in w["bodies"]), args.steps, dt))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * dt / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": describe_workload(w, n, sum(len(b[0]) for b in w["bodies"]), w["params"]),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, local_rank, world = dist_env()
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    torch.cuda.set_device(local_rank)
+    import fluids_gb300
+    from fluids_gb300 import capi, workloads
+    fluids_gb300.build()
+    w = load_workload(args.workload, capi.SPH_MODE_PHYSICS, seed=rank)
+    params = w["params"]
+    params.neighbor_mode = args.neighbor_mode
+    stream = torch.cuda.Stream()
+    ctx = capi.Context(params)
+    capi.check(capi.lib().sph_set_stream(ctx.h, capi.C.c_void_p(stream.cuda_stream)), ctx.h)
+    ctx.set_rect_limits(*w["container"])
+    for pts, rot, mv, mass in w["bodies"]:
+        ctx.add_boundary(pts, can_move=mv, rot3x4=rot, mass=mass)
+    ctx.add_volume(w["fluid"], w.get("velocities"))
+    n, nb = ctx.particle_count(), ctx.boundary_particle_count()
+    d = capi.describe(params, w["container"])
+
+    ctx.simulate(max(args.warmup, 3))
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler() if rank == 0 else None
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    e0.record(stream)
+    ctx.simulate(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop() if clocks else None
+    t = e0.elapsed_time(e1) / 1000.0
+    if world > 1:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    flags = ctx.device_flags()
+    value = n * args.steps * world / t
+
+    # per-kernel device time of the same step (events between the kernels, no graph)
+    kern = ctx.profile_step(min(args.steps, 20))
+    top = max(kern, key=kern.get)
+    peak, peak_kind = measured_hbm_peak()
+    alg = ALG_BYTES.get(top)
+    roof = None
+    if alg is not None:
+        bnd_extra = 20.0 * nb if top in ("k_wc_density", "k_wc_forces") else 0.0
+        bytes_launch = alg * n + bnd_extra
+        achieved = bytes_launch / (kern[top] / 1000.0) / 1e9
+        tr = measured_traffic(top, w["name"])
+        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes": bytes_launch,
+                "traffic": tr, "ms_per_launch": kern[top]}
+    passes = (d["key_bits"] + 7) // 8
+    launches_per_step = sum(1 for k in kern) + (passes if "sort" in kern else 0)
+    # e2e through the C ABI with pinned host buffers: state in, result out, every step
+    e2e = None
+    if not args.no_e2e:
+        hp = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+        hv = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+        hh = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+        L = capi.lib()
+        for f, a in (("POS", hp), ("VEL", hv), ("VEL_HALF", hh)):
+            capi.check(L.sph_get_field(ctx.h, capi.FIELDS[f], a.ctypes.data, a.nbytes), ctx.h)
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        k_e2e = args.steps
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            for f, a in (("POS", hp), ("VEL", hv), ("VEL_HALF", hh)):
+                capi.check(L.sph_set_field(ctx.h, capi.FIELDS[f], a.ctypes.data, a.nbytes), ctx.h)
+            capi.check(L.sph_simulate(ctx.h, 1), ctx.h)
+            for f, a in (("POS", hp), ("VEL", hv), ("VEL_HALF", hh)):
+                capi.check(L.sph_get_field(ctx.h, capi.FIELDS[f], a.ctypes.data, a.nbytes), ctx.h)
+        te = time.perf_counter() - t0
+        if world > 1:
+            tt = torch.tensor([te], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": n * k_e2e * world / te, "unit": UNIT, "h2d_bytes_per_step": 48 * n,
+               "d2h_bytes_per_step": 48 * n, "steps": k_e2e, "host_buffers": "pinned"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        z = w["fluid"][:, 2]
+        crop = np.nonzero(z < np.quantile(z, 1.0 / 16))[0] if args.workload == "wcsph4m" else None
+        cpu = cpu_baseline(args.workload, capi.SPH_MODE_PHYSICS, 10 if crop is not None else 3,
+                           "oracle PHYSICS FP32 (same step as the GPU path), z-slab of the workload", crop)
+    if rank == 0:
+        cfg = describe_workload(w, n, nb, params)
+        cfg["grid_cells"] = d["grid_dims"]
+        cfg["parallelism"] = "replicas" if world > 1 else "single GPU"
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + jitter)",
+                "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches_per_step * args.steps, "clocks": clk,
+                "kernel_ms_per_step": kern, "device_flags": flags}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

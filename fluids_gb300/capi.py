@@ -39,7 +39,7 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_synchronize", "sph_device_flags", "sph_field_elems", "sph_field_kind", "sph_get_field",
            "sph_set_field", "sph_field_device_ptr", "sph_body_forces", "sph_stats", "sph_sort_pairs",
            "sph_scene_box_volume", "sph_scene_fishtank", "sph_scene_cube", "sph_jitter", "sph_cuda_available",
-           "sph_describe"]
+           "sph_describe", "sph_profile_step"]
 
 
 class SphParams(C.Structure):
@@ -119,6 +119,7 @@ def lib():
             "sph_jitter": (None, [fp, ip, C.c_float, C.c_uint64]),
             "sph_cuda_available": (ip, []),
             "sph_describe": (ip, [PP, fp, C.POINTER(SphDerived)]),
+            "sph_profile_step": (ip, [vp, ip, C.POINTER(C.c_float), ip, C.POINTER(ip), C.c_char_p, C.c_size_t]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -280,6 +281,15 @@ class Context:
         t = np.zeros((nbodies, 4), np.float32)
         self._c(self._lib.sph_body_forces(self.h, ptr(f), ptr(t), int(nbodies)))
         return f, t
+
+    def profile_step(self, nsteps):
+        """Average device ms per step of each kernel group of the step (sph_profile_step)."""
+        ms = (C.c_float * 64)()
+        ng = C.c_int()
+        names = C.create_string_buffer(4096)
+        self._c(self._lib.sph_profile_step(self.h, int(nsteps), ms, 64, C.byref(ng), names, 4096))
+        keys = names.value.decode().split(",") if ng.value else []
+        return dict(zip(keys, [float(ms[i]) for i in range(ng.value)]))
 
     def stats(self):
         out = (C.c_double * 8)()

@@ -57,6 +57,9 @@ struct sph_ctx {
     uint32_t* cur_keys = nullptr;
     int32_t* cur_mask = nullptr;
     bool has_state = false;
+    std::vector<cudaEvent_t>* prof = nullptr;   /* set only by sph_profile_step */
+    std::vector<const char*> prof_names;
+    std::string prof_list;
 };
 
 namespace {
@@ -353,6 +356,17 @@ int run_stage_impl(sph_ctx* x, int stage) {
 }
 
 /* One full step: the fused sequence of WCSPHSimulation::simulate / _simulate_pcisph_step. */
+/* Profiling marks: when x->prof is set, an event is recorded after each kernel group of the
+ * step so sph_profile_step can report per-kernel device time (never inside a graph). */
+void mark(sph_ctx* x, const char* name) {
+    if (!x->prof) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, x->stream);
+    x->prof->push_back(e);
+    x->prof_names.push_back(name);
+}
+
 int enqueue_step(sph_ctx* x, int pci_max_iter) {
     if (x->N <= 0) return SPH_OK;
     Bufs& b = x->b;
@@ -360,31 +374,57 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
     const cudaStream_t s = x->stream;
     const int bs = x->bs;
     int rc;
+    mark(x, "start");
     const int pre[] = {SPH_S_BOUNDARY_SYNC, SPH_S_HASHES, SPH_S_SORT, SPH_S_SHUFFLE, SPH_S_CELL_INTERVALS};
-    for (int st : pre)
-        if ((rc = run_stage_impl(x, st)) != SPH_OK) return rc;
+    const char* pre_names[] = {"boundary_sync", "k_hashes", "sort", "k_gather", "k_cell_ranges"};
+    for (int k = 0; k < 5; ++k) {
+        if (pre[k] == SPH_S_BOUNDARY_SYNC && !(x->NB > 0 && x->any_movable)) continue;
+        if ((rc = run_stage_impl(x, pre[k])) != SPH_OK) return rc;
+        mark(x, pre_names[k]);
+    }
     if (x->p.method == SPH_WCSPH) {
         const bool lists = x->p.neighbor_mode == SPH_NEIGH_LIST;
-        if (lists) sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs);
+        if (lists) {
+            sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs);
+            mark(x, "k_neigh_lists");
+        }
         sph::launch_wc_density(s, c, b, lists, bs);
-        if (c.sigma != 0.f) sph::launch_normals(s, c, b, lists, bs);
-        if (x->any_massive) sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
+        mark(x, "k_wc_density");
+        if (c.sigma != 0.f) {
+            sph::launch_normals(s, c, b, lists, bs);
+            mark(x, "k_normals");
+        }
+        if (x->any_massive) {
+            sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
+            mark(x, "k_bnd_forces");
+        }
         sph::launch_wc_forces(s, c, b, lists, true, false, bs);
+        mark(x, "k_wc_forces");
     } else {
         sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs);
+        mark(x, "k_neigh_lists");
         sph::launch_pci_init_density(s, c, b, bs);
-        if (c.sigma != 0.f) sph::launch_normals(s, c, b, true, bs);
+        mark(x, "k_pci_init_density");
+        if (c.sigma != 0.f) {
+            sph::launch_normals(s, c, b, true, bs);
+            mark(x, "k_normals");
+        }
         sph::launch_pci_init_forces(s, c, b, bs);
+        mark(x, "k_pci_init_forces");
         cudaMemsetAsync(b.pci_maxerr, 0, sizeof(float) * x->max_iter_slots, s);
         cudaMemsetAsync(b.barrier, 0, 4 * sizeof(unsigned), s);
         if (x->any_massive) {
             cudaError_t e = sph::launch_pci_loop(s, c, b, c.pci_min_iter, pci_max_iter, x->coop_blocks, bs, false);
             if (e != cudaSuccess) return cuda_fail(x, e, "cooperative launch of the PCISPH loop");
+            mark(x, "k_pci_loop");
             sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
+            mark(x, "k_bnd_forces");
             sph::launch_pci_integrate(s, c, b, bs);
+            mark(x, "k_pci_integrate");
         } else {
             cudaError_t e = sph::launch_pci_loop(s, c, b, c.pci_min_iter, pci_max_iter, x->coop_blocks, bs, true);
             if (e != cudaSuccess) return cuda_fail(x, e, "cooperative launch of the PCISPH loop");
+            mark(x, "k_pci_loop");
         }
     }
     cudaError_t e = cudaGetLastError();
@@ -838,6 +878,51 @@ int sph_simulate(sph_ctx* x, int nsteps) {
             int rc = enqueue_step(x, x->c.pci_max_iter);
             if (rc != SPH_OK) return rc;
         }
+    }
+    return SPH_OK;
+}
+
+int sph_profile_step(sph_ctx* x, int nsteps, float* ms_out, int max_groups, int* ngroups, char* names,
+                     size_t names_len) {
+    if (check_ctx(x) || nsteps <= 0 || !ms_out || !ngroups) return SPH_E_INVALID;
+    if (!x->has_state || x->N <= 0) return fail(x, SPH_E_STATE, "no particles added");
+    std::vector<cudaEvent_t> ev;
+    std::vector<double> acc;
+    std::vector<const char*> nm;
+    int rc = SPH_OK;
+    for (int k = 0; k < nsteps && rc == SPH_OK; ++k) {
+        ev.clear();
+        x->prof_names.clear();
+        x->prof = &ev;
+        rc = enqueue_step(x, x->c.pci_max_iter);
+        x->prof = nullptr;
+        if (rc != SPH_OK) break;
+        cudaError_t e = cudaStreamSynchronize(x->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(x, e, "profiled step"); break; }
+        if (acc.empty()) {
+            acc.assign(ev.size() > 0 ? ev.size() - 1 : 0, 0.0);
+            nm.assign(x->prof_names.begin() + (x->prof_names.empty() ? 0 : 1), x->prof_names.end());
+        }
+        for (size_t g = 1; g < ev.size() && g - 1 < acc.size(); ++g) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[g - 1], ev[g]);
+            acc[g - 1] += ms;
+        }
+        for (auto e2 : ev) cudaEventDestroy(e2);
+    }
+    x->prof_names.clear();
+    if (rc != SPH_OK) return rc;
+    const int ng = (int)acc.size();
+    *ngroups = ng;
+    for (int g = 0; g < ng && g < max_groups; ++g) ms_out[g] = (float)(acc[g] / nsteps);
+    if (names && names_len) {
+        std::string all;
+        for (int g = 0; g < ng; ++g) {
+            if (g) all += ",";
+            all += nm[g];
+        }
+        std::strncpy(names, all.c_str(), names_len - 1);
+        names[names_len - 1] = 0;
     }
     return SPH_OK;
 }

@@ -174,6 +174,13 @@ int sph_boundary_particle_count(const sph_ctx* ctx);
 int sph_simulate(sph_ctx* ctx, int nsteps);
 /* Runs one stage (one reference launch point) on the current state. */
 int sph_run_stage(sph_ctx* ctx, int stage);
+/* Runs nsteps steps of the same kernel sequence as sph_simulate, without the graph, with a
+ * CUDA event after each kernel group (replaces the reference's per-kernel profiling queue,
+ * opencl/clenvironment.cpp:45-48 and clmisc.cpp:3-22).  Writes the average device ms per
+ * step of each group to ms_out[0..max_groups), the group count to *ngroups and the group
+ * names, comma-separated, to names. */
+int sph_profile_step(sph_ctx* ctx, int nsteps, float* ms_out, int max_groups, int* ngroups, char* names,
+                     size_t names_len);
 /* Waits for the context stream. */
 int sph_synchronize(sph_ctx* ctx);
 /* Reads (and with clear = 1 resets) the device status word; synchronises. */

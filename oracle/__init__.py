@@ -10,7 +10,7 @@ their host-side constant derivation, float or double, COMPAT or PHYSICS mode).
 those pin the oracle.
 """
 from .oracle import (Oracle, OrcDerived, build_oracle, lib_path, STAGES, FIELDS,
-                     WCSPH_STEP, morton3, stable_sort_pairs)
+                     WCSPH_STEP, morton3, stable_sort_pairs, kwargs_from_params)
 
 __all__ = ["Oracle", "OrcDerived", "build_oracle", "lib_path", "STAGES", "FIELDS",
-           "WCSPH_STEP", "morton3", "stable_sort_pairs"]
+           "WCSPH_STEP", "morton3", "stable_sort_pairs", "kwargs_from_params"]

@@ -57,6 +57,19 @@ def lib_path():
     return _LIB
 
 
+def kwargs_from_params(p, container):
+    """Oracle keywords equal to a solver parameter struct (any object with the sph_params
+    field names, e.g. fluids_gb300.capi.SphParams)."""
+    return dict(method=p.method, mode=p.mode, container=tuple(container), neigh_cap=p.neigh_cap,
+                time_step=p.time_step, max_vel=p.max_vel, particle_radius=p.particle_radius,
+                support_radius=p.support_radius, pci_min_iter=p.pcisph_min_iterations,
+                pci_max_iter=p.pcisph_max_iterations, pci_error_ratio=p.pcisph_error_ratio,
+                pci_relax_max_iter=p.pcisph_relax_max_iterations, rest_density=p.rest_density,
+                k_viscosity=p.k_viscosity, gravity=p.gravity, gas_stiffness=p.gas_stiffness,
+                surface_tension=p.surface_tension, grid_size=p.grid_size, grid_margin=p.grid_margin,
+                phi_coeff=p.boundary_phi_coeff, relax_on_add=p.relax_on_add)
+
+
 def build_oracle(force=False):
     """Compiles oracle/sph_oracle.cpp with g++ (OpenMP, no FMA contraction)."""
     src = os.path.join(HERE, "sph_oracle.cpp")

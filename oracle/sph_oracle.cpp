@@ -687,11 +687,43 @@ struct Oracle : OracleBase {
         ids = ids_s;
     }
 
-    /* kernels/boundary.cl:4-31 over each body's own particles (boundaryhandler.cpp:238-249) */
+    /* kernels/boundary.cl:4-31 over each body's own particles (boundaryhandler.cpp:238-249).
+     * Bodies above kBrute particles are summed over the same pairs (r^2 < h^2 within the
+     * body) found through cells of the grid, in cell order, instead of the O(n^2) loop. */
+    static constexpr int kBrute = 20000;
     void boundary_phi() {
         const R H = h_def, H2 = pown(H, 2);
         bphi.assign(NB, 0);
         for (auto& b : bodies) {
+            if (b.count > kBrute) {
+                std::vector<std::pair<long long, int>> cells(b.count);
+                for (int ii = 0; ii < b.count; ++ii) {
+                    int c[3];
+                    coords(ld(bpos, b.origin + ii), c);
+                    cells[ii] = {cell_id(c[0], c[1], c[2]), ii};
+                }
+                std::sort(cells.begin(), cells.end());
+#pragma omp parallel for schedule(dynamic, 256)
+                for (int ii = 0; ii < b.count; ++ii) {
+                    int i = b.origin + ii;
+                    V3<R> pi = ld(bpos, i);
+                    int c[3];
+                    coords(pi, c);
+                    R del = 0;
+                    for (int o = 0; o < 27; ++o) {
+                        long long id;
+                        if (!cell_ok(c[0] + kOff[o][0], c[1] + kOff[o][1], c[2] + kOff[o][2], id)) continue;
+                        auto lo = std::lower_bound(cells.begin(), cells.end(), std::make_pair(id, -1));
+                        for (auto it = lo; it != cells.end() && it->first == id; ++it) {
+                            V3<R> r = pi - ld(bpos, b.origin + it->second);
+                            R r2 = dot(r, r);
+                            if (r2 < H2) del += pown(pown(H, 2) - r2, 3);
+                        }
+                    }
+                    bphi[i] = (rho0 / (del * boundary_eval)) / R(cfg.phi_coeff);
+                }
+                continue;
+            }
 #pragma omp parallel for schedule(static)
             for (int ii = 0; ii < b.count; ++ii) {
                 int i = b.origin + ii;

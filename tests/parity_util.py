@@ -2,7 +2,7 @@
 oracle, and compare fields."""
 import numpy as np
 
-from oracle import Oracle
+from oracle import Oracle, kwargs_from_params
 from fluids_gb300 import capi
 
 # FP32 tolerance of the parity bar: max over particles of |a_i - b_i| (norm-wise for
@@ -29,14 +29,7 @@ def assert_close(name, a, b, width=1, rtol=RTOL):
 
 def oracle_config(params, container):
     """OrcConfig keywords equal to a capi.SphParams."""
-    p = params
-    return dict(method=p.method, mode=p.mode, container=container, neigh_cap=p.neigh_cap, time_step=p.time_step,
-                max_vel=p.max_vel, particle_radius=p.particle_radius, support_radius=p.support_radius,
-                pci_min_iter=p.pcisph_min_iterations, pci_max_iter=p.pcisph_max_iterations,
-                pci_error_ratio=p.pcisph_error_ratio, pci_relax_max_iter=p.pcisph_relax_max_iterations,
-                rest_density=p.rest_density, k_viscosity=p.k_viscosity, gravity=p.gravity,
-                gas_stiffness=p.gas_stiffness, surface_tension=p.surface_tension, grid_size=p.grid_size,
-                grid_margin=p.grid_margin, phi_coeff=p.boundary_phi_coeff, relax_on_add=p.relax_on_add)
+    return kwargs_from_params(params, container)
 
 
 def make_pair(params, fluid, bodies, container, precision=0, vel=None):
