@@ -41,6 +41,7 @@ ALG_BYTES = {
     "k_gather": 4 + 3 * 16 * 2 + 4 * 2,      # perm; pos/vel/vhalf gathered and written; ids
     "k_cell_ranges": 16 + 8 + 4 + 8,         # sorted pos, 2 keys, cell id out, range writes (per cell)
     "k_wc_density": 16 + 8,                  # own position; density and pressure out
+    "k_lists_density": 16 + 8,               # same compulsory bytes; the lists it writes are scratch
     "k_normals": 16 + 16,                    # own position; normal out
     "k_wc_forces": 16 * 3 + 4 + 4 + 16 + 4 + 16 * 3 + 4,   # pos,vel,vhalf,rho,p,normal,id in; pos,vel,vhalf,id out
 }
@@ -55,7 +56,7 @@ def parse():
     ap.add_argument("--workload", choices=["wcsph4m", "wcsph65k", "pcisph"], default="wcsph4m")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--neighbor-mode", type=int, default=0)
+    ap.add_argument("--neighbor-mode", type=int, default=1, help="0 = cell scan in every pass, 1 = lists")
     return ap.parse_args()
 
 

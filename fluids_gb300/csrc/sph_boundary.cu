@@ -62,7 +62,7 @@ __global__ void k_bnd_phi(Const c, int nb, const float4* __restrict__ bpos_s, co
     cu.cap = 0x7fffffff;
     cu.h2_list = HH;
     float del = 0.f;
-    scan_neighbors(cu, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float dx, float dy, float dz) {
+    scan_neighbors<true>(cu, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float dx, float dy, float dz) {
         if (__ldg(&body_s[j]) == bi) {
             const float t = HH - r2_exact(dx, dy, dz);
             del += (t * t) * t;

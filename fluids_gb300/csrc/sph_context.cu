@@ -145,6 +145,10 @@ int derive(sph_ctx* x) {
     float t = 1e-5f;
     if ((double)t > 1e-5) t = std::nextafter(t, 0.0f);
     c.rmin_wc = t;
+    c.rmin2_wc = t * t;
+    /* cell skipping bound with a 1e-3 relative margin, far above the rounding of the cell
+     * coordinates (<= 2^-13 cell units for grids up to 1024 cells per axis) */
+    c.cull2 = (c.h2_list / (h * h)) * 1.001f;
     if (p.method == SPH_WCSPH) {
         const float mf = rho0 * std::pow(2.0f * r, 3.0f) / 1.0f;
         c.mass = mf;
@@ -232,6 +236,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.normal = cv.take<float4>(n); b.accel = cv.take<float4>(n); b.pos_pred = cv.take<float4>(n);
     b.f_other = cv.take<float4>(n); b.f_press = cv.take<float4>(n);
     b.density = cv.take<float>(n); b.pressure = cv.take<float>(n); b.dens_var = cv.take<float>(n);
+    b.aux = cv.take<float4>(n);
     b.keys = cv.take<uint32_t>(n); b.keys_alt = cv.take<uint32_t>(n);
     b.mask = cv.take<int32_t>(n); b.mask_alt = cv.take<int32_t>(n);
     b.ids = cv.take<int32_t>(n); b.ids_s = cv.take<int32_t>(n);
@@ -320,9 +325,11 @@ int run_stage_impl(sph_ctx* x, int stage) {
         sph::launch_wc_density(s, c, b, x->p.neighbor_mode == SPH_NEIGH_LIST, bs);
         break;
     case SPH_S_NORMALS:
+        sph::launch_aux(s, c, b, bs);   /* the density field may have been set from outside */
         sph::launch_normals(s, c, b, uses_lists(x), bs);
         break;
     case SPH_S_WC_ACCEL:
+        sph::launch_aux(s, c, b, bs);
         sph::launch_wc_forces(s, c, b, x->p.neighbor_mode == SPH_NEIGH_LIST, false, true, bs);
         break;
     case SPH_S_WC_INTEGRATE:
@@ -385,11 +392,12 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
     if (x->p.method == SPH_WCSPH) {
         const bool lists = x->p.neighbor_mode == SPH_NEIGH_LIST;
         if (lists) {
-            sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs);
-            mark(x, "k_neigh_lists");
+            sph::launch_lists_density(s, c, b, bs);
+            mark(x, "k_lists_density");
+        } else {
+            sph::launch_wc_density(s, c, b, false, bs);
+            mark(x, "k_wc_density");
         }
-        sph::launch_wc_density(s, c, b, lists, bs);
-        mark(x, "k_wc_density");
         if (c.sigma != 0.f) {
             sph::launch_normals(s, c, b, lists, bs);
             mark(x, "k_normals");
@@ -648,7 +656,7 @@ void bump_default_params(sph_params* p) {
     p->pcisph_min_iterations = 3;
     p->pcisph_relax_max_iterations = 10000;
     p->use_graph = 1;
-    p->neighbor_mode = SPH_NEIGH_SCAN;
+    p->neighbor_mode = SPH_NEIGH_LIST;
 }
 
 /* cached scratch for the standalone sort entry point */

@@ -33,6 +33,8 @@ struct Const {
     int pci_min_iter, pci_max_iter;
     int key_bits;
     float rmin_wc;       /* largest float <= 1e-5: wcsph.cl:152 compares r > 0.00001 (a double) */
+    float rmin2_wc;      /* rmin_wc^2: the same guard on r^2 */
+    float cull2;         /* (h_list / cell)^2 * (1 + 1e-4): face-distance bound for skipping cells */
 };
 
 constexpr unsigned kFlagNan = 1u, kFlagEscaped = 2u, kFlagTimeout = 4u, kFlagOverflow = 8u,
@@ -104,30 +106,70 @@ __device__ __forceinline__ void neigh_offset(int o, int& dx, int& dy, int& dz) {
     dz = t % 3 - 1;
 }
 
+/* Squared distance, in cell units, from a particle to the face of the neighbour cell in
+ * direction o (-1, 0, +1) along one axis, given its fractional position fr in its cell. */
+__device__ __forceinline__ float face_gap2(int o, float fr) {
+    const float g = o < 0 ? fr : (o > 0 ? 1.0f - fr : 0.0f);
+    return g * g;
+}
+
 /* Visits the neighbours j of a point (px, py, pz) among the particles npos[] binned in
  * table tab, in the reference's list order, keeping at most c.cap with r^2 < h2_list.
- * f(j, pj, dx, dy, dz) receives the neighbour and d = p - pj (IEEE, uncontracted). */
-template <class F>
+ * f(j, pj, dx, dy, dz) receives the neighbour and d = p - pj (IEEE subtraction).
+ * EXACT: r^2 as uncontracted IEEE sum (bit-exact membership, used for the lists and in
+ * COMPAT); otherwise FMA-contracted (membership can differ only for r within an ulp of h,
+ * where every smoothing kernel is zero).
+ * On the clamped PHYSICS grid, a neighbour cell whose nearest face is farther than h from
+ * the particle cannot hold a neighbour and is skipped (same visits, same order), and the
+ * cap is checked once per cell when the cell cannot overflow it. */
+template <bool EXACT, class F>
 __device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py, float pz,
                                               const int2* __restrict__ tab, const float4* __restrict__ npos,
                                               F&& f) {
+    const float qx = __fdiv_rn(__fsub_rn(px, c.ox), c.cell);
+    const float qy = __fdiv_rn(__fsub_rn(py, c.oy), c.cell);
+    const float qz = __fdiv_rn(__fsub_rn(pz, c.oz), c.cell);
     int cx, cy, cz;
     cell_of(c, px, py, pz, cx, cy, cz);
+    /* fractional positions; an axis that was clamped (or the wrapped COMPAT grid) culls nothing */
+    const bool cull = !c.wrap;
+    float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
+    const bool inx = cull && floorf(qx) == (float)cx, iny = cull && floorf(qy) == (float)cy,
+               inz = cull && floorf(qz) == (float)cz;
     int cnt = 0;
 #pragma unroll 1
     for (int o = 0; o < 27 && cnt < c.cap; ++o) {
         int ox, oy, oz;
         neigh_offset(o, ox, oy, oz);
+        if (cull) {
+            const float g = (inx ? face_gap2(ox, fx) : 0.f) + (iny ? face_gap2(oy, fy) : 0.f) +
+                            (inz ? face_gap2(oz, fz) : 0.f);
+            if (g > c.cull2) continue;
+        }
         long long id;
         if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) continue;
         const int2 r = __ldg(&tab[id]);
+        if (cnt + (r.y - r.x) <= c.cap) {
+#pragma unroll 2
+            for (int j = r.x; j < r.y; ++j) {
+                const float4 pj = __ldg(&npos[j]);
+                const float dx = __fsub_rn(px, pj.x), dy = __fsub_rn(py, pj.y), dz = __fsub_rn(pz, pj.z);
+                const float r2 = EXACT ? r2_exact(dx, dy, dz) : dx * dx + dy * dy + dz * dz;
+                if (r2 < c.h2_list) {
+                    f(j, pj, dx, dy, dz);
+                    ++cnt;
+                }
+            }
+        } else {
 #pragma unroll 1
-        for (int j = r.x; j < r.y && cnt < c.cap; ++j) {
-            const float4 pj = __ldg(&npos[j]);
-            const float dx = __fsub_rn(px, pj.x), dy = __fsub_rn(py, pj.y), dz = __fsub_rn(pz, pj.z);
-            if (r2_exact(dx, dy, dz) < c.h2_list) {
-                f(j, pj, dx, dy, dz);
-                ++cnt;
+            for (int j = r.x; j < r.y && cnt < c.cap; ++j) {
+                const float4 pj = __ldg(&npos[j]);
+                const float dx = __fsub_rn(px, pj.x), dy = __fsub_rn(py, pj.y), dz = __fsub_rn(pz, pj.z);
+                const float r2 = EXACT ? r2_exact(dx, dy, dz) : dx * dx + dy * dy + dz * dz;
+                if (r2 < c.h2_list) {
+                    f(j, pj, dx, dy, dz);
+                    ++cnt;
+                }
             }
         }
     }
@@ -148,7 +190,7 @@ __device__ __forceinline__ void list_neighbors(int i, int n, const int* __restri
 }
 
 /* Neighbour source: either the cell scan or the materialised list, same order. */
-template <bool LIST>
+template <bool LIST, bool EXACT = true>
 struct Neigh {
     const int2* tab;
     const int* list;
@@ -157,7 +199,7 @@ struct Neigh {
     template <class F>
     __device__ __forceinline__ void visit(const Const& c, int i, float px, float py, float pz, F&& f) const {
         if (LIST) list_neighbors(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
-        else scan_neighbors(c, px, py, pz, tab, npos, f);
+        else scan_neighbors<EXACT>(c, px, py, pz, tab, npos, f);
     }
 };
 

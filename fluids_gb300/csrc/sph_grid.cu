@@ -101,14 +101,14 @@ __global__ void k_neigh_lists(Const c, const float4* __restrict__ spos, const in
     const float4 pi = spos[i];
     const size_t n = (size_t)c.n;
     int k = 0;
-    scan_neighbors(c, pi.x, pi.y, pi.z, tab, spos, [&](int j, float4, float, float, float) {
+    scan_neighbors<true>(c, pi.x, pi.y, pi.z, tab, spos, [&](int j, float4, float, float, float) {
         nlist[(size_t)k * n + i] = j;
         ++k;
     });
     nlen[i] = k;
     int kb = 0;
     if (c.nb > 0) {
-        scan_neighbors(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float, float, float) {
+        scan_neighbors<true>(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float, float, float) {
             sblist[(size_t)kb * n + i] = j;
             ++kb;
         });

@@ -16,6 +16,7 @@ struct Bufs {
     float4 *pos_s, *vel_s, *vhalf_s;       /* this step's sorted copies */
     float4 *normal, *accel, *pos_pred, *f_other, *f_press;
     float *density, *pressure, *dens_var;
+    float4* aux;                           /* per particle (p/rho^2, 1/rho, rho, p) */
     uint32_t *keys, *keys_alt;
     int32_t *mask, *mask_alt;
     uint32_t* keys_sorted;                 /* where the sort left the keys */
@@ -72,6 +73,8 @@ void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, i
 void launch_wc_forces(cudaStream_t s, const Const& c, const Bufs& b, bool lists, bool fuse_integrate,
                       bool write_acc, int bs);
 void launch_wc_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs);
 
 /* sph_pcisph.cu */
 void launch_pci_init_density(cudaStream_t s, const Const& c, const Bufs& b, int bs);

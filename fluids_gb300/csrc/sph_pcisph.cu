@@ -210,7 +210,9 @@ __global__ void __launch_bounds__(256) k_pci_init_density(Const c, Bufs b) {
                        const float t = HH - (dx * dx + dy * dy + dz * dz);
                        bdi += ((t * t) * t) * __ldg(&b.bphi_s[j]);
                    });
-    b.density[i] = c.default_eval * ((di * c.mass_def) + bdi);
+    const float d = c.default_eval * ((di * c.mass_def) + bdi);
+    b.density[i] = d;
+    b.aux[i] = make_float4(0.f, 1.0f / d, d, 0.f);
 }
 
 __global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {

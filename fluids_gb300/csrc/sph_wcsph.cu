@@ -4,6 +4,8 @@
  *   k_wc_density  compute_density_pressure (kernels/wcsph.cl:32-79): rho from fluid and
  *                 boundary (Psi-weighted) poly6 sums, Tait pressure max(0, k((rho/rho0)^7-1)).
  *                 COMPAT evaluates poly6 at r as the kernel text does; PHYSICS at r^2 (P1).
+ *                 Also writes aux = (p/rho^2, 1/rho, rho, p) so the later passes divide by
+ *                 nothing inside their neighbour loops.
  *   k_normals     compute_normals (kernels/normals.cl:23-70), shared with PCISPH.
  *   k_wc_forces   compute_acceleration (kernels/wcsph.cl:81-173): boundary pressure, fluid
  *                 pressure, viscosity and Akinci surface tension, gravity; PHYSICS carries
@@ -11,16 +13,22 @@
  *                 leapfrog integration of predict_vel_n_pos (kernels/wcsph.cl:176-224) runs
  *                 as the epilogue, so the acceleration never round-trips through HBM.
  * One thread per particle in Morton order: the 32 particles of a warp share most of their
- * 27 neighbour cells, so neighbour positions come from L1/L2 rather than HBM.
+ * 27 neighbour cells, so neighbour data comes from L1/L2 rather than HBM.  Inside the
+ * neighbour loops 1/r comes from rsqrtf and 1/rho_j from aux (FP32 results differ from the
+ * reference's IEEE divisions by a few ulp, inside the parity tolerance).
  */
 #include "sph_kernels.cuh"
 
 namespace sph {
 
+__device__ __forceinline__ float4 make_aux(float d, float p) {
+    return make_float4(p / (d * d), 1.0f / d, d, p);
+}
+
 template <bool COMPAT, bool LIST>
-__global__ void __launch_bounds__(256) k_wc_density(Const c, Neigh<LIST> fl, Neigh<LIST> bl,
+__global__ void __launch_bounds__(256) k_wc_density(Const c, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl,
                                                     const float* __restrict__ bphi_s, float* __restrict__ dens,
-                                                    float* __restrict__ pres) {
+                                                    float* __restrict__ pres, float4* __restrict__ aux) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const float4 pi = __ldg(&fl.npos[i]);
@@ -43,11 +51,69 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c, Neigh<LIST> fl, Nei
     di += c.poly6_eval * bdi;
     dens[i] = di;
     const float pv = c.kgas * (pown7(di / c.rho0) - 1.0f);
-    pres[i] = (0.f < pv) ? pv : 0.f;
+    const float p = (0.f < pv) ? pv : 0.f;
+    pres[i] = p;
+    aux[i] = make_aux(di, p);
 }
 
-template <bool LIST>
-__global__ void __launch_bounds__(256) k_normals(Const c, Neigh<LIST> fl, const float* __restrict__ dens,
+/* compute_neigh_list (kernels/grid.cl:145-182, fluid and boundary) fused with
+ * compute_density_pressure: the density sums run over exactly the pairs written to the
+ * lists, in list order, so the step needs no separate density pass. */
+template <bool COMPAT>
+__global__ void __launch_bounds__(256) k_lists_density(Const c, const float4* __restrict__ spos,
+                                                       const int2* __restrict__ tab,
+                                                       const float4* __restrict__ bpos_s,
+                                                       const int2* __restrict__ btab,
+                                                       const float* __restrict__ bphi_s, int* __restrict__ nlist,
+                                                       int* __restrict__ nlen, int* __restrict__ sblist,
+                                                       int* __restrict__ sblen, float* __restrict__ dens,
+                                                       float* __restrict__ pres, float4* __restrict__ aux) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const float4 pi = spos[i];
+    const size_t n = (size_t)c.n;
+    const float hh = c.h * c.h;
+    int k = 0;
+    float di = 0.f;
+    scan_neighbors<true>(c, pi.x, pi.y, pi.z, tab, spos, [&](int j, float4, float dx, float dy, float dz) {
+        nlist[(size_t)k * n + i] = j;
+        ++k;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float t = hh - (COMPAT ? sqrtf(r2) : r2);
+        di += (t * t) * t;
+    });
+    nlen[i] = k;
+    di *= c.poly6_eval * c.mass;
+    int kb = 0;
+    float bdi = 0.f;
+    if (c.nb > 0) {
+        scan_neighbors<true>(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float dx, float dy, float dz) {
+            sblist[(size_t)kb * n + i] = j;
+            ++kb;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float t = hh - (COMPAT ? sqrtf(r2) : r2);
+            bdi += ((t * t) * t) * __ldg(&bphi_s[j]);
+        });
+    }
+    sblen[i] = kb;
+    di += c.poly6_eval * bdi;
+    dens[i] = di;
+    const float pv = c.kgas * (pown7(di / c.rho0) - 1.0f);
+    const float p = (0.f < pv) ? pv : 0.f;
+    pres[i] = p;
+    aux[i] = make_aux(di, p);
+}
+
+/* aux from the density / pressure fields (used when those fields were set from outside). */
+__global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ dens, const float* __restrict__ pres,
+                                             float4* __restrict__ aux) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    aux[i] = make_aux(dens[i], pres[i]);
+}
+
+template <bool LIST, bool EXACT>
+__global__ void __launch_bounds__(256) k_normals(Const c, Neigh<LIST, EXACT> fl, const float4* __restrict__ aux,
                                                  float4* __restrict__ normal) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
@@ -56,15 +122,13 @@ __global__ void __launch_bounds__(256) k_normals(Const c, Neigh<LIST> fl, const 
     float nx = 0.f, ny = 0.f, nz = 0.f;
     fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
         const float t = HH - (dx * dx + dy * dy + dz * dz);
-        const float s = t * t;
-        const float dj = __ldg(&dens[j]);
-        nx += (dx * s) / dj;
-        ny += (dy * s) / dj;
-        nz += (dz * s) / dj;
+        const float k = (t * t) * __ldg(&aux[j].y);
+        nx += dx * k;
+        ny += dy * k;
+        nz += dz * k;
     });
-    const float k = c.poly6_grad;
-    normal[i] = make_float4(((k * nx) * c.mass_def) * H, ((k * ny) * c.mass_def) * H, ((k * nz) * c.mass_def) * H,
-                            0.f);
+    const float k = (c.poly6_grad * c.mass_def) * H;
+    normal[i] = make_float4(nx * k, ny * k, nz * k, 0.f);
 }
 
 /* predict_vel_n_pos (kernels/wcsph.cl:176-224) for one particle. */
@@ -102,68 +166,72 @@ __device__ __forceinline__ void wc_integrate_one(const Const& c, float4 p, float
 }
 
 template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST>
-__global__ void __launch_bounds__(256) k_wc_forces(Const c, Neigh<LIST> fl, Neigh<LIST> bl, Bufs b) {
+__global__ void __launch_bounds__(256) k_wc_forces(Const c, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const float4 pi = __ldg(&b.pos_s[i]);
     const float4 vi = __ldg(&b.vel_s[i]);
-    const float di = __ldg(&b.density[i]), p_i = __ldg(&b.pressure[i]);
-    const float C = p_i / (di * di);
+    const float4 ai = __ldg(&b.aux[i]);
+    const float C = ai.x, di = ai.z;
     const float h = c.h, sg = c.spiky_grad;
     float bax = 0.f, bay = 0.f, baz = 0.f;
     if (c.nb > 0) {
+        const float c2 = 2.0f * C * sg;
         bl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
-            const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
-            const float phi = -__ldg(&b.bphi_s[j]);
-            const float s = sg / rn, t = (h - rn) * (h - rn);
-            bax += ((((phi * dx) * s) * t) * 2.0f) * C;
-            bay += ((((phi * dy) * s) * t) * 2.0f) * C;
-            baz += ((((phi * dz) * s) * t) * 2.0f) * C;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float irn = rsqrtf(r2);
+            const float w = h - r2 * irn;
+            const float k = -__ldg(&b.bphi_s[j]) * (irn * (w * w)) * c2;
+            bax += dx * k;
+            bay += dy * k;
+            baz += dz * k;
         });
     }
     float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ST) ni = __ldg(&b.normal[i]);
     float pax = 0.f, pay = 0.f, paz = 0.f, vax = 0.f, vay = 0.f, vaz = 0.f;
     float cux = 0.f, cuy = 0.f, cuz = 0.f, cox = 0.f, coy = 0.f, coz = 0.f;
-    const float rmin = c.rmin_wc;
+    const float rmin2 = c.rmin2_wc, two_rho0 = 2.0f * c.rho0;
     fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
-        const float dj = __ldg(&b.density[j]);
-        const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
-        if (di > 0.f && dj > 0.f && rn > rmin) {
-            const float pj = __ldg(&b.pressure[j]);
-            const float4 vj = __ldg(&b.vel_s[j]);
-            const float s = sg / rn, t = (h - rn) * (h - rn), q = C + pj / (dj * dj);
-            pax += ((dx * s) * t) * q;
-            pay += ((dy * s) * t) * q;
-            paz += ((dz * s) * t) * q;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float4 aj = __ldg(&b.aux[j]);
+        if (di > 0.f && aj.z > 0.f && r2 > rmin2) {
+            const float irn = rsqrtf(r2);
+            const float rn = r2 * irn;
             const float w = h - rn;
-            vax += ((vj.x - vi.x) * w) / dj;
-            vay += ((vj.y - vi.y) * w) / dj;
-            vaz += ((vj.z - vi.z) * w) / dj;
+            const float q = (sg * irn) * (w * w) * (C + aj.x);
+            pax += dx * q;
+            pay += dy * q;
+            paz += dz * q;
+            const float4 vj = __ldg(&b.vel_s[j]);
+            const float vw = w * aj.y;
+            vax += (vj.x - vi.x) * vw;
+            vay += (vj.y - vi.y) * vw;
+            vaz += (vj.z - vi.z) * vw;
             if (ST) {
                 const float4 nj = __ldg(&b.normal[j]);
-                const float K = st_corr(c.rho0, di, dj);
+                const float K = __fdividef(two_rho0, di + aj.z);
                 cux += (ni.x - nj.x) * K;
                 cuy += (ni.y - nj.y) * K;
                 cuz += (ni.z - nj.z) * K;
-                const float sk = st_kernel(rn, h, c.st_term);
-                cox += ((dx / rn) * sk) * K;
-                coy += ((dy / rn) * sk) * K;
-                coz += ((dz / rn) * sk) * K;
+                const float ck = st_kernel(rn, h, c.st_term) * K * irn;
+                cox += dx * ck;
+                coy += dy * ck;
+                coz += dz * ck;
             }
         }
     });
     const float m = c.mass;
     pax *= -m; pay *= -m; paz *= -m;
-    const float vs = COMPAT ? (c.visc_lapl * c.mu) : (c.visc_lapl * c.mu) * (m / di);
+    const float vs = COMPAT ? (c.visc_lapl * c.mu) : (c.visc_lapl * c.mu) * (m * ai.y);
     vax *= vs; vay *= vs; vaz *= vs;
     float ax = pax + vax + bax, ay = c.g + pay + vay + bay, az = paz + vaz + baz;
     if (ST) {
         const float cs = COMPAT ? c.st_main : c.st_main * m;
         const float ns = -c.sigma;
-        ax = ((((ns * (cux + cox * cs)) + pax) + vax) + bax);
+        ax = (((ns * (cux + cox * cs)) + pax) + vax) + bax;
         ay = (((c.g + ns * (cuy + coy * cs)) + pay) + vay) + bay;
-        az = ((((ns * (cuz + coz * cs)) + paz) + vaz) + baz);
+        az = (((ns * (cuz + coz * cs)) + paz) + vaz) + baz;
     }
     if (WRITE_ACC) b.accel[i] = make_float4(ax, ay, az, 0.f);
     if (FUSE) {
@@ -194,40 +262,61 @@ __global__ void __launch_bounds__(256) k_wc_integrate(Const c, Bufs b) {
 
 static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
 
-template <bool LIST>
-static Neigh<LIST> fluid_src(const Bufs& b) {
-    return Neigh<LIST>{b.tab, b.nlist, b.nlen, b.pos_s};
+template <bool LIST, bool EXACT>
+static Neigh<LIST, EXACT> fluid_src(const Bufs& b) {
+    return Neigh<LIST, EXACT>{b.tab, b.nlist, b.nlen, b.pos_s};
 }
-template <bool LIST>
-static Neigh<LIST> bnd_src(const Bufs& b) {
-    return Neigh<LIST>{b.btab, b.sblist, b.sblen, b.bpos_s};
+template <bool LIST, bool EXACT>
+static Neigh<LIST, EXACT> bnd_src(const Bufs& b) {
+    return Neigh<LIST, EXACT>{b.btab, b.sblist, b.sblen, b.bpos_s};
+}
+
+template <bool COMPAT, bool LIST>
+static void density_dispatch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    k_wc_density<COMPAT, LIST><<<nblk(c.n, bs), bs, 0, s>>>(c, fluid_src<LIST, COMPAT>(b), bnd_src<LIST, COMPAT>(b),
+                                                            b.bphi_s, b.density, b.pressure, b.aux);
 }
 
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs) {
     if (c.n <= 0) return;
-    const int g = nblk(c.n, bs);
     if (c.compat) {
-        if (lists) k_wc_density<true, true><<<g, bs, 0, s>>>(c, fluid_src<true>(b), bnd_src<true>(b), b.bphi_s, b.density, b.pressure);
-        else k_wc_density<true, false><<<g, bs, 0, s>>>(c, fluid_src<false>(b), bnd_src<false>(b), b.bphi_s, b.density, b.pressure);
+        if (lists) density_dispatch<true, true>(s, c, b, bs);
+        else density_dispatch<true, false>(s, c, b, bs);
     } else {
-        if (lists) k_wc_density<false, true><<<g, bs, 0, s>>>(c, fluid_src<true>(b), bnd_src<true>(b), b.bphi_s, b.density, b.pressure);
-        else k_wc_density<false, false><<<g, bs, 0, s>>>(c, fluid_src<false>(b), bnd_src<false>(b), b.bphi_s, b.density, b.pressure);
+        if (lists) density_dispatch<false, true>(s, c, b, bs);
+        else density_dispatch<false, false>(s, c, b, bs);
     }
+}
+
+void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    if (c.compat)
+        k_lists_density<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist,
+                                                           b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux);
+    else
+        k_lists_density<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist,
+                                                            b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux);
+}
+
+void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    k_aux<<<nblk(c.n, bs), bs, 0, s>>>(c.n, b.density, b.pressure, b.aux);
 }
 
 void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs) {
     if (c.n <= 0) return;
     const int g = nblk(c.n, bs);
-    if (lists) k_normals<true><<<g, bs, 0, s>>>(c, fluid_src<true>(b), b.density, b.normal);
-    else k_normals<false><<<g, bs, 0, s>>>(c, fluid_src<false>(b), b.density, b.normal);
+    if (lists) k_normals<true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal);
+    else if (c.compat) k_normals<false, true><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.normal);
+    else k_normals<false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal);
 }
 
 template <bool COMPAT, bool LIST>
 static void forces_dispatch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs) {
     const int g = nblk(c.n, bs);
     const bool st = c.sigma != 0.f;
-    auto fs = fluid_src<LIST>(b);
-    auto bsrc = bnd_src<LIST>(b);
+    auto fs = fluid_src<LIST, COMPAT>(b);
+    auto bsrc = bnd_src<LIST, COMPAT>(b);
 #define SPH_WCF(F, W, S) k_wc_forces<COMPAT, LIST, F, W, S><<<g, bs, 0, s>>>(c, fs, bsrc, b)
     if (fuse) {
         if (write_acc) { if (st) SPH_WCF(true, true, true); else SPH_WCF(true, true, false); }
