@@ -39,7 +39,7 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_synchronize", "sph_device_flags", "sph_field_elems", "sph_field_kind", "sph_get_field",
            "sph_set_field", "sph_field_device_ptr", "sph_body_forces", "sph_stats", "sph_sort_pairs",
            "sph_scene_box_volume", "sph_scene_fishtank", "sph_scene_cube", "sph_jitter", "sph_cuda_available",
-           "sph_describe", "sph_profile_step"]
+           "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc"]
 
 
 class SphParams(C.Structure):
@@ -120,6 +120,7 @@ def lib():
             "sph_cuda_available": (ip, []),
             "sph_describe": (ip, [PP, fp, C.POINTER(SphDerived)]),
             "sph_profile_step": (ip, [vp, ip, C.POINTER(C.c_float), ip, C.POINTER(ip), C.c_char_p, C.c_size_t]),
+            "sph_sort_pairs_noalloc": (ip, [vp, vp, vp, vp, ip, ip, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

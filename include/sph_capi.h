@@ -213,6 +213,20 @@ int sph_stats(sph_ctx* ctx, double* out8);
  * key.  Scratch memory is allocated on first use and cached per device. */
 int sph_sort_pairs(uint32_t* d_keys, int32_t* d_vals, int n, int key_bits, void* cuda_stream);
 
+/* The same stable sort for callers that cannot allocate device memory (no counterpart in
+ * the reference).  Host programs whose own allocator owns the device heap, or that sort
+ * from a callback where an allocation is not allowed, cannot accept the scratch that
+ * sph_sort_pairs allocates; this variant allocates nothing.  The caller passes the input
+ * pairs (only read) and separate output buffers; everything else lives in one fixed
+ * device array of 9,441,792 bytes per GPU, held until the process exits.  At most
+ * SPH_NOALLOC_SORT_MAX_PAIRS pairs (SPH_E_OVERFLOW above that, nothing launched).  The
+ * first call on a device looks up the array's address, so make it before any stream
+ * capture.  All calls on a device share the array: calls that overlap on the GPU race, so
+ * serialise them.  Asynchronous on cuda_stream. */
+#define SPH_NOALLOC_SORT_MAX_PAIRS 1048576
+int sph_sort_pairs_noalloc(const uint32_t* d_keys_in, const int32_t* d_vals_in, uint32_t* d_keys_out,
+                           int32_t* d_vals_out, int n, int key_bits, void* cuda_stream);
+
 /* ---- scene builders (host) ------------------------------------------------------------ */
 
 /* BoxVolume::particles (fluid/simulation/boxvolume.cpp:11-40): fills out4 (capacity cap
