@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--neighbor-mode", type=int, default=1, help="0 = cell scan in every pass, 1 = lists")
+    ap.add_argument("--batched-steps", type=int, default=500, help="0 skips the batched comparison")
     return ap.parse_args()
 
 
@@ -178,6 +179,53 @@ def cpu_baseline(wl_name, mode, sample_steps, sample_desc_prefix, crop=None):
     return {"value": n * sample_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%s: %d steps of %d fluid particles (+%d boundary), %.1f s" % (
                 sample_desc_prefix, sample_steps, n, sum(len(b[0]) for b in w["bodies"]), dt)}
+
+
+def bench_batched(steps, warmup, torch, nscenes=256):
+    """256 independent dam breaks (N log-uniform in [2048, 65536], containers a x 1 x 1 with
+    a ~ U[1, 3], per-scene viscosity and c0): one batched context against looping the plain
+    single-scene solver over the same scenes, both on one stream, same steps."""
+    from fluids_gb300 import capi, workloads
+    scenes = workloads.batched_scenes(nscenes, seed=0)
+    shared = workloads.batched_params()
+    stream = torch.cuda.Stream()
+    b = capi.BatchContext(shared, scenes)
+    b.set_stream(stream.cuda_stream)
+    n = b.particle_count()
+    b.simulate(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.simulate(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    tb = e0.elapsed_time(e1) / 1000.0
+    sb = b.scene_stats()
+    flags_b = b.device_flags()
+    b.close()
+    singles = []
+    for s in scenes:
+        c = workloads.build_scene_context(shared, s)
+        c.set_stream(stream.cuda_stream)
+        singles.append(c)
+    for c in singles:
+        c.simulate(warmup)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for c in singles:
+        c.simulate(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    tl = e0.elapsed_time(e1) / 1000.0
+    sl = np.array([[c.stats()[k] for k in ("mean_compression", "mean_abs_density_error")] for c in singles])
+    for c in singles:
+        c.close()
+    return {"scenes": nscenes, "particles": n, "boundary_particles": int(sum(len(s["boundary"]) for s in scenes)),
+            "steps": steps, "batched_updates_per_s": n * steps / tb, "looped_updates_per_s": n * steps / tl,
+            "speedup": tl / tb, "batched_ms_per_step": 1000 * tb / steps, "looped_ms_per_step": 1000 * tl / steps,
+            "mean_density_error_batched": float(sb[:, 0].mean()), "mean_density_error_looped": float(sl[:, 0].mean()),
+            "mean_abs_density_error_batched": float(sb[:, 1].mean()),
+            "mean_abs_density_error_looped": float(sl[:, 1].mean()), "device_flags": flags_b}
 
 
 def run_reference(args):
@@ -307,6 +355,10 @@ def main():
             te = float(tt.item())
         e2e = {"value": n * k_e2e * world / te, "unit": UNIT, "h2d_bytes_per_step": 48 * n,
                "d2h_bytes_per_step": 48 * n, "steps": k_e2e, "host_buffers": "pinned"}
+    ctx.close()
+    batched = None
+    if args.batched_steps > 0 and args.workload == "wcsph4m":
+        batched = bench_batched(args.batched_steps, max(args.warmup, 3), torch)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         z = w["fluid"][:, 2]
@@ -322,9 +374,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + jitter)",
                 "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk,
-                "kernel_ms_per_step": kern, "device_flags": flags}
+                "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched}
         print(json.dumps(line), flush=True)
-    ctx.close()
     if world > 1:
         dist.destroy_process_group()
 

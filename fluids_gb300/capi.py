@@ -39,7 +39,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_synchronize", "sph_device_flags", "sph_field_elems", "sph_field_kind", "sph_get_field",
            "sph_set_field", "sph_field_device_ptr", "sph_body_forces", "sph_stats", "sph_sort_pairs",
            "sph_scene_box_volume", "sph_scene_fishtank", "sph_scene_cube", "sph_jitter", "sph_cuda_available",
-           "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc"]
+           "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc", "sph_batch_create",
+           "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid"]
 
 
 class SphParams(C.Structure):
@@ -69,6 +70,12 @@ class SphDerived(C.Structure):
         d["grid_origin"] = list(self.grid_origin)
         d["grid_dims"] = list(self.grid_dims)
         return d
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("container", C.c_float * 3), ("k_viscosity", C.c_float), ("gas_stiffness", C.c_float),
+                ("fluid_pos4", C.c_void_p), ("fluid_vel4", C.c_void_p), ("n_fluid", C.c_int),
+                ("boundary_pos4", C.c_void_p), ("n_boundary", C.c_int)]
 
 
 class SphError(RuntimeError):
@@ -121,6 +128,11 @@ def lib():
             "sph_describe": (ip, [PP, fp, C.POINTER(SphDerived)]),
             "sph_profile_step": (ip, [vp, ip, C.POINTER(C.c_float), ip, C.POINTER(ip), C.c_char_p, C.c_size_t]),
             "sph_sort_pairs_noalloc": (ip, [vp, vp, vp, vp, ip, ip, vp]),
+            "sph_batch_create": (ip, [PP, ip, C.POINTER(SceneDesc), C.POINTER(vp)]),
+            "sph_batch_scene_count": (ip, [vp]),
+            "sph_batch_scene_range": (ip, [vp, ip, C.POINTER(ip), C.POINTER(ip)]),
+            "sph_batch_stats": (ip, [vp, C.POINTER(C.c_double), ip]),
+            "sph_batch_scene_grid": (ip, [vp, ip, C.POINTER(C.c_float), C.POINTER(ip), C.POINTER(C.c_longlong)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -210,6 +222,10 @@ class Context:
     def _c(self, rc):
         return check(rc, self.h)
 
+    def set_stream(self, cuda_stream):
+        """Runs this context's work on a caller stream (an integer cudaStream_t)."""
+        self._c(self._lib.sph_set_stream(self.h, C.c_void_p(int(cuda_stream))))
+
     def set_rect_limits(self, w, h, d):
         self._c(self._lib.sph_set_rect_limits(self.h, w, h, d))
 
@@ -298,6 +314,51 @@ class Context:
         keys = ["mean_compression", "mean_abs_density_error", "max_density_error", "kinetic", "potential",
                 "com_x", "com_y", "com_z"]
         return dict(zip(keys, list(out)))
+
+
+class BatchContext(Context):
+    """A batched context (sph_batch_create): ``scenes`` is a list of dicts with keys
+    container (w, h, d), mu, kgas, fluid ((n, 4) array), boundary ((m, 4) array) and
+    optionally vel."""
+
+    def __init__(self, params, scenes):
+        self._lib = lib()
+        keep = []
+        descs = (SceneDesc * len(scenes))()
+        for d, s in zip(descs, scenes):
+            fl = f4(s["fluid"])
+            bd = f4(s["boundary"]) if s.get("boundary") is not None else None
+            vl = f4(s["vel"]) if s.get("vel") is not None else None
+            keep += [fl, bd, vl]
+            for a in range(3):
+                d.container[a] = s["container"][a]
+            d.k_viscosity = s["mu"]
+            d.gas_stiffness = s["kgas"]
+            d.fluid_pos4, d.n_fluid = ptr(fl), len(fl)
+            d.fluid_vel4 = ptr(vl)
+            d.boundary_pos4, d.n_boundary = (ptr(bd), len(bd)) if bd is not None else (None, 0)
+        h = C.c_void_p()
+        check(self._lib.sph_batch_create(C.byref(params), len(scenes), descs, C.byref(h)))
+        self.h = h
+        self.params = params
+        self.nscenes = len(scenes)
+
+    def scene_range(self, s):
+        a, n = C.c_int(), C.c_int()
+        self._c(self._lib.sph_batch_scene_range(self.h, int(s), C.byref(a), C.byref(n)))
+        return a.value, n.value
+
+    def scene_grid(self, s):
+        o = (C.c_float * 3)()
+        d = (C.c_int * 3)()
+        base = C.c_longlong()
+        self._c(self._lib.sph_batch_scene_grid(self.h, int(s), o, d, C.byref(base)))
+        return list(o), list(d), base.value
+
+    def scene_stats(self):
+        out = (C.c_double * (8 * self.nscenes))()
+        self._c(self._lib.sph_batch_stats(self.h, out, self.nscenes))
+        return np.array(out[:], dtype=np.float64).reshape(self.nscenes, 8)
 
 
 def sort_pairs_device(d_keys, d_vals, n, key_bits=32, stream=None):

@@ -52,7 +52,8 @@ __global__ void k_bnd_transform(int nb, const float4* __restrict__ raw, const in
 
 __global__ void k_bnd_phi(Const c, int nb, const float4* __restrict__ bpos_s, const int32_t* __restrict__ body_s,
                           const int2* __restrict__ btab, const int32_t* __restrict__ bmask_s, float phi_coeff,
-                          float* __restrict__ bphi_s, float* __restrict__ bphi) {
+                          float* __restrict__ bphi_s, float* __restrict__ bphi, const SceneDev* __restrict__ scenes,
+                          const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nb) return;
     const float4 pi = bpos_s[i];
@@ -61,6 +62,9 @@ __global__ void k_bnd_phi(Const c, int nb, const float4* __restrict__ bpos_s, co
     Const cu = c;
     cu.cap = 0x7fffffff;
     cu.h2_list = HH;
+    /* batched contexts: one boundary body per scene (scene_of = body ids), binned on that
+     * scene's grid; a single-scene context passes no scene_of */
+    btab += scene_setup(cu, scenes, scene_of, i);
     float del = 0.f;
     scan_neighbors<true>(cu, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float dx, float dy, float dz) {
         if (__ldg(&body_s[j]) == bi) {
@@ -187,6 +191,60 @@ __global__ void k_stats(Const c, const float* __restrict__ dens, const float4* _
     }
 }
 
+/* Per-scene version of k_stats for batched contexts: out[8 * scene + k], same layout.
+ * Scenes are contiguous ranges, so a warp almost always belongs to one scene and reduces
+ * with shuffles before one atomic per quantity. */
+__global__ void k_scene_stats(Const c, const float* __restrict__ dens, const float4* __restrict__ pos,
+                              const float4* __restrict__ vel, const int32_t* __restrict__ scene_of,
+                              double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < c.n;
+    const int s = live ? scene_of[i] : -1;
+    double a[7] = {0, 0, 0, 0, 0, 0, 0};
+    float mx = -3.0e38f;
+    if (live) {
+        const float e = (dens[i] - c.rho0) / c.rho0;
+        a[0] = e > 0.f ? e : 0.f;
+        a[1] = fabsf(e);
+        mx = e;
+        const float4 p = pos[i], v = vel[i];
+        a[2] = 0.5 * (double)c.mass * (double)(v.x * v.x + v.y * v.y + v.z * v.z);
+        a[3] = (double)c.mass * (double)(-c.g) * (double)p.y;
+        a[4] = p.x; a[5] = p.y; a[6] = p.z;
+    }
+    const int s0 = __shfl_sync(0xffffffffu, s, 0);
+    const bool uniform = __all_sync(0xffffffffu, s == s0);
+    if (uniform) {
+        if (s0 < 0) return;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 7; ++k) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if ((threadIdx.x & 31) != 0) return;
+    } else if (s < 0) {
+        return;
+    }
+    double* o = out + 8 * (size_t)(uniform ? s0 : s);
+    atomicAdd(&o[0], a[0]);
+    atomicAdd(&o[1], a[1]);
+    atomicAdd(&o[3], a[2]);
+    atomicAdd(&o[4], a[3]);
+    atomicAdd(&o[5], a[4]);
+    atomicAdd(&o[6], a[5]);
+    atomicAdd(&o[7], a[6]);
+    unsigned u = __float_as_uint(mx);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    atomicMax(reinterpret_cast<unsigned long long*>(&o[2]), (unsigned long long)u);
+}
+
+void launch_scene_stats(cudaStream_t s, const Const& c, const Bufs& b, double* out, int nscenes) {
+    cudaMemsetAsync(out, 0, 8 * sizeof(double) * nscenes, s);
+    if (c.n <= 0) return;
+    k_scene_stats<<<(c.n + 255) / 256, 256, 0, s>>>(c, b.density, b.pos, b.vel, b.scene_of, out);
+}
+
 static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
 
 void launch_bnd_transform(cudaStream_t s, const Bufs& b, int nbodies, int nb, bool compat, bool only_movable,
@@ -198,7 +256,7 @@ void launch_bnd_transform(cudaStream_t s, const Bufs& b, int nbodies, int nb, bo
 void launch_bnd_phi(cudaStream_t s, const Const& c, const Bufs& b, float phi_coeff, int bs) {
     if (c.nb <= 0) return;
     k_bnd_phi<<<nblk(c.nb, bs), bs, 0, s>>>(c, c.nb, b.bpos_s, b.bbody_s, b.btab, b.bmask_sorted, phi_coeff,
-                                            b.bphi_s, b.bphi);
+                                            b.bphi_s, b.bphi, b.scenes, b.scene_of ? b.bbody_s : nullptr);
 }
 void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs) {
     if (c.nb <= 0 || nbodies <= 0) return;

@@ -60,6 +60,17 @@ struct sph_ctx {
     std::vector<cudaEvent_t>* prof = nullptr;   /* set only by sph_profile_step */
     std::vector<const char*> prof_names;
     std::string prof_list;
+    /* batched contexts: one entry per scene (container, viscosity, stiffness, ranges) */
+    struct SceneIn {
+        float lim[3];
+        float mu, kgas;
+        int first, count, first_b, count_b;
+    };
+    std::vector<SceneIn> scene_in;
+    std::vector<sph::SceneDev> h_scenes;
+    sph::SceneDev* d_scenes = nullptr;
+    int32_t* d_scene_of = nullptr;
+    double* d_scene_stats = nullptr;
 };
 
 namespace {
@@ -207,6 +218,46 @@ int derive(sph_ctx* x) {
         c.key_bits = 3 * bits;
     }
     c.ncells = (long long)c.nx * c.ny * c.nz;
+    if (!x->scene_in.empty()) {
+        /* batched: one container-fitted grid per scene, cells concatenated in one table;
+         * sort key = scene id above the Morton bits of the largest grid */
+        if (compat || p.method != SPH_WCSPH)
+            return fail(x, SPH_E_INVALID, "batched contexts run WCSPH in PHYSICS mode");
+        const float m = p.grid_margin > 0.f ? p.grid_margin : 2.0f;
+        x->h_scenes.assign(x->scene_in.size(), sph::SceneDev{});
+        long long base = 0;
+        int mx = 1;
+        for (size_t s = 0; s < x->scene_in.size(); ++s) {
+            const sph_ctx::SceneIn& in = x->scene_in[s];
+            sph::SceneDev& sd = x->h_scenes[s];
+            float o[3];
+            int n[3];
+            for (int a = 0; a < 3; ++a) {
+                const float L = in.lim[a];
+                o[a] = -(L / 2.0f) - m * h;
+                n[a] = std::max(1, (int)std::ceil((L + 2.0f * m * h) / h));
+                mx = std::max(mx, n[a]);
+            }
+            sd.ox = o[0]; sd.oy = o[1]; sd.oz = o[2];
+            sd.nx = n[0]; sd.ny = n[1]; sd.nz = n[2];
+            sd.ncells = (long long)n[0] * n[1] * n[2];
+            sd.cell_base = base;
+            base += sd.ncells;
+            sd.lim_x = in.lim[0]; sd.lim_y = in.lim[1]; sd.lim_z = in.lim[2];
+            sd.mu = in.mu; sd.kgas = in.kgas;
+            sd.first = in.first; sd.count = in.count; sd.first_b = in.first_b; sd.count_b = in.count_b;
+        }
+        int bits = 0;
+        while ((1 << bits) < mx) ++bits;
+        int sbits = 0;
+        while ((1u << sbits) < x->scene_in.size()) ++sbits;
+        if (bits > 10 || 3 * bits + sbits > 32)
+            return fail(x, SPH_E_INVALID, "scene grids too large for 32-bit (scene, Morton) keys");
+        c.batched = 1;
+        c.scene_shift = 3 * bits;
+        c.key_bits = 3 * bits + sbits;
+        c.ncells = base;
+    }
     if (c.ncells > (1LL << 31) - 1) return fail(x, SPH_E_INVALID, "grid has more than 2^31 cells");
     c.n = x->N;
     c.nb = x->NB;
@@ -262,6 +313,14 @@ void carve(sph_ctx* x, Carver& cv) {
     b.pci_maxerr = cv.take<float>((size_t)x->max_iter_slots);
     b.barrier = cv.take<unsigned>(4);
     b.stats = cv.take<double>(8);
+    /* every context has a scene table; a single-scene context has one entry */
+    x->d_scenes = cv.take<sph::SceneDev>(x->scene_in.empty() ? 1 : x->scene_in.size());
+    x->d_scene_of = nullptr;
+    x->d_scene_stats = nullptr;
+    if (!x->scene_in.empty()) {
+        x->d_scene_of = cv.take<int32_t>(n);
+        x->d_scene_stats = cv.take<double>(8 * x->scene_in.size());
+    }
 }
 
 void drop_graph(sph_ctx* x) {
@@ -277,12 +336,15 @@ void boundary_sort(sph_ctx* x) {
     Bufs& b = x->b;
     const cudaStream_t s = x->stream;
     Const cb = x->c;
-    sph::launch_hashes(s, cb, b.bpos, x->NB, b.bkeys, b.bmask, b.btab, b.bcell_prev, b.flags, x->bs);
+    /* batched: the boundary body of scene s is body s, so body ids are scene ids */
+    sph::launch_hashes(s, cb, b.bpos, x->NB, b.bkeys, b.bmask, b.btab, b.bcell_prev, b.flags, x->bs, b.scenes,
+                       b.scene_of ? b.bbody : nullptr);
     sph::sort_pairs(s, b.bkeys, b.bmask, b.bkeys_alt, b.bmask_alt, x->NB, x->c.key_bits, b.bsort_ws, b.flags,
                     x->num_sms, &b.bkeys_sorted, &b.bmask_sorted);
     sph::launch_gather_boundary(s, x->NB, b.bmask_sorted, b.bpos, b.bpos_s, b.bbody, b.bbody_s, b.bphi, b.bphi_s,
                                 x->bs);
-    sph::launch_cell_ranges(s, cb, b.bpos_s, b.bkeys_sorted, x->NB, b.btab, b.bcell_prev, b.flags, x->bs);
+    sph::launch_cell_ranges(s, cb, b.bpos_s, b.bkeys_sorted, x->NB, b.btab, b.bcell_prev, b.flags, x->bs, b.scenes,
+                            b.scene_of ? b.bbody_s : nullptr);
 }
 
 bool uses_lists(const sph_ctx* x) { return x->p.method == SPH_PCISPH || x->p.neighbor_mode == SPH_NEIGH_LIST; }
@@ -300,7 +362,7 @@ int run_stage_impl(sph_ctx* x, int stage) {
         }
         break;
     case SPH_S_HASHES:
-        sph::launch_hashes(s, c, b.pos, x->N, b.keys, b.mask, b.tab, b.cell_prev, b.flags, bs);
+        sph::launch_hashes(s, c, b.pos, x->N, b.keys, b.mask, b.tab, b.cell_prev, b.flags, bs, b.scenes, b.scene_of);
         x->cur_keys = b.keys;
         x->cur_mask = b.mask;
         break;
@@ -315,11 +377,13 @@ int run_stage_impl(sph_ctx* x, int stage) {
                            x->p.method == SPH_WCSPH ? b.vhalf : nullptr, b.vhalf_s, b.ids, b.ids_s, bs);
         break;
     case SPH_S_CELL_INTERVALS:
-        sph::launch_cell_ranges(s, c, b.pos_s, b.keys_sorted, x->N, b.tab, b.cell_prev, b.flags, bs);
+        sph::launch_cell_ranges(s, c, b.pos_s, b.keys_sorted, x->N, b.tab, b.cell_prev, b.flags, bs, b.scenes,
+                                b.scene_of);
         break;
     case SPH_S_NEIGH_LIST:
     case SPH_S_SB_NEIGH_LIST:
-        sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs);
+        sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
+                                b.scenes, b.scene_of);
         break;
     case SPH_S_WC_DENSITY:
         sph::launch_wc_density(s, c, b, x->p.neighbor_mode == SPH_NEIGH_LIST, bs);
@@ -409,7 +473,8 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
         sph::launch_wc_forces(s, c, b, lists, true, false, bs);
         mark(x, "k_wc_forces");
     } else {
-        sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs);
+        sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
+                                b.scenes, b.scene_of);
         mark(x, "k_neigh_lists");
         sph::launch_pci_init_density(s, c, b, bs);
         mark(x, "k_pci_init_density");
@@ -517,6 +582,28 @@ int rebuild(sph_ctx* x, bool keep) {
     SPH_CUDA(x, cudaMemsetAsync(x->arena, 0, x->arena_bytes, s));
     SPH_CUDA(x, cudaMemsetAsync(b.cell_prev, 0xff, sizeof(int32_t) * (x->N > 0 ? x->N : 1), s));
     SPH_CUDA(x, cudaMemsetAsync(b.bcell_prev, 0xff, sizeof(int32_t) * (x->NB > 0 ? x->NB : 1), s));
+    if (x->scene_in.empty()) {
+        /* the one scene of a single-scene context: its grid and parameters */
+        sph::SceneDev sd{};
+        const Const& c = x->c;
+        sd.ox = c.ox; sd.oy = c.oy; sd.oz = c.oz;
+        sd.nx = c.nx; sd.ny = c.ny; sd.nz = c.nz;
+        sd.cell_base = 0;
+        sd.ncells = c.ncells;
+        sd.lim_x = c.lim_x; sd.lim_y = c.lim_y; sd.lim_z = c.lim_z;
+        sd.mu = c.mu; sd.kgas = c.kgas;
+        sd.first = 0; sd.count = x->N; sd.first_b = 0; sd.count_b = x->NB;
+        x->h_scenes.assign(1, sd);
+    } else {
+        std::vector<int32_t> so(x->N > 0 ? x->N : 1, 0);
+        for (size_t sc = 0; sc < x->scene_in.size(); ++sc)
+            for (int i = 0; i < x->scene_in[sc].count; ++i) so[x->scene_in[sc].first + i] = (int32_t)sc;
+        SPH_CUDA(x, cudaMemcpyAsync(x->d_scene_of, so.data(), 4 * so.size(), cudaMemcpyHostToDevice, s));
+        b.scene_of = x->d_scene_of;
+    }
+    SPH_CUDA(x, cudaMemcpyAsync(x->d_scenes, x->h_scenes.data(), sizeof(sph::SceneDev) * x->h_scenes.size(),
+                                cudaMemcpyHostToDevice, s));
+    b.scenes = x->d_scenes;
     if (x->N > 0) {
         std::vector<float> p4(x->vol_pos), v4(x->vol_vel);
         std::vector<int32_t> ids(x->N);
@@ -713,6 +800,107 @@ void sph_default_params(int method, sph_params* p) {
     }
 }
 
+int sph_batch_create(const sph_params* params, int nscenes, const sph_scene_desc* scenes, sph_ctx** out) {
+    if (!params || !scenes || !out || nscenes <= 0) return fail(nullptr, SPH_E_INVALID, "null argument or no scenes");
+    *out = nullptr;
+    if (params->method != SPH_WCSPH || params->mode != SPH_MODE_PHYSICS)
+        return fail(nullptr, SPH_E_INVALID, "batched contexts run WCSPH in PHYSICS mode");
+    if (nscenes > 65536) return fail(nullptr, SPH_E_OVERFLOW, "more than 65536 scenes");
+    sph_ctx* x = nullptr;
+    int rc = sph_create(params, &x);
+    if (rc != SPH_OK) return rc;
+    long long nf = 0, nb = 0;
+    for (int s = 0; s < nscenes; ++s) {
+        const sph_scene_desc& d = scenes[s];
+        if (d.n_fluid < 0 || d.n_boundary < 0 || (d.n_fluid > 0 && !d.fluid_pos4) ||
+            (d.n_boundary > 0 && !d.boundary_pos4) || !(d.container[0] > 0.f && d.container[1] > 0.f &&
+                                                         d.container[2] > 0.f)) {
+            sph_destroy(x);
+            return fail(nullptr, SPH_E_INVALID, "scene " + std::to_string(s) + ": bad description");
+        }
+        sph_ctx::SceneIn in;
+        for (int a = 0; a < 3; ++a) in.lim[a] = d.container[a];
+        in.mu = d.k_viscosity;
+        in.kgas = d.gas_stiffness;
+        in.first = (int)nf;
+        in.count = d.n_fluid;
+        in.first_b = (int)nb;
+        in.count_b = d.n_boundary;
+        x->scene_in.push_back(in);
+        x->vol_pos.insert(x->vol_pos.end(), d.fluid_pos4, d.fluid_pos4 + 4 * (size_t)d.n_fluid);
+        const size_t old = x->vol_vel.size();
+        x->vol_vel.resize(old + 4 * (size_t)d.n_fluid, 0.f);
+        if (d.fluid_vel4 && d.n_fluid > 0) std::memcpy(&x->vol_vel[old], d.fluid_vel4, 16 * (size_t)d.n_fluid);
+        /* one static boundary body per scene (identity transform), so body id = scene id */
+        SphBody bd;
+        bd.origin = (int)nb;
+        bd.count = d.n_boundary;
+        static const float I[20] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        std::memcpy(bd.xf, I, sizeof bd.xf);
+        x->bodies.push_back(bd);
+        if (d.n_boundary > 0)
+            x->braw_host.insert(x->braw_host.end(), d.boundary_pos4, d.boundary_pos4 + 4 * (size_t)d.n_boundary);
+        nf += d.n_fluid;
+        nb += d.n_boundary;
+        if (nf > 0x3fffffff || nb > 0x3fffffff) {
+            sph_destroy(x);
+            return fail(nullptr, SPH_E_OVERFLOW, "more than 2^30 particles");
+        }
+    }
+    rc = rebuild(x, false);
+    if (rc != SPH_OK) {
+        std::string m = x->err;
+        sph_destroy(x);
+        return fail(nullptr, rc, m);
+    }
+    *out = x;
+    return SPH_OK;
+}
+
+int sph_batch_scene_count(const sph_ctx* x) { return x ? (int)x->scene_in.size() : 0; }
+
+int sph_batch_scene_range(const sph_ctx* x, int scene, int* first, int* count) {
+    if (!x || scene < 0 || scene >= (int)x->scene_in.size() || !first || !count) return SPH_E_INVALID;
+    *first = x->scene_in[scene].first;
+    *count = x->scene_in[scene].count;
+    return SPH_OK;
+}
+
+int sph_batch_scene_grid(const sph_ctx* x, int scene, float* origin3, int* dims3, long long* cell_base) {
+    if (!x || scene < 0 || scene >= (int)x->h_scenes.size() || !origin3 || !dims3) return SPH_E_INVALID;
+    const sph::SceneDev& sd = x->h_scenes[scene];
+    origin3[0] = sd.ox; origin3[1] = sd.oy; origin3[2] = sd.oz;
+    dims3[0] = sd.nx; dims3[1] = sd.ny; dims3[2] = sd.nz;
+    if (cell_base) *cell_base = sd.cell_base;
+    return SPH_OK;
+}
+
+int sph_batch_stats(sph_ctx* x, double* out8, int nscenes) {
+    if (check_ctx(x) || !out8) return SPH_E_INVALID;
+    if (x->scene_in.empty()) return fail(x, SPH_E_STATE, "not a batched context");
+    if (nscenes != (int)x->scene_in.size()) return fail(x, SPH_E_INVALID, "nscenes must equal the scene count");
+    sph::launch_scene_stats(x->stream, x->c, x->b, x->d_scene_stats, nscenes);
+    SPH_CUDA(x, cudaGetLastError());
+    std::vector<double> raw(8 * (size_t)nscenes);
+    SPH_CUDA(x, cudaStreamSynchronize(x->stream));
+    SPH_CUDA(x, cudaMemcpy(raw.data(), x->d_scene_stats, 8 * sizeof(double) * nscenes, cudaMemcpyDeviceToHost));
+    for (int s = 0; s < nscenes; ++s) {
+        const double* r = &raw[8 * (size_t)s];
+        double* o = out8 + 8 * (size_t)s;
+        const double n = x->scene_in[s].count > 0 ? (double)x->scene_in[s].count : 1.0;
+        unsigned long long bits;
+        std::memcpy(&bits, &r[2], 8);
+        unsigned u = (unsigned)bits;
+        u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+        float mx;
+        std::memcpy(&mx, &u, 4);
+        o[0] = r[0] / n; o[1] = r[1] / n; o[2] = x->scene_in[s].count > 0 ? (double)mx : 0.0;
+        o[3] = r[3]; o[4] = r[4];
+        o[5] = r[5] / n; o[6] = r[6] / n; o[7] = r[7] / n;
+    }
+    return SPH_OK;
+}
+
 int sph_describe(const sph_params* params, const float container3[3], sph_derived* out) {
     if (!params || !out) return SPH_E_INVALID;
     sph_ctx tmp;
@@ -815,6 +1003,7 @@ int sph_reset(sph_ctx* x, const sph_params* params) {
 
 int sph_set_rect_limits(sph_ctx* x, float w, float h, float d) {
     if (check_ctx(x)) return SPH_E_INVALID;
+    if (!x->scene_in.empty()) return fail(x, SPH_E_STATE, "a batched context sets containers per scene");
     if (!(w > 0.f && h > 0.f && d > 0.f)) return fail(x, SPH_E_INVALID, "container extents must be > 0");
     x->lim[0] = w; x->lim[1] = h; x->lim[2] = d;
     if (!x->has_state) return derive(x);
@@ -823,6 +1012,7 @@ int sph_set_rect_limits(sph_ctx* x, float w, float h, float d) {
 
 int sph_add_volume(sph_ctx* x, const float* pos4, const float* vel4, int n) {
     if (check_ctx(x)) return SPH_E_INVALID;
+    if (!x->scene_in.empty()) return fail(x, SPH_E_STATE, "a batched context takes its particles at creation");
     if (n < 0 || (n > 0 && !pos4)) return fail(x, SPH_E_INVALID, "bad particle array");
     const size_t old = x->vol_pos.size();
     x->vol_pos.insert(x->vol_pos.end(), pos4, pos4 + 4 * (size_t)n);
@@ -837,6 +1027,7 @@ int sph_add_volume(sph_ctx* x, const float* pos4, const float* vel4, int n) {
 int sph_add_boundary(sph_ctx* x, const float* pos4, int n, int can_move, const float* rot3x4, const float* lin4,
                      const float* ang4, float mass) {
     if (check_ctx(x)) return SPH_E_INVALID;
+    if (!x->scene_in.empty()) return fail(x, SPH_E_STATE, "a batched context takes its boundaries at creation");
     if (n <= 0 || !pos4) return fail(x, SPH_E_INVALID, "bad boundary array");
     SphBody bd;
     bd.origin = (int)(x->braw_host.size() / 4);

@@ -35,7 +35,39 @@ struct Const {
     float rmin_wc;       /* largest float <= 1e-5: wcsph.cl:152 compares r > 0.00001 (a double) */
     float rmin2_wc;      /* rmin_wc^2: the same guard on r^2 */
     float cull2;         /* (h_list / cell)^2 * (1 + 1e-4): face-distance bound for skipping cells */
+    int batched;         /* 1: per-scene grid and parameters from a SceneDev table */
+    int scene_shift;     /* Morton bits below the scene id in the sort key */
 };
+
+/* One scene of a batched context: its grid (origin, dimensions, offset of its cells in the
+ * concatenated cell table), its parameters and its particle range. */
+struct SceneDev {
+    float ox, oy, oz, lim_x;
+    int nx, ny, nz, first;
+    long long cell_base, ncells;
+    float lim_y, lim_z, mu, kgas;
+    int count, first_b, count_b, pad;
+};
+
+/* The constants of the scene a particle belongs to: grid, viscosity, stiffness, container. */
+__device__ __forceinline__ void apply_scene(Const& c, const SceneDev& s) {
+    c.ox = s.ox; c.oy = s.oy; c.oz = s.oz;
+    c.nx = s.nx; c.ny = s.ny; c.nz = s.nz;
+    c.ncells = s.ncells;
+    c.mu = s.mu; c.kgas = s.kgas;
+    c.lim_x = s.lim_x; c.lim_y = s.lim_y; c.lim_z = s.lim_z;
+}
+/* Switches c to particle i's scene and returns that scene's offset in the cell tables.
+ * Every context has a scene table (one entry for a single scene, scene_of null), and the
+ * update is unconditional: with nvcc 13.0 for sm_103a at -O3, updating a copy of the
+ * by-value kernel parameter only under a condition (if (table) ...) left the first member
+ * (ox) at the parameter's value, while an unconditional update keeps every member. */
+__device__ __forceinline__ long long scene_setup(Const& c, const SceneDev* scenes, const int32_t* scene_of, int i) {
+    const int sid = scene_of ? scene_of[i] : 0;
+    const SceneDev& sd = scenes[sid];
+    apply_scene(c, sd);
+    return sd.cell_base;
+}
 
 constexpr unsigned kFlagNan = 1u, kFlagEscaped = 2u, kFlagTimeout = 4u, kFlagOverflow = 8u,
                    kFlagNonconverged = 16u;

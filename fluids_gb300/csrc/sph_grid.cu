@@ -17,19 +17,24 @@
 
 namespace sph {
 
-__global__ void k_hashes(Const c, const float4* __restrict__ pos, int n, uint32_t* __restrict__ keys,
+__global__ void k_hashes(Const c0, const float4* __restrict__ pos, int n, uint32_t* __restrict__ keys,
                          int32_t* __restrict__ mask, int2* __restrict__ tab, const int32_t* __restrict__ cell_prev,
-                         unsigned* __restrict__ flags) {
+                         unsigned* __restrict__ flags, const SceneDev* __restrict__ scenes,
+                         const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (cell_prev) {
         const int pc = cell_prev[i];
         if (pc >= 0) tab[pc] = make_int2(0, 0);
     }
+    Const c = c0;
+    const uint32_t sid = scene_of ? (uint32_t)scene_of[i] : 0u;
+    scene_setup(c, scenes, scene_of, i);
     const float4 p = pos[i];
     int cx, cy, cz;
     cell_of(c, p.x, p.y, p.z, cx, cy, cz);
-    keys[i] = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+    /* batched: the scene id above the Morton bits keeps every scene's range contiguous */
+    keys[i] = (sid << c.scene_shift) | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
     mask[i] = i;
     if (!c.wrap) {
         /* PHYSICS grid clamps: report particles outside it (informational) */
@@ -67,16 +72,26 @@ __global__ void k_gather_boundary(int n, const int32_t* __restrict__ perm, const
     if (phi) phi_s[i] = phi[src];
 }
 
+/* Global cell id of a sorted particle: linear id in its scene's grid + the scene's offset;
+ * -1 when outside the table. */
+__device__ __forceinline__ long long global_cell(const Const& c0, const float4& p, const SceneDev* scenes,
+                                                 const int32_t* scene_of, int i) {
+    Const c = c0;
+    const long long base = scene_setup(c, scenes, scene_of, i);
+    int x, y, z;
+    cell_of(c, p.x, p.y, p.z, x, y, z);
+    const long long id = cell_lin(c, x, y, z);
+    return (id >= 0 && id < c.ncells) ? base + id : -1;
+}
+
 __global__ void k_cell_ranges(Const c, const float4* __restrict__ spos, const uint32_t* __restrict__ keys, int n,
-                              int2* __restrict__ tab, int32_t* __restrict__ cell_out, unsigned* __restrict__ flags) {
+                              int2* __restrict__ tab, int32_t* __restrict__ cell_out, unsigned* __restrict__ flags,
+                              const SceneDev* __restrict__ scenes, const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int* t = reinterpret_cast<int*>(tab);
-    const float4 p0 = spos[i];
-    int x, y, z;
-    cell_of(c, p0.x, p0.y, p0.z, x, y, z);
-    const long long id0 = cell_lin(c, x, y, z);
-    const bool ok0 = id0 >= 0 && id0 < c.ncells;
+    const long long id0 = global_cell(c, spos[i], scenes, scene_of, i);
+    const bool ok0 = id0 >= 0;
     if (!ok0) atomicOr(flags, kFlagEscaped);
     cell_out[i] = ok0 ? (int)id0 : -1;
     if (i == n - 1) {
@@ -84,20 +99,24 @@ __global__ void k_cell_ranges(Const c, const float4* __restrict__ spos, const ui
     } else {
         const uint32_t h0 = keys[i], h1 = keys[i + 1];
         if (h0 < h1) {
-            const float4 p1 = spos[i + 1];
-            cell_of(c, p1.x, p1.y, p1.z, x, y, z);
-            const long long id1 = cell_lin(c, x, y, z);
+            const long long id1 = global_cell(c, spos[i + 1], scenes, scene_of, i + 1);
             if (ok0) t[2 * id0 + 1] = i + 1;
-            if (id1 >= 0 && id1 < c.ncells) t[2 * id1] = i + 1;
+            if (id1 >= 0) t[2 * id1] = i + 1;
         }
     }
 }
 
-__global__ void k_neigh_lists(Const c, const float4* __restrict__ spos, const int2* __restrict__ tab,
-                              const float4* __restrict__ bpos_s, const int2* __restrict__ btab, int* __restrict__ nlist,
-                              int* __restrict__ nlen, int* __restrict__ sblist, int* __restrict__ sblen) {
+__global__ void k_neigh_lists(Const c0, const float4* __restrict__ spos, const int2* __restrict__ tab0,
+                              const float4* __restrict__ bpos_s, const int2* __restrict__ btab0,
+                              int* __restrict__ nlist, int* __restrict__ nlen, int* __restrict__ sblist,
+                              int* __restrict__ sblen, const SceneDev* __restrict__ scenes,
+                              const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    if (i >= c0.n) return;
+    Const c = c0;
+    const long long base = scene_setup(c, scenes, scene_of, i);
+    const int2* tab = tab0 + base;
+    const int2* btab = btab0 + base;
     const float4 pi = spos[i];
     const size_t n = (size_t)c.n;
     int k = 0;
@@ -119,9 +138,10 @@ __global__ void k_neigh_lists(Const c, const float4* __restrict__ spos, const in
 static inline int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 void launch_hashes(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int32_t* mask,
-                   int2* tab, const int32_t* cell_prev, unsigned* flags, int bs) {
+                   int2* tab, const int32_t* cell_prev, unsigned* flags, int bs, const SceneDev* scenes,
+                   const int32_t* scene_of) {
     if (n <= 0) return;
-    k_hashes<<<blocks_for(n, bs), bs, 0, s>>>(c, pos, n, keys, mask, tab, cell_prev, flags);
+    k_hashes<<<blocks_for(n, bs), bs, 0, s>>>(c, pos, n, keys, mask, tab, cell_prev, flags, scenes, scene_of);
 }
 void launch_gather(cudaStream_t s, int n, const int32_t* perm, const float4* a, float4* as, const float4* b,
                    float4* bs_, const float4* c3, float4* cs, const int32_t* ids, int32_t* ids_s, int bs) {
@@ -134,14 +154,17 @@ void launch_gather_boundary(cudaStream_t s, int n, const int32_t* perm, const fl
     k_gather_boundary<<<blocks_for(n, bs), bs, 0, s>>>(n, perm, pos, pos_s, body, body_s, phi, phi_s);
 }
 void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, const uint32_t* keys, int n,
-                        int2* tab, int32_t* cell_out, unsigned* flags, int bs) {
+                        int2* tab, int32_t* cell_out, unsigned* flags, int bs, const SceneDev* scenes,
+                        const int32_t* scene_of) {
     if (n <= 0) return;
-    k_cell_ranges<<<blocks_for(n, bs), bs, 0, s>>>(c, spos, keys, n, tab, cell_out, flags);
+    k_cell_ranges<<<blocks_for(n, bs), bs, 0, s>>>(c, spos, keys, n, tab, cell_out, flags, scenes, scene_of);
 }
 void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, const int2* tab, const float4* bpos_s,
-                        const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs) {
+                        const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs,
+                        const SceneDev* scenes, const int32_t* scene_of) {
     if (c.n <= 0) return;
-    k_neigh_lists<<<blocks_for(c.n, bs), bs, 0, s>>>(c, spos, tab, bpos_s, btab, nlist, nlen, sblist, sblen);
+    k_neigh_lists<<<blocks_for(c.n, bs), bs, 0, s>>>(c, spos, tab, bpos_s, btab, nlist, nlen, sblist, sblen, scenes,
+                                                     scene_of);
 }
 
 }  // namespace sph

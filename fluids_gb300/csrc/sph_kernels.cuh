@@ -41,6 +41,9 @@ struct Bufs {
     float* body_xf;                        /* 20 floats per body: rot3x4, lin4, ang4 */
     int32_t* body_range;                   /* origin, count, can_move, has_mass per body */
     float4 *body_force, *body_torque;
+    /* batched contexts: scene table and the scene of each fluid particle (ranges never move) */
+    const SceneDev* scenes;
+    const int32_t* scene_of;
     /* status */
     unsigned* flags;
     int32_t* pci_iters;
@@ -56,16 +59,21 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
                 void* ws, unsigned* flags, int num_sms, uint32_t** kres, int32_t** vres);
 
 /* sph_grid.cu */
+/* scenes: the context's scene table (never null); scene_of: scene of each particle, or
+ * null for a single-scene context. */
 void launch_hashes(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int32_t* mask,
-                   int2* tab, const int32_t* cell_prev, unsigned* flags, int bs);
+                   int2* tab, const int32_t* cell_prev, unsigned* flags, int bs, const SceneDev* scenes,
+                   const int32_t* scene_of);
 void launch_gather(cudaStream_t s, int n, const int32_t* perm, const float4* a, float4* as, const float4* b,
                    float4* bs_, const float4* c3, float4* cs, const int32_t* ids, int32_t* ids_s, int bs);
 void launch_gather_boundary(cudaStream_t s, int n, const int32_t* perm, const float4* pos, float4* pos_s,
                             const int32_t* body, int32_t* body_s, const float* phi, float* phi_s, int bs);
 void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, const uint32_t* keys, int n,
-                        int2* tab, int32_t* cell_out, unsigned* flags, int bs);
+                        int2* tab, int32_t* cell_out, unsigned* flags, int bs, const SceneDev* scenes,
+                        const int32_t* scene_of);
 void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, const int2* tab, const float4* bpos_s,
-                        const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs);
+                        const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs,
+                        const SceneDev* scenes, const int32_t* scene_of);
 
 /* sph_wcsph.cu */
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);
@@ -90,5 +98,6 @@ void launch_bnd_transform(cudaStream_t s, const Bufs& b, int nbodies, int nb, bo
 void launch_bnd_phi(cudaStream_t s, const Const& c, const Bufs& b, float phi_coeff, int bs);
 void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs);
 void launch_stats(cudaStream_t s, const Const& c, const Bufs& b);
+void launch_scene_stats(cudaStream_t s, const Const& c, const Bufs& b, double* out, int nscenes);
 
 }  // namespace sph

@@ -26,11 +26,17 @@ __device__ __forceinline__ float4 make_aux(float d, float p) {
 }
 
 template <bool COMPAT, bool LIST>
-__global__ void __launch_bounds__(256) k_wc_density(Const c, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl,
+__global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl,
                                                     const float* __restrict__ bphi_s, float* __restrict__ dens,
-                                                    float* __restrict__ pres, float4* __restrict__ aux) {
+                                                    float* __restrict__ pres, float4* __restrict__ aux,
+                                                    const SceneDev* __restrict__ scenes,
+                                                    const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    if (i >= c0.n) return;
+    Const c = c0;
+    const long long base = scene_setup(c, scenes, scene_of, i);
+    fl.tab += base;
+    bl.tab += base;
     const float4 pi = __ldg(&fl.npos[i]);
     const float hh = c.h * c.h;
     float di = 0.f;
@@ -60,16 +66,22 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c, Neigh<LIST, COMPAT>
  * compute_density_pressure: the density sums run over exactly the pairs written to the
  * lists, in list order, so the step needs no separate density pass. */
 template <bool COMPAT>
-__global__ void __launch_bounds__(256) k_lists_density(Const c, const float4* __restrict__ spos,
+__global__ void __launch_bounds__(256) k_lists_density(Const c0, const float4* __restrict__ spos,
                                                        const int2* __restrict__ tab,
                                                        const float4* __restrict__ bpos_s,
                                                        const int2* __restrict__ btab,
                                                        const float* __restrict__ bphi_s, int* __restrict__ nlist,
                                                        int* __restrict__ nlen, int* __restrict__ sblist,
                                                        int* __restrict__ sblen, float* __restrict__ dens,
-                                                       float* __restrict__ pres, float4* __restrict__ aux) {
+                                                       float* __restrict__ pres, float4* __restrict__ aux,
+                                                       const SceneDev* __restrict__ scenes,
+                                                       const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    if (i >= c0.n) return;
+    Const c = c0;
+    const long long base = scene_setup(c, scenes, scene_of, i);
+    tab += base;
+    btab += base;
     const float4 pi = spos[i];
     const size_t n = (size_t)c.n;
     const float hh = c.h * c.h;
@@ -113,10 +125,13 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
 }
 
 template <bool LIST, bool EXACT>
-__global__ void __launch_bounds__(256) k_normals(Const c, Neigh<LIST, EXACT> fl, const float4* __restrict__ aux,
-                                                 float4* __restrict__ normal) {
+__global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl, const float4* __restrict__ aux,
+                                                 float4* __restrict__ normal, const SceneDev* __restrict__ scenes,
+                                                 const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    if (i >= c0.n) return;
+    Const c = c0;
+    fl.tab += scene_setup(c, scenes, scene_of, i);
     const float4 pi = __ldg(&fl.npos[i]);
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
@@ -166,9 +181,13 @@ __device__ __forceinline__ void wc_integrate_one(const Const& c, float4 p, float
 }
 
 template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST>
-__global__ void __launch_bounds__(256) k_wc_forces(Const c, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
+__global__ void __launch_bounds__(256) k_wc_forces(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    if (i >= c0.n) return;
+    Const c = c0;
+    const long long base = scene_setup(c, b.scenes, b.scene_of, i);
+    fl.tab += base;
+    bl.tab += base;
     const float4 pi = __ldg(&b.pos_s[i]);
     const float4 vi = __ldg(&b.vel_s[i]);
     const float4 ai = __ldg(&b.aux[i]);
@@ -246,9 +265,11 @@ __global__ void __launch_bounds__(256) k_wc_forces(Const c, Neigh<LIST, COMPAT> 
     }
 }
 
-__global__ void __launch_bounds__(256) k_wc_integrate(Const c, Bufs b) {
+__global__ void __launch_bounds__(256) k_wc_integrate(Const c0, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    if (i >= c0.n) return;
+    Const c = c0;
+    scene_setup(c, b.scenes, b.scene_of, i);
     const float4 a = __ldg(&b.accel[i]);
     float4 po, vo, vho;
     bool bad;
@@ -274,7 +295,8 @@ static Neigh<LIST, EXACT> bnd_src(const Bufs& b) {
 template <bool COMPAT, bool LIST>
 static void density_dispatch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     k_wc_density<COMPAT, LIST><<<nblk(c.n, bs), bs, 0, s>>>(c, fluid_src<LIST, COMPAT>(b), bnd_src<LIST, COMPAT>(b),
-                                                            b.bphi_s, b.density, b.pressure, b.aux);
+                                                            b.bphi_s, b.density, b.pressure, b.aux, b.scenes,
+                                                            b.scene_of);
 }
 
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs) {
@@ -292,10 +314,12 @@ void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs)
     if (c.n <= 0) return;
     if (c.compat)
         k_lists_density<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist,
-                                                           b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux);
+                                                           b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux,
+                                                           b.scenes, b.scene_of);
     else
         k_lists_density<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist,
-                                                            b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux);
+                                                            b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux,
+                                                            b.scenes, b.scene_of);
 }
 
 void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
@@ -306,9 +330,13 @@ void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
 void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs) {
     if (c.n <= 0) return;
     const int g = nblk(c.n, bs);
-    if (lists) k_normals<true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal);
-    else if (c.compat) k_normals<false, true><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.normal);
-    else k_normals<false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal);
+    if (lists)
+        k_normals<true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes, b.scene_of);
+    else if (c.compat)
+        k_normals<false, true><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.normal, b.scenes, b.scene_of);
+    else
+        k_normals<false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal, b.scenes,
+                                                 b.scene_of);
 }
 
 template <bool COMPAT, bool LIST>

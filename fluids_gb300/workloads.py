@@ -82,6 +82,49 @@ def pcisph_cube(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=500, dx=0.0125, **kw):
                 bodies=bodies, container=container, steps=steps, dx=dx)
 
 
+def batched_scenes(nscenes=256, seed=0, dx=0.015, nmin=2048, nmax=65536):
+    """Independent dam breaks of uneven size: N log-uniform in [nmin, nmax], container
+    (a, 1, 1) with a ~ U[1, 3], viscosity log-uniform in [1e-3, 1e-1], c0 ~ U[10, 40] m/s.
+    Each block has aspect ~1:2:1 and rests on the floor against the +x wall."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for s in range(nscenes):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        a = float(rng.uniform(1.0, 3.0))
+        mu = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-1))))
+        c0 = float(rng.uniform(10.0, 40.0))
+        nx = max(2, int(round((n / 2.0) ** (1.0 / 3.0))))
+        ny = max(2, min(64, int(round(n / (nx * nx)))))
+        container = (a, 1.0, 1.0)
+        fluid = dam_break(nx, ny, nx, dx, container, seed=seed * 100003 + s)
+        walls = FishTank(*container).surface_sampling(dx)
+        scenes.append(dict(container=container, mu=mu, kgas=tait_stiffness(c0), c0=c0, fluid=fluid,
+                           boundary=walls, vel=None))
+    return scenes
+
+
+def batched_params(dx=0.015, dt=2e-4, **kw):
+    """Shared parameters of the batched scenes (viscosity and stiffness come per scene)."""
+    return wcsph_params(dx, dt, capi.SPH_MODE_PHYSICS, **kw)
+
+
+def scene_params(shared, scene):
+    """The single-scene parameters equal to one scene of a batch."""
+    p = capi.SphParams.from_buffer_copy(shared)
+    p.k_viscosity = scene["mu"]
+    p.gas_stiffness = scene["kgas"]
+    return p
+
+
+def build_scene_context(shared, scene):
+    """A plain single-scene context for one scene of a batch."""
+    ctx = capi.Context(scene_params(shared, scene))
+    ctx.set_rect_limits(*scene["container"])
+    ctx.add_boundary(scene["boundary"])
+    ctx.add_volume(scene["fluid"], scene.get("vel"))
+    return ctx
+
+
 def build_context(w, params=None):
     """Creates a context and loads a workload: limits, boundaries, then the fluid."""
     ctx = capi.Context(params if params is not None else w["params"])

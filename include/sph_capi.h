@@ -206,6 +206,37 @@ int sph_body_forces(sph_ctx* ctx, float* force4, float* torque4, int bodies);
  * of mass x, y, z.  Computed on the device; synchronises. */
 int sph_stats(sph_ctx* ctx, double* out8);
 
+/* ---- batched scenes ------------------------------------------------------------------- */
+
+/* One independent scene of a batched context (the reference runs one FluidSimulation per
+ * Fluid, scene/fluid.cpp:32; a batch runs many in one launch per stage). */
+typedef struct sph_scene_desc {
+    float container[3];          /* set_rect_limits of this scene */
+    float k_viscosity;           /* per-scene viscosity */
+    float gas_stiffness;         /* per-scene Tait stiffness k = rho0 c0^2 / gamma */
+    const float* fluid_pos4;     /* n_fluid float4 particles */
+    const float* fluid_vel4;     /* initial velocities or NULL */
+    int n_fluid;
+    const float* boundary_pos4;  /* static boundary particles, world coordinates */
+    int n_boundary;
+} sph_scene_desc;
+
+/* Creates a context that advances nscenes independent WCSPH scenes (PHYSICS mode) with one
+ * launch per stage: every scene keeps its own grid, container, viscosity and stiffness,
+ * and its particles stay in one contiguous range of the arrays (the sort key puts the scene
+ * id above the Morton bits, which makes the one sort a segmented sort).  The other
+ * parameters are shared.  sph_simulate / sph_get_field work as for one scene. */
+int sph_batch_create(const sph_params* params, int nscenes, const sph_scene_desc* scenes, sph_ctx** out);
+/* Number of scenes (0 for a single-scene context). */
+int sph_batch_scene_count(const sph_ctx* ctx);
+/* Particle range [first, first + count) of a scene in every fluid field. */
+int sph_batch_scene_range(const sph_ctx* ctx, int scene, int* first, int* count);
+/* Grid of a scene (Grid::info, grid.h:66-118): origin, cells per axis, offset of its cells
+ * in the concatenated cell table. */
+int sph_batch_scene_grid(const sph_ctx* ctx, int scene, float* origin3, int* dims3, long long* cell_base);
+/* sph_stats for every scene: out8[8 * scene + k]; synchronises. */
+int sph_batch_stats(sph_ctx* ctx, double* out8, int nscenes);
+
 /* ---- primitives ---------------------------------------------------------------------- */
 
 /* clsort<cl_uint, cl_int> (opencl/algorithms/clsort.h:13-35): stable ascending sort of n
