@@ -60,13 +60,20 @@ __device__ __forceinline__ void apply_scene(Const& c, const SceneDev& s) {
 /* Switches c to particle i's scene and returns that scene's offset in the cell tables.
  * Every context has a scene table (one entry for a single scene, scene_of null), and the
  * update is unconditional: with nvcc 13.0 for sm_103a at -O3, updating a copy of the
- * by-value kernel parameter only under a condition (if (table) ...) left the first member
- * (ox) at the parameter's value, while an unconditional update keeps every member. */
+ * by-value kernel parameter only under a runtime condition (if (table) ...) left the first
+ * member (ox) at the parameter's value, while an unconditional update keeps every member. */
 __device__ __forceinline__ long long scene_setup(Const& c, const SceneDev* scenes, const int32_t* scene_of, int i) {
     const int sid = scene_of ? scene_of[i] : 0;
     const SceneDev& sd = scenes[sid];
     apply_scene(c, sd);
     return sd.cell_base;
+}
+/* Compile-time choice: single-scene kernels (BATCH = false) use the parameter's grid and
+ * carry no scene code at all; batched kernels always apply the particle's scene. */
+template <bool BATCH>
+__device__ __forceinline__ long long scene_setup_t(Const& c, const SceneDev* scenes, const int32_t* scene_of, int i) {
+    if constexpr (BATCH) return scene_setup(c, scenes, scene_of, i);
+    else return 0;
 }
 
 constexpr unsigned kFlagNan = 1u, kFlagEscaped = 2u, kFlagTimeout = 4u, kFlagOverflow = 8u,

@@ -25,7 +25,7 @@ __device__ __forceinline__ float4 make_aux(float d, float p) {
     return make_float4(p / (d * d), 1.0f / d, d, p);
 }
 
-template <bool COMPAT, bool LIST>
+template <bool COMPAT, bool LIST, bool BATCH>
 __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl,
                                                     const float* __restrict__ bphi_s, float* __restrict__ dens,
                                                     float* __restrict__ pres, float4* __restrict__ aux,
@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
-    const long long base = scene_setup(c, scenes, scene_of, i);
+    const long long base = scene_setup_t<BATCH>(c, scenes, scene_of, i);
     fl.tab += base;
     bl.tab += base;
     const float4 pi = __ldg(&fl.npos[i]);
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
 /* compute_neigh_list (kernels/grid.cl:145-182, fluid and boundary) fused with
  * compute_density_pressure: the density sums run over exactly the pairs written to the
  * lists, in list order, so the step needs no separate density pass. */
-template <bool COMPAT>
+template <bool COMPAT, bool BATCH>
 __global__ void __launch_bounds__(256) k_lists_density(Const c0, const float4* __restrict__ spos,
                                                        const int2* __restrict__ tab,
                                                        const float4* __restrict__ bpos_s,
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) k_lists_density(Const c0, const float4* _
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
-    const long long base = scene_setup(c, scenes, scene_of, i);
+    const long long base = scene_setup_t<BATCH>(c, scenes, scene_of, i);
     tab += base;
     btab += base;
     const float4 pi = spos[i];
@@ -124,14 +124,14 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
     aux[i] = make_aux(dens[i], pres[i]);
 }
 
-template <bool LIST, bool EXACT>
+template <bool LIST, bool EXACT, bool BATCH>
 __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl, const float4* __restrict__ aux,
                                                  float4* __restrict__ normal, const SceneDev* __restrict__ scenes,
                                                  const int32_t* __restrict__ scene_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
-    fl.tab += scene_setup(c, scenes, scene_of, i);
+    fl.tab += scene_setup_t<BATCH>(c, scenes, scene_of, i);
     const float4 pi = __ldg(&fl.npos[i]);
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
@@ -180,12 +180,12 @@ __device__ __forceinline__ void wc_integrate_one(const Const& c, float4 p, float
     bad = !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(vx) && isfinite(vy) && isfinite(vz));
 }
 
-template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST>
+template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST, bool BATCH>
 __global__ void __launch_bounds__(256) k_wc_forces(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
-    const long long base = scene_setup(c, b.scenes, b.scene_of, i);
+    const long long base = scene_setup_t<BATCH>(c, b.scenes, b.scene_of, i);
     fl.tab += base;
     bl.tab += base;
     const float4 pi = __ldg(&b.pos_s[i]);
@@ -292,11 +292,20 @@ static Neigh<LIST, EXACT> bnd_src(const Bufs& b) {
     return Neigh<LIST, EXACT>{b.btab, b.sblist, b.sblen, b.bpos_s};
 }
 
+template <bool COMPAT, bool LIST, bool BATCH>
+static void density_launch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    k_wc_density<COMPAT, LIST, BATCH><<<nblk(c.n, bs), bs, 0, s>>>(c, fluid_src<LIST, COMPAT>(b),
+                                                                   bnd_src<LIST, COMPAT>(b), b.bphi_s, b.density,
+                                                                   b.pressure, b.aux, b.scenes, b.scene_of);
+}
+
+/* Batched contexts exist only in PHYSICS mode, so the scene lookup is compiled for that mode alone. */
 template <bool COMPAT, bool LIST>
 static void density_dispatch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
-    k_wc_density<COMPAT, LIST><<<nblk(c.n, bs), bs, 0, s>>>(c, fluid_src<LIST, COMPAT>(b), bnd_src<LIST, COMPAT>(b),
-                                                            b.bphi_s, b.density, b.pressure, b.aux, b.scenes,
-                                                            b.scene_of);
+    if constexpr (!COMPAT) {
+        if (c.batched) { density_launch<false, LIST, true>(s, c, b, bs); return; }
+    }
+    density_launch<COMPAT, LIST, false>(s, c, b, bs);
 }
 
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs) {
@@ -310,16 +319,18 @@ void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists
     }
 }
 
+template <bool COMPAT, bool BATCH>
+static void lists_density_launch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    k_lists_density<COMPAT, BATCH><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s,
+                                                                b.nlist, b.nlen, b.sblist, b.sblen, b.density,
+                                                                b.pressure, b.aux, b.scenes, b.scene_of);
+}
+
 void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     if (c.n <= 0) return;
-    if (c.compat)
-        k_lists_density<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist,
-                                                           b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux,
-                                                           b.scenes, b.scene_of);
-    else
-        k_lists_density<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist,
-                                                            b.nlen, b.sblist, b.sblen, b.density, b.pressure, b.aux,
-                                                            b.scenes, b.scene_of);
+    if (c.compat) lists_density_launch<true, false>(s, c, b, bs);
+    else if (c.batched) lists_density_launch<false, true>(s, c, b, bs);
+    else lists_density_launch<false, false>(s, c, b, bs);
 }
 
 void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
@@ -330,22 +341,32 @@ void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
 void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs) {
     if (c.n <= 0) return;
     const int g = nblk(c.n, bs);
-    if (lists)
-        k_normals<true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes, b.scene_of);
-    else if (c.compat)
-        k_normals<false, true><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.normal, b.scenes, b.scene_of);
-    else
-        k_normals<false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal, b.scenes,
-                                                 b.scene_of);
+    if (lists) {
+        if (c.batched)
+            k_normals<true, true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes,
+                                                         b.scene_of);
+        else
+            k_normals<true, true, false><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes,
+                                                          b.scene_of);
+    } else if (c.compat) {
+        k_normals<false, true, false><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.normal, b.scenes,
+                                                       b.scene_of);
+    } else if (c.batched) {
+        k_normals<false, false, true><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal, b.scenes,
+                                                       b.scene_of);
+    } else {
+        k_normals<false, false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal, b.scenes,
+                                                        b.scene_of);
+    }
 }
 
-template <bool COMPAT, bool LIST>
-static void forces_dispatch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs) {
+template <bool COMPAT, bool LIST, bool BATCH>
+static void forces_launch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs) {
     const int g = nblk(c.n, bs);
     const bool st = c.sigma != 0.f;
     auto fs = fluid_src<LIST, COMPAT>(b);
     auto bsrc = bnd_src<LIST, COMPAT>(b);
-#define SPH_WCF(F, W, S) k_wc_forces<COMPAT, LIST, F, W, S><<<g, bs, 0, s>>>(c, fs, bsrc, b)
+#define SPH_WCF(F, W, S) k_wc_forces<COMPAT, LIST, F, W, S, BATCH><<<g, bs, 0, s>>>(c, fs, bsrc, b)
     if (fuse) {
         if (write_acc) { if (st) SPH_WCF(true, true, true); else SPH_WCF(true, true, false); }
         else { if (st) SPH_WCF(true, false, true); else SPH_WCF(true, false, false); }
@@ -353,6 +374,14 @@ static void forces_dispatch(cudaStream_t s, const Const& c, const Bufs& b, bool 
         if (st) SPH_WCF(false, true, true); else SPH_WCF(false, true, false);
     }
 #undef SPH_WCF
+}
+
+template <bool COMPAT, bool LIST>
+static void forces_dispatch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs) {
+    if constexpr (!COMPAT) {
+        if (c.batched) { forces_launch<false, LIST, true>(s, c, b, fuse, write_acc, bs); return; }
+    }
+    forces_launch<COMPAT, LIST, false>(s, c, b, fuse, write_acc, bs);
 }
 
 void launch_wc_forces(cudaStream_t s, const Const& c, const Bufs& b, bool lists, bool fuse_integrate,
