@@ -215,14 +215,87 @@ __device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py
     return cnt;
 }
 
-/* Visits the materialised list of particle i (column-major list[k * n + i], grid.cl:174). */
+/* The scan of scan_neighbors<true> (same cells, order, cap and exact r^2), written for the
+ * list builder: every candidate runs the same instructions and f(hit, j, r2) applies the
+ * hit with predicated stores and selects instead of a branch, so the lanes of a warp that
+ * walk the same cell stay converged whichever of them hit. */
 template <class F>
+__device__ __forceinline__ int build_scan(const Const& c, float px, float py, float pz,
+                                          const int2* __restrict__ tab, const float4* __restrict__ npos, F&& f) {
+    const float qx = __fdiv_rn(__fsub_rn(px, c.ox), c.cell);
+    const float qy = __fdiv_rn(__fsub_rn(py, c.oy), c.cell);
+    const float qz = __fdiv_rn(__fsub_rn(pz, c.oz), c.cell);
+    int cx, cy, cz;
+    cell_of(c, px, py, pz, cx, cy, cz);
+    const bool cull = !c.wrap;
+    const float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
+    const bool inx = cull && floorf(qx) == (float)cx, iny = cull && floorf(qy) == (float)cy,
+               inz = cull && floorf(qz) == (float)cz;
+    const float h2 = c.h2_list;
+    int cnt = 0;
+#pragma unroll 1
+    for (int o = 0; o < 27 && cnt < c.cap; ++o) {
+        int ox, oy, oz;
+        neigh_offset(o, ox, oy, oz);
+        if (cull) {
+            const float g = (inx ? face_gap2(ox, fx) : 0.f) + (iny ? face_gap2(oy, fy) : 0.f) +
+                            (inz ? face_gap2(oz, fz) : 0.f);
+            if (g > c.cull2) continue;
+        }
+        long long id;
+        if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) continue;
+        const int2 r = __ldg(&tab[id]);
+        if (cnt + (r.y - r.x) <= c.cap) {
+#pragma unroll 4
+            for (int j = r.x; j < r.y; ++j) {
+                const float4 pj = __ldg(&npos[j]);
+                const float r2 = r2_exact(__fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
+                const bool hit = r2 < h2;
+                f(hit, j, r2);
+                cnt += hit ? 1 : 0;
+            }
+        } else {
+#pragma unroll 1
+            for (int j = r.x; j < r.y && cnt < c.cap; ++j) {
+                const float4 pj = __ldg(&npos[j]);
+                const float r2 = r2_exact(__fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
+                const bool hit = r2 < h2;
+                f(hit, j, r2);
+                cnt += hit ? 1 : 0;
+            }
+        }
+    }
+    return cnt;
+}
+
+/* Visits the materialised list of particle i (column-major list[k * n + i], grid.cl:174).
+ * The pass is bound by the latency of the dependent loads (list entry, then the
+ * neighbour's data), so U entries and their positions are loaded before the U visits
+ * run; the visits still run in list order, so every sum keeps the list's order. */
+#ifndef SPH_LIST_UNROLL
+#define SPH_LIST_UNROLL 4
+#endif
+template <int U = SPH_LIST_UNROLL, class F>
 __device__ __forceinline__ void list_neighbors(int i, int n, const int* __restrict__ list, int len,
                                                const float4* __restrict__ npos, float px, float py, float pz,
                                                F&& f) {
+    const size_t sn = (size_t)n;
+    const int* __restrict__ p = list + i;
+    int k = 0;
 #pragma unroll 1
-    for (int k = 0; k < len; ++k) {
-        const int j = __ldg(&list[(size_t)k * n + i]);
+    for (; k + U <= len; k += U, p += U * sn) {
+        int j[U];
+        float4 q[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) j[u] = __ldg(p + u * sn);
+#pragma unroll
+        for (int u = 0; u < U; ++u) q[u] = __ldg(&npos[j[u]]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) f(j[u], q[u], __fsub_rn(px, q[u].x), __fsub_rn(py, q[u].y), __fsub_rn(pz, q[u].z));
+    }
+#pragma unroll 1
+    for (; k < len; ++k, p += sn) {
+        const int j = __ldg(p);
         const float4 pj = __ldg(&npos[j]);
         f(j, pj, __fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
     }

@@ -65,8 +65,11 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
 /* compute_neigh_list (kernels/grid.cl:145-182, fluid and boundary) fused with
  * compute_density_pressure: the density sums run over exactly the pairs written to the
  * lists, in list order, so the step needs no separate density pass. */
+#ifndef SPH_LISTS_MIN_BLOCKS
+#define SPH_LISTS_MIN_BLOCKS 1
+#endif
 template <bool COMPAT, bool BATCH>
-__global__ void __launch_bounds__(256) k_lists_density(Const c0, const float4* __restrict__ spos,
+__global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Const c0, const float4* __restrict__ spos,
                                                        const int2* __restrict__ tab,
                                                        const float4* __restrict__ bpos_s,
                                                        const int2* __restrict__ btab,
@@ -85,13 +88,12 @@ __global__ void __launch_bounds__(256) k_lists_density(Const c0, const float4* _
     const float4 pi = spos[i];
     const size_t n = (size_t)c.n;
     const float hh = c.h * c.h;
-    int k = 0;
     float di = 0.f;
-    scan_neighbors<true>(c, pi.x, pi.y, pi.z, tab, spos, [&](int j, float4, float dx, float dy, float dz) {
-        nlist[(size_t)k * n + i] = j;
-        ++k;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        const float t = hh - (COMPAT ? sqrtf(r2) : r2);
+    int* out = nlist + i;
+    const int k = build_scan(c, pi.x, pi.y, pi.z, tab, spos, [&](bool hit, int j, float r2) {
+        if (hit) *out = j;
+        out += hit ? n : 0;
+        const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
         di += (t * t) * t;
     });
     nlen[i] = k;
@@ -99,12 +101,14 @@ __global__ void __launch_bounds__(256) k_lists_density(Const c0, const float4* _
     int kb = 0;
     float bdi = 0.f;
     if (c.nb > 0) {
-        scan_neighbors<true>(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float dx, float dy, float dz) {
-            sblist[(size_t)kb * n + i] = j;
-            ++kb;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const float t = hh - (COMPAT ? sqrtf(r2) : r2);
-            bdi += ((t * t) * t) * __ldg(&bphi_s[j]);
+        int* bout = sblist + i;
+        kb = build_scan(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](bool hit, int j, float r2) {
+            if (hit) *bout = j;
+            bout += hit ? n : 0;
+            const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
+            float w = 0.f;
+            if (hit) w = __ldg(&bphi_s[j]);
+            bdi += ((t * t) * t) * w;
         });
     }
     sblen[i] = kb;
@@ -136,8 +140,9 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
     fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
+        const float inv_rho = __ldg(&aux[j].y);
         const float t = HH - (dx * dx + dy * dy + dz * dz);
-        const float k = (t * t) * __ldg(&aux[j].y);
+        const float k = (t * t) * inv_rho;
         nx += dx * k;
         ny += dy * k;
         nz += dz * k;
@@ -180,8 +185,11 @@ __device__ __forceinline__ void wc_integrate_one(const Const& c, float4 p, float
     bad = !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(vx) && isfinite(vy) && isfinite(vz));
 }
 
+#ifndef SPH_FORCES_MIN_BLOCKS
+#define SPH_FORCES_MIN_BLOCKS 4
+#endif
 template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST, bool BATCH>
-__global__ void __launch_bounds__(256) k_wc_forces(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
+__global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
@@ -213,7 +221,11 @@ __global__ void __launch_bounds__(256) k_wc_forces(Const c0, Neigh<LIST, COMPAT>
     const float rmin2 = c.rmin2_wc, two_rho0 = 2.0f * c.rho0;
     fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
         const float r2 = dx * dx + dy * dy + dz * dz;
+        /* loaded ahead of the guard so that the list loop can issue them early */
         const float4 aj = __ldg(&b.aux[j]);
+        const float4 vj = __ldg(&b.vel_s[j]);
+        float4 nj = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ST) nj = __ldg(&b.normal[j]);
         if (di > 0.f && aj.z > 0.f && r2 > rmin2) {
             const float irn = rsqrtf(r2);
             const float rn = r2 * irn;
@@ -222,13 +234,11 @@ __global__ void __launch_bounds__(256) k_wc_forces(Const c0, Neigh<LIST, COMPAT>
             pax += dx * q;
             pay += dy * q;
             paz += dz * q;
-            const float4 vj = __ldg(&b.vel_s[j]);
             const float vw = w * aj.y;
             vax += (vj.x - vi.x) * vw;
             vay += (vj.y - vi.y) * vw;
             vaz += (vj.z - vi.z) * vw;
             if (ST) {
-                const float4 nj = __ldg(&b.normal[j]);
                 const float K = __fdividef(two_rho0, di + aj.z);
                 cux += (ni.x - nj.x) * K;
                 cuy += (ni.y - nj.y) * K;
