@@ -19,7 +19,7 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libsph_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["sph_sort.cu", "sph_grid.cu", "sph_wcsph.cu", "sph_pcisph.cu", "sph_boundary.cu", "sph_context.cu",
-           "sph_scene.cpp", "sph_sort_noalloc.cu"]
+           "sph_scene.cpp", "sph_sort_noalloc.cu", "sph_adjoint.cu"]
 _lock = threading.Lock()
 
 

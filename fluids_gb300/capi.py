@@ -19,7 +19,7 @@ _lib = None
 SPH_WCSPH, SPH_PCISPH = 0, 1
 SPH_MODE_COMPAT, SPH_MODE_PHYSICS = 0, 1
 SPH_NEIGH_SCAN, SPH_NEIGH_LIST = 0, 1
-FLAGS = dict(NAN=1, ESCAPED=2, TIMEOUT=4, OVERFLOW=8, NONCONVERGED=16)
+FLAGS = dict(NAN=1, ESCAPED=2, TIMEOUT=4, OVERFLOW=8, NONCONVERGED=16, NONSMOOTH=32)
 STATUS = {0: "SPH_OK", 1: "SPH_E_INVALID", 2: "SPH_E_CUDA", 3: "SPH_E_NONCONVERGED", 4: "SPH_E_ESCAPED",
           5: "SPH_E_NAN", 6: "SPH_E_TIMEOUT", 7: "SPH_E_OVERFLOW", 8: "SPH_E_STATE", 9: "SPH_E_NOMEM"}
 STAGES = dict(BOUNDARY_SYNC=0, HASHES=1, SORT=2, SHUFFLE=3, CELL_INTERVALS=4, NEIGH_LIST=5, SB_NEIGH_LIST=6,
@@ -40,7 +40,9 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_set_field", "sph_field_device_ptr", "sph_body_forces", "sph_stats", "sph_sort_pairs",
            "sph_scene_box_volume", "sph_scene_fishtank", "sph_scene_cube", "sph_jitter", "sph_cuda_available",
            "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc", "sph_batch_create",
-           "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid"]
+           "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid",
+           "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
+           "sph_adj_flags", "sph_adj_tape_bytes"]
 
 
 class SphParams(C.Structure):
@@ -133,6 +135,14 @@ def lib():
             "sph_batch_scene_range": (ip, [vp, ip, C.POINTER(ip), C.POINTER(ip)]),
             "sph_batch_stats": (ip, [vp, C.POINTER(C.c_double), ip]),
             "sph_batch_scene_grid": (ip, [vp, ip, C.POINTER(C.c_float), C.POINTER(ip), C.POINTER(C.c_longlong)]),
+            "sph_adj_create": (ip, [vp, ip, ip, C.POINTER(vp)]),
+            "sph_adj_destroy": (ip, [vp]),
+            "sph_adj_last_error": (cp, [vp]),
+            "sph_adj_forward": (ip, [vp, vp, vp, C.c_float, C.c_float, vp, vp]),
+            "sph_adj_backward": (ip, [vp, vp, vp, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]),
+            "sph_adj_flags": (ip, [vp, C.POINTER(C.c_uint)]),
+            "sph_adj_tape_bytes": (ip, [vp, C.POINTER(C.c_size_t)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -209,9 +219,20 @@ class Context:
         self.params = params
 
     def close(self):
+        for ref in getattr(self, "_dependents", ()):
+            dep = ref()
+            if dep is not None:
+                dep.close()
         if getattr(self, "h", None):
             self._lib.sph_destroy(self.h)
             self.h = None
+
+    def _attach(self, dep):
+        """Handles that use this context (an Adjoint) are closed before it."""
+        import weakref
+        if not hasattr(self, "_dependents"):
+            self._dependents = []
+        self._dependents.append(weakref.ref(dep))
 
     def __del__(self):
         try:
@@ -359,6 +380,83 @@ class BatchContext(Context):
         out = (C.c_double * (8 * self.nscenes))()
         self._c(self._lib.sph_batch_stats(self.h, out, self.nscenes))
         return np.array(out[:], dtype=np.float64).reshape(self.nscenes, 8)
+
+
+class Adjoint:
+    """Differentiable WCSPH over a context (sph_adj_*): ``forward`` runs ``steps`` steps
+    from (x0, v0) with viscosity ``mu`` and Tait stiffness ``k``; ``backward`` takes dL/dx_T
+    (and optionally dL/dv_T) and returns the gradients.  Arrays are (n, 4) float32 in
+    particle-id order: numpy arrays (host) or integer device addresses."""
+
+    def __init__(self, ctx, steps, checkpoint_every=20):
+        self._lib = lib()
+        self.ctx = ctx
+        self.n = ctx.particle_count()
+        self.steps = int(steps)
+        h = C.c_void_p()
+        check(self._lib.sph_adj_create(ctx.h, int(steps), int(checkpoint_every), C.byref(h)), ctx.h)
+        self.h = h
+        ctx._attach(self)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.sph_adj_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, rc):
+        if rc != 0:
+            msg = self._lib.sph_adj_last_error(self.h)
+            raise SphError(rc, msg.decode() if msg else "")
+        return rc
+
+    @staticmethod
+    def _addr(a):
+        if a is None:
+            return None
+        if isinstance(a, int):
+            return C.c_void_p(a)
+        return C.c_void_p(ptr(a))
+
+    def forward(self, x0, v0, mu, k, out_x=None, out_v=None):
+        """Returns (xT, vT) as numpy arrays unless device outputs are given."""
+        host_out = out_x is None
+        if host_out:
+            x0, v0 = f4(x0), f4(v0)
+            out_x = np.zeros((self.n, 4), np.float32)
+            out_v = np.zeros((self.n, 4), np.float32)
+        self._c(self._lib.sph_adj_forward(self.h, self._addr(x0), self._addr(v0), float(mu), float(k),
+                                          self._addr(out_x), self._addr(out_v)))
+        return (out_x, out_v) if host_out else None
+
+    def backward(self, gxT, gvT=None, out_gx0=None, out_gv0=None):
+        """Returns dict(g_x0, g_v0, g_mu, g_k, g_c0); arrays are numpy unless device
+        outputs are given."""
+        host_out = out_gx0 is None and not isinstance(gxT, int)
+        if host_out:
+            gxT = f4(gxT)
+            gvT = f4(gvT) if gvT is not None else None
+            out_gx0 = np.zeros((self.n, 4), np.float32)
+            out_gv0 = np.zeros((self.n, 4), np.float32)
+        gm, gk, gc = C.c_double(), C.c_double(), C.c_double()
+        self._c(self._lib.sph_adj_backward(self.h, self._addr(gxT), self._addr(gvT), self._addr(out_gx0),
+                                           self._addr(out_gv0), C.byref(gm), C.byref(gk), C.byref(gc)))
+        return dict(g_x0=out_gx0, g_v0=out_gv0, g_mu=gm.value, g_k=gk.value, g_c0=gc.value)
+
+    def flags(self):
+        f = C.c_uint()
+        self._c(self._lib.sph_adj_flags(self.h, C.byref(f)))
+        return f.value
+
+    def tape_bytes(self):
+        b = C.c_size_t()
+        self._c(self._lib.sph_adj_tape_bytes(self.h, C.byref(b)))
+        return b.value
 
 
 def sort_pairs_device(d_keys, d_vals, n, key_bits=32, stream=None):

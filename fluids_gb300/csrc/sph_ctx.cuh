@@ -1,0 +1,63 @@
+/*
+ * sph_ctx.cuh -- the solver context (struct sph_ctx of include/sph_capi.h), shared by the
+ * translation units that implement the C ABI (sph_context.cu, sph_adjoint.cu).
+ */
+#pragma once
+#include <string>
+#include <vector>
+
+#include "sph_capi.h"
+#include "sph_kernels.cuh"
+
+using sph::Bufs;
+using sph::Const;
+
+struct SphBody {
+    int origin = 0, count = 0, can_move = 0;
+    float mass = 0.f;
+    float xf[20];   /* rot3x4 (row-major), lin4, ang4 */
+};
+
+struct sph_ctx {
+    sph_params p{};
+    Const c{};
+    Bufs b{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0, num_sms = 1;
+    std::string err;
+    float lim[3] = {0.f, 0.f, 0.f};
+    /* host copies of what was added (FluidSimulation::add_volume / add_boundary) */
+    std::vector<float> vol_pos, vol_vel;
+    std::vector<float> braw_host;
+    std::vector<SphBody> bodies;
+    int N = 0, NB = 0;
+    bool any_movable = false, any_massive = false;
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    int max_iter_slots = 1;
+    int coop_blocks = 0;
+    int bs = 256;
+    bool graph_ok = true;
+    cudaGraphExec_t gexec = nullptr;
+    uint32_t* cur_keys = nullptr;
+    int32_t* cur_mask = nullptr;
+    bool has_state = false;
+    std::vector<cudaEvent_t>* prof = nullptr;   /* set only by sph_profile_step */
+    std::vector<const char*> prof_names;
+    std::string prof_list;
+    /* batched contexts: one entry per scene (container, viscosity, stiffness, ranges) */
+    struct SceneIn {
+        float lim[3];
+        float mu, kgas;
+        int first, count, first_b, count_b;
+    };
+    std::vector<SceneIn> scene_in;
+    std::vector<sph::SceneDev> h_scenes;
+    sph::SceneDev* d_scenes = nullptr;
+    int32_t* d_scene_of = nullptr;
+    double* d_scene_stats = nullptr;
+};
+
+/* Records msg as the context's last error (or the last creation error) and returns code. */
+int sph_ctx_fail(sph_ctx* x, int code, const std::string& msg);

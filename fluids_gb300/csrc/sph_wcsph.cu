@@ -68,7 +68,10 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
 #ifndef SPH_LISTS_MIN_BLOCKS
 #define SPH_LISTS_MIN_BLOCKS 1
 #endif
-template <bool COMPAT, bool BATCH>
+/* REMAP (the adjoint's tape, which keeps particles in id order): the list of sorted particle
+ * i is written as row remap[i] with entries remap[j], and its density, pressure and aux go to
+ * remap[i]; the visits, their order and the arithmetic are those of the plain builder. */
+template <bool COMPAT, bool BATCH, bool REMAP = false>
 __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Const c0, const float4* __restrict__ spos,
                                                        const int2* __restrict__ tab,
                                                        const float4* __restrict__ bpos_s,
@@ -78,7 +81,9 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
                                                        int* __restrict__ sblen, float* __restrict__ dens,
                                                        float* __restrict__ pres, float4* __restrict__ aux,
                                                        const SceneDev* __restrict__ scenes,
-                                                       const int32_t* __restrict__ scene_of) {
+                                                       const int32_t* __restrict__ scene_of,
+                                                       const int32_t* __restrict__ remap = nullptr,
+                                                       unsigned* __restrict__ flags = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
@@ -88,19 +93,21 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     const float4 pi = spos[i];
     const size_t n = (size_t)c.n;
     const float hh = c.h * c.h;
+    const int row = REMAP ? __ldg(&remap[i]) : i;
     float di = 0.f;
-    int* out = nlist + i;
+    int* out = nlist + row;
     const int k = build_scan(c, pi.x, pi.y, pi.z, tab, spos, [&](bool hit, int j, float r2) {
-        if (hit) *out = j;
+        if (hit) *out = REMAP ? __ldg(&remap[j]) : j;
         out += hit ? n : 0;
         const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
         di += (t * t) * t;
     });
-    nlen[i] = k;
+    nlen[row] = k;
+    if (k >= c.cap && REMAP) atomicOr(flags, kFlagOverflow);
     di *= c.poly6_eval * c.mass;
     int kb = 0;
     float bdi = 0.f;
-    if (c.nb > 0) {
+    if (c.nb > 0 && !REMAP) {
         int* bout = sblist + i;
         kb = build_scan(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](bool hit, int j, float r2) {
             if (hit) *bout = j;
@@ -111,13 +118,13 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
             bdi += ((t * t) * t) * w;
         });
     }
-    sblen[i] = kb;
+    if (!REMAP) sblen[i] = kb;
     di += c.poly6_eval * bdi;
-    dens[i] = di;
+    dens[row] = di;
     const float pv = c.kgas * (pown7(di / c.rho0) - 1.0f);
     const float p = (0.f < pv) ? pv : 0.f;
-    pres[i] = p;
-    aux[i] = make_aux(di, p);
+    pres[row] = p;
+    aux[row] = make_aux(di, p);
 }
 
 /* aux from the density / pressure fields (used when those fields were set from outside). */
@@ -334,6 +341,13 @@ static void lists_density_launch(cudaStream_t s, const Const& c, const Bufs& b, 
     k_lists_density<COMPAT, BATCH><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s,
                                                                 b.nlist, b.nlen, b.sblist, b.sblen, b.density,
                                                                 b.pressure, b.aux, b.scenes, b.scene_of);
+}
+
+void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, const int32_t* remap, int bs) {
+    if (c.n <= 0) return;
+    k_lists_density<false, false, true><<<nblk(c.n, bs), bs, 0, s>>>(
+        c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist, b.nlen, b.sblist, b.sblen, b.density, b.pressure,
+        b.aux, b.scenes, b.scene_of, remap, b.flags);
 }
 
 void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs) {

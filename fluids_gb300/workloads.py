@@ -133,3 +133,44 @@ def build_context(w, params=None):
         ctx.add_boundary(pts, can_move=mv, rot3x4=rot, mass=mass)
     ctx.add_volume(w["fluid"], w.get("velocities"))
     return ctx
+
+
+def fourier_velocity(pos, nmodes=8, amp=0.5, seed=0, length=0.48):
+    """Divergence-free random Fourier field v(x) = sum_k a_k sin(k.x + phi_k) with every a_k
+    perpendicular to k (so div v = 0), |k| uniform in [2 pi / length, 8 pi / length], scaled
+    so that the largest particle speed is amp."""
+    rng = np.random.default_rng(seed)
+    x = np.asarray(pos, dtype=np.float64)[:, :3]
+    v = np.zeros_like(x)
+    for _ in range(nmodes):
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        k = d * rng.uniform(2 * np.pi / length, 8 * np.pi / length)
+        a = rng.normal(size=3)
+        a -= d * np.dot(a, d)
+        phi = rng.uniform(0, 2 * np.pi)
+        v += np.sin(x @ k + phi)[:, None] * a[None, :]
+    v *= amp / np.max(np.linalg.norm(v, axis=1))
+    out = np.zeros((len(x), 4), np.float32)
+    out[:, :3] = v
+    return out
+
+
+def adjoint_block(n_side=32, dx=0.015, seed=0, steps=200, checkpoint_every=20, mu=0.01, c0=20.0):
+    """Differentiable WCSPH workload: an n_side^3 lattice block at dx (jitter 1e-4) centred in a
+    2x2x2 m container (no boundary particles, no wall contact within the run), a divergence-
+    free Fourier initial velocity with 8 modes and amplitude 0.5 m/s, and a seeded target
+    cloud (each particle's start plus a 1 cm Gaussian offset and a 1 cm shift in x) for the
+    loss mean_i |x_i(T) - y_i|^2.  Surface tension is 0."""
+    container = (2.0, 2.0, 2.0)
+    lo = -(n_side - 1) * dx / 2
+    fluid = jitter(lattice_block(n_side, n_side, n_side, dx, (lo, lo, lo)), 1e-4, seed)
+    vel = fourier_velocity(fluid, 8, 0.5, seed + 1, length=n_side * dx)
+    rng = np.random.default_rng(seed + 2)
+    target = fluid.copy()
+    target[:, :3] += rng.normal(scale=0.01, size=(len(fluid), 3)).astype(np.float32)
+    target[:, 0] += 0.01
+    p = wcsph_params(dx, 2e-4, capi.SPH_MODE_PHYSICS, c0=c0, mu=mu, sigma=0.0)
+    return dict(name="wcsph_adjoint_%d" % len(fluid), params=p, fluid=fluid, velocities=vel, target=target,
+                bodies=[], container=container, steps=steps, checkpoint_every=checkpoint_every, dx=dx, mu=mu,
+                c0=c0, kgas=tait_stiffness(c0))

@@ -44,7 +44,8 @@ enum sph_flag {
     SPH_FLAG_ESCAPED = 2u,
     SPH_FLAG_TIMEOUT = 4u,
     SPH_FLAG_OVERFLOW = 8u,
-    SPH_FLAG_NONCONVERGED = 16u
+    SPH_FLAG_NONCONVERGED = 16u,
+    SPH_FLAG_NONSMOOTH = 32u   /* adjoint: a velocity clamp or wall reflection was active */
 };
 
 enum sph_method { SPH_WCSPH = 0, SPH_PCISPH = 1 };
@@ -236,6 +237,38 @@ int sph_batch_scene_range(const sph_ctx* ctx, int scene, int* first, int* count)
 int sph_batch_scene_grid(const sph_ctx* ctx, int scene, float* origin3, int* dims3, long long* cell_base);
 /* sph_stats for every scene: out8[8 * scene + k]; synchronises. */
 int sph_batch_stats(sph_ctx* ctx, double* out8, int nscenes);
+
+/* ---- differentiable WCSPH (adjoint) ----------------------------------------------------
+ * No counterpart in the reference, which has no gradients.  The forward step is the WCSPH
+ * step of WCSPHSimulation::simulate (wcsphsimluation.cpp:40-106) in PHYSICS mode; the
+ * backward pass runs hand-written adjoint kernels over the same neighbour lists (held fixed
+ * per step), recomputing each segment of checkpoint_every steps from its checkpoint.
+ * Requirements: a single-scene WCSPH context in PHYSICS mode with fluid particles, no
+ * boundary particles and surface_tension = 0 (SPH_E_INVALID otherwise).  The context's
+ * grid, container and constants are used; its own particle state is not touched.
+ * Particle arrays are float4 (x, y, z, unused) in particle-id order (the order of
+ * sph_add_volume), host or device pointers. */
+typedef struct sph_adj sph_adj;
+int sph_adj_create(sph_ctx* ctx, int steps, int checkpoint_every, sph_adj** out);
+/* Frees the handle; valid even after its context was destroyed (no other call is). */
+int sph_adj_destroy(sph_adj* adj);
+const char* sph_adj_last_error(const sph_adj* adj);
+/* Runs `steps` steps from positions x0 and velocities v0 (the half-step velocity starts at
+ * v0, as sph_add_volume does) with viscosity mu and Tait stiffness gas_stiffness, keeping a
+ * checkpoint every checkpoint_every steps.  Writes the final positions / velocities to
+ * xT_4 / vT_4 when they are not NULL.  Synchronises. */
+int sph_adj_forward(sph_adj* adj, const float* x0_4, const float* v0_4, float mu, float gas_stiffness,
+                    float* xT_4, float* vT_4);
+/* Given dL/dx_T (and dL/dv_T, or NULL for zero) of the last forward pass, writes dL/dx0,
+ * dL/dv0 (either may be NULL), dL/dmu, dL/dk and dL/dc0 (k = rho0 c0^2 / 7).
+ * Deterministic: no atomics in any sum.  Synchronises. */
+int sph_adj_backward(sph_adj* adj, const float* gxT_4, const float* gvT_4, float* gx0_4, float* gv0_4,
+                     double* g_mu, double* g_stiffness, double* g_c0);
+/* SPH_FLAG_* raised since the last forward: OVERFLOW (a list reached the cap, so the lists
+ * may not be symmetric), NONSMOOTH (a clamp or reflection was crossed), NAN, ESCAPED. */
+int sph_adj_flags(sph_adj* adj, unsigned* flags);
+/* Device bytes the adjoint holds (checkpoints, one segment's tape, scratch). */
+int sph_adj_tape_bytes(const sph_adj* adj, size_t* bytes);
 
 /* ---- primitives ---------------------------------------------------------------------- */
 
