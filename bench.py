@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--neighbor-mode", type=int, default=1, help="0 = cell scan in every pass, 1 = lists")
     ap.add_argument("--batched-steps", type=int, default=500, help="0 skips the batched comparison")
+    ap.add_argument("--adjoint-steps", type=int, default=200, help="0 skips the adjoint comparison")
+    ap.add_argument("--pcisph-steps", type=int, default=100, help="0 skips the PCISPH line")
     return ap.parse_args()
 
 
@@ -228,6 +230,108 @@ def bench_batched(steps, warmup, torch, nscenes=256):
             "mean_abs_density_error_looped": float(sl[:, 1].mean()), "device_flags": flags_b}
 
 
+def bench_adjoint(torch, steps=200, every=20):
+    """Differentiable WCSPH, 32^3 particles (Fourier initial velocity, 200 steps, checkpoint
+    every 20): adjoint forward + backward against the plain solver's forward on the same
+    scene and GPU, plus central differences of the GPU forward (FP32) for the gradients."""
+    from fluids_gb300 import capi, workloads
+    w = workloads.adjoint_block(32, steps=steps, checkpoint_every=every)
+    stream = torch.cuda.Stream()
+    ctx = workloads.build_context(w)
+    ctx.set_stream(stream.cuda_stream)
+    n = ctx.particle_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
+
+    ctx.simulate(3)
+    t_plain = timed(lambda: ctx.simulate(steps))
+    adj = capi.Adjoint(ctx, steps, every)
+    dev = torch.device("cuda")
+    x0 = torch.tensor(w["fluid"], device=dev)
+    v0 = torch.tensor(w["velocities"], device=dev)
+    y = torch.tensor(w["target"], device=dev)
+    xT, vT, gx = torch.empty_like(x0), torch.empty_like(x0), torch.zeros_like(x0)
+    gx0, gv0 = torch.empty_like(x0), torch.empty_like(x0)
+    mu, k = w["mu"], w["kgas"]
+
+    def fwd(v=v0, m=mu, kk=k):
+        adj.forward(x0.data_ptr(), v.data_ptr(), m, kk, out_x=xT.data_ptr(), out_v=vT.data_ptr())
+
+    res = {}
+
+    def bwd():
+        res.update(adj.backward(gx.data_ptr(), None, out_gx0=gx0.data_ptr(), out_gv0=gv0.data_ptr()))
+
+    fwd()
+    gx[:, :3] = 2.0 * (xT[:, :3] - y[:, :3]) / n
+    bwd()
+    t_fwd = min(timed(fwd) for _ in range(3))
+    t_bwd = min(timed(bwd) for _ in range(3))
+
+    def loss(**kw):
+        fwd(**kw)
+        torch.cuda.synchronize()
+        return float(((xT[:, :3].double() - y[:, :3].double()) ** 2).sum(dim=1).mean())
+
+    fd = {}
+    e = 0.1 * mu
+    fd["mu"] = dict(eps_rel=0.1, fd=(loss(m=mu + e) - loss(m=mu - e)) / (2 * e), adjoint=res["g_mu"])
+    c0, e = w["c0"], 0.01 * w["c0"]
+    fd["c0"] = dict(eps_rel=0.01, fd=(loss(kk=workloads.tait_stiffness(c0 + e)) -
+                                      loss(kk=workloads.tait_stiffness(c0 - e))) / (2 * e), adjoint=res["g_c0"])
+    dd = torch.tensor(workloads.fourier_velocity(w["fluid"], 8, 1.0, seed=99), device=dev)
+    e = 1e-2
+    fd["v0_smooth_direction"] = dict(eps=e, fd=(loss(v=v0 + e * dd) - loss(v=v0 - e * dd)) / (2 * e),
+                                     adjoint=float((gv0[:, :3].double() * dd[:, :3].double()).sum()))
+    for d in fd.values():
+        d["rel_err"] = abs(d["adjoint"] - d["fd"]) / abs(d["fd"])
+    out = {"particles": n, "steps": steps, "checkpoint_every": every,
+           "plain_updates_per_s": n * steps / t_plain, "plain_ms": 1000 * t_plain,
+           "adjoint_forward_ms": 1000 * t_fwd, "adjoint_backward_ms": 1000 * t_bwd,
+           "adjoint_updates_per_s": n * steps / (t_fwd + t_bwd),
+           "adjoint_over_plain_time": (t_fwd + t_bwd) / t_plain,
+           "gradients": {"d_mu": res["g_mu"], "d_c0": res["g_c0"], "d_k": res["g_k"]},
+           "fd_check_fp32": fd, "flags": adj.flags(), "tape_bytes": adj.tape_bytes()}
+    adj.close()
+    ctx.close()
+    return out
+
+
+def bench_pcisph(torch, steps, warmup):
+    """PCISPH double block + rotated cube (358,400 fluid particles), PHYSICS mode: device time
+    of `steps` graph-replayed steps (the predict-correct loop is one persistent kernel)."""
+    from fluids_gb300 import capi, workloads
+    w = workloads.pcisph_cube(capi.SPH_MODE_PHYSICS)
+    stream = torch.cuda.Stream()
+    ctx = workloads.build_context(w)
+    ctx.set_stream(stream.cuda_stream)
+    n, nb = ctx.particle_count(), ctx.boundary_particle_count()
+    ctx.simulate(warmup)
+    iters = []
+    for _ in range(5):
+        ctx.simulate(1)
+        iters.append(int(ctx.get("PCI_ITERS")[0]))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.simulate(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1000.0
+    out = {"workload": w["name"], "particles": n, "boundary_particles": nb, "steps": steps,
+           "updates_per_s": n * steps / t, "ms_per_step": 1000 * t / steps,
+           "pci_iterations_sampled": iters, "device_flags": ctx.device_flags()}
+    ctx.close()
+    return out
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -359,6 +463,11 @@ def main():
     batched = None
     if args.batched_steps > 0 and args.workload == "wcsph4m":
         batched = bench_batched(args.batched_steps, max(args.warmup, 3), torch)
+    adjoint = pcisph = None
+    if args.adjoint_steps > 0 and args.workload == "wcsph4m":
+        adjoint = bench_adjoint(torch, args.adjoint_steps)
+    if args.pcisph_steps > 0 and args.workload == "wcsph4m":
+        pcisph = bench_pcisph(torch, args.pcisph_steps, max(args.warmup, 3))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         z = w["fluid"][:, 2]
@@ -374,7 +483,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + jitter)",
                 "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk,
-                "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched}
+                "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched, "adjoint": adjoint,
+                "pcisph": pcisph}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
