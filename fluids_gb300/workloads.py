@@ -63,12 +63,15 @@ def double_dam_4m(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=200, n=128, **kw):
 
 
 def pcisph_cube(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=500, dx=0.0125, **kw):
-    """Two 0.5x1.0x0.7 m BoxVolumes at (+-0.74, dx, -0.1) (raised one spacing so the bottom
-    layer does not sit on the floor's boundary particles) and a static 0.3 m cube at
-    (0, -0.35, 0) rotated 0.5 rad about y."""
+    """Two 0.5x1.0x0.7 m BoxVolumes centred at x = +-(0.75 - dx), y = dx, z = -0.1 and a static
+    0.3 m cube at (0, -0.35, 0) rotated 0.5 rad about y.  BoxVolume puts its first layer on the
+    box's lower face, so centres at (+-0.74, 0, -0.1) would put that layer on the floor's
+    boundary particles and 0.8 dx from the -x wall's; the blocks are raised one spacing and
+    moved in to one spacing from the side walls."""
     container = (2.0, 1.0, 1.0)
     r = dx / 2.0
-    vols = [BoxVolume((0.5, 1.0, 0.7), (0.74, dx, -0.1)), BoxVolume((0.5, 1.0, 0.7), (-0.74, dx, -0.1))]
+    cx = 0.75 - dx
+    vols = [BoxVolume((0.5, 1.0, 0.7), (cx, dx, -0.1)), BoxVolume((0.5, 1.0, 0.7), (-cx, dx, -0.1))]
     fluid = jitter(np.concatenate([v.particles(r) for v in vols]), 1e-4, seed)
     cube = Cube(0.3, 0.0, (0.0, -0.35, 0.0), rotation_y(0.5))
     p = capi.make_params(capi.SPH_PCISPH, mode=mode, time_step=5e-4, max_vel=20.0, particle_radius=r,
