@@ -258,6 +258,31 @@ void launch_bnd_phi(cudaStream_t s, const Const& c, const Bufs& b, float phi_coe
     k_bnd_phi<<<nblk(c.nb, bs), bs, 0, s>>>(c, c.nb, b.bpos_s, b.bbody_s, b.btab, b.bmask_sorted, phi_coeff,
                                             b.bphi_s, b.bphi, b.scenes, b.scene_of ? b.bbody_s : nullptr);
 }
+/* bnear[cell] = 1 for the 27 cells around each sorted boundary particle's cell (the cells
+ * whose particles can have a boundary neighbour); concurrent stores all write 1. */
+__global__ void k_bnd_near(Const c0, int nb, const float4* __restrict__ bpos_s, uint8_t* __restrict__ near,
+                           const SceneDev* __restrict__ scenes, const int32_t* __restrict__ scene_of) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    Const c = c0;
+    const long long base = scene_setup(c, scenes, scene_of, i);
+    const float4 p = bpos_s[i];
+    int cx, cy, cz;
+    cell_of(c, p.x, p.y, p.z, cx, cy, cz);
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                long long id;
+                if (neigh_cell(c, cx + dx, cy + dy, cz + dz, id)) near[base + id] = 1;
+            }
+}
+
+void launch_bnd_near(cudaStream_t s, const Const& c, const Bufs& b, int nb, int bs) {
+    cudaMemsetAsync(b.bnear, 0, (size_t)c.ncells, s);
+    if (nb <= 0) return;
+    k_bnd_near<<<nblk(nb, bs), bs, 0, s>>>(c, nb, b.bpos_s, b.bnear, b.scenes, b.scene_of ? b.bbody_s : nullptr);
+}
+
 void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs) {
     if (c.nb <= 0 || nbodies <= 0) return;
     cudaMemsetAsync(b.body_force, 0, sizeof(float4) * nbodies, s);

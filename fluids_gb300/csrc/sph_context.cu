@@ -253,6 +253,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.bmask = cv.take<int32_t>(nb); b.bmask_alt = cv.take<int32_t>(nb);
     b.btab = cv.take<int2>((size_t)x->c.ncells);
     b.bcell_prev = cv.take<int32_t>(nb);
+    b.bnear = cv.take<uint8_t>((size_t)x->c.ncells);
     b.bsort_ws = cv.take<char>(sph::sort_workspace_bytes((int)nb, x->c.key_bits));
     b.body_xf = cv.take<float>(20 * nbod);
     b.body_range = cv.take<int32_t>(4 * nbod);
@@ -294,6 +295,7 @@ void boundary_sort(sph_ctx* x) {
                                 x->bs);
     sph::launch_cell_ranges(s, cb, b.bpos_s, b.bkeys_sorted, x->NB, b.btab, b.bcell_prev, b.flags, x->bs, b.scenes,
                             b.scene_of ? b.bbody_s : nullptr);
+    sph::launch_bnd_near(s, cb, b, x->NB, x->bs);
 }
 
 bool uses_lists(const sph_ctx* x) { return x->p.method == SPH_PCISPH || x->p.neighbor_mode == SPH_NEIGH_LIST; }

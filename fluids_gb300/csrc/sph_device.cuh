@@ -218,30 +218,19 @@ __device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py
 /* The scan of scan_neighbors<true> (same cells, order, cap and exact r^2), written for the
  * list builder: every candidate runs the same instructions and f(hit, j, r2) applies the
  * hit with predicated stores and selects instead of a branch, so the lanes of a warp that
- * walk the same cell stay converged whichever of them hit. */
+ * walk the same cell stay converged whichever of them hit.  The particle's cell (cx, cy, cz)
+ * comes from the caller.  No cell is skipped by distance: in a warp the lanes that share a
+ * cell would skip different cells, so the warp walks their union anyway, and measured on
+ * GB300 the skipping test cost more than it saved. */
 template <class F>
-__device__ __forceinline__ int build_scan(const Const& c, float px, float py, float pz,
+__device__ __forceinline__ int build_scan(const Const& c, float px, float py, float pz, int cx, int cy, int cz,
                                           const int2* __restrict__ tab, const float4* __restrict__ npos, F&& f) {
-    const float qx = __fdiv_rn(__fsub_rn(px, c.ox), c.cell);
-    const float qy = __fdiv_rn(__fsub_rn(py, c.oy), c.cell);
-    const float qz = __fdiv_rn(__fsub_rn(pz, c.oz), c.cell);
-    int cx, cy, cz;
-    cell_of(c, px, py, pz, cx, cy, cz);
-    const bool cull = !c.wrap;
-    const float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
-    const bool inx = cull && floorf(qx) == (float)cx, iny = cull && floorf(qy) == (float)cy,
-               inz = cull && floorf(qz) == (float)cz;
     const float h2 = c.h2_list;
     int cnt = 0;
 #pragma unroll 1
     for (int o = 0; o < 27 && cnt < c.cap; ++o) {
         int ox, oy, oz;
         neigh_offset(o, ox, oy, oz);
-        if (cull) {
-            const float g = (inx ? face_gap2(ox, fx) : 0.f) + (iny ? face_gap2(oy, fy) : 0.f) +
-                            (inz ? face_gap2(oz, fz) : 0.f);
-            if (g > c.cull2) continue;
-        }
         long long id;
         if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) continue;
         const int2 r = __ldg(&tab[id]);

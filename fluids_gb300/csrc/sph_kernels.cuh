@@ -36,6 +36,7 @@ struct Bufs {
     int32_t* bmask_sorted;
     int2* btab;
     int32_t* bcell_prev;
+    uint8_t* bnear;                        /* per cell: 1 when a boundary particle is binned within one cell */
     void* bsort_ws;
     /* per-body data (device) */
     float* body_xf;                        /* 20 floats per body: rot3x4, lin4, ang4 */
@@ -98,6 +99,8 @@ void launch_pci_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs)
 void launch_bnd_transform(cudaStream_t s, const Bufs& b, int nbodies, int nb, bool compat, bool only_movable,
                           int bs);
 void launch_bnd_phi(cudaStream_t s, const Const& c, const Bufs& b, float phi_coeff, int bs);
+/* marks bnear for the 27 cells around every sorted boundary particle (after clearing it) */
+void launch_bnd_near(cudaStream_t s, const Const& c, const Bufs& b, int nb, int bs);
 void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs);
 void launch_stats(cudaStream_t s, const Const& c, const Bufs& b);
 void launch_scene_stats(cudaStream_t s, const Const& c, const Bufs& b, double* out, int nscenes);

@@ -83,7 +83,8 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
                                                        const SceneDev* __restrict__ scenes,
                                                        const int32_t* __restrict__ scene_of,
                                                        const int32_t* __restrict__ remap = nullptr,
-                                                       unsigned* __restrict__ flags = nullptr) {
+                                                       unsigned* __restrict__ flags = nullptr,
+                                                       const uint8_t* __restrict__ bnear = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
@@ -94,9 +95,11 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     const size_t n = (size_t)c.n;
     const float hh = c.h * c.h;
     const int row = REMAP ? __ldg(&remap[i]) : i;
+    int cx, cy, cz;
+    cell_of(c, pi.x, pi.y, pi.z, cx, cy, cz);
     float di = 0.f;
     int* out = nlist + row;
-    const int k = build_scan(c, pi.x, pi.y, pi.z, tab, spos, [&](bool hit, int j, float r2) {
+    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, [&](bool hit, int j, float r2) {
         if (hit) *out = REMAP ? __ldg(&remap[j]) : j;
         out += hit ? n : 0;
         const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
@@ -107,9 +110,12 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     di *= c.poly6_eval * c.mass;
     int kb = 0;
     float bdi = 0.f;
-    if (c.nb > 0 && !REMAP) {
+    /* the boundary scan only where a boundary particle is binned in one of the 27 cells
+     * (bnear, PHYSICS grid); every other particle's boundary list is empty */
+    const bool scan_b = c.wrap || bnear == nullptr || bnear[base + cell_lin(c, cx, cy, cz)] != 0;
+    if (c.nb > 0 && !REMAP && scan_b) {
         int* bout = sblist + i;
-        kb = build_scan(c, pi.x, pi.y, pi.z, btab, bpos_s, [&](bool hit, int j, float r2) {
+        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, [&](bool hit, int j, float r2) {
             if (hit) *bout = j;
             bout += hit ? n : 0;
             const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
@@ -340,7 +346,8 @@ template <bool COMPAT, bool BATCH>
 static void lists_density_launch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     k_lists_density<COMPAT, BATCH><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s,
                                                                 b.nlist, b.nlen, b.sblist, b.sblen, b.density,
-                                                                b.pressure, b.aux, b.scenes, b.scene_of);
+                                                                b.pressure, b.aux, b.scenes, b.scene_of, nullptr,
+                                                                nullptr, b.bnear);
 }
 
 void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, const int32_t* remap, int bs) {
