@@ -14,10 +14,15 @@ def build(force=False, verbose=False):
     return _build_mod.build(force=force, verbose=verbose)
 
 
+def build_driver(force=False):
+    """Compiles the headless C++ driver (driver/sph_driver.cpp) against the library."""
+    return _build_mod.build_driver(force=force)
+
+
 def cuda_available():
     from . import capi
     return capi.cuda_available()
 
 
-__all__ = ["build", "cuda_available", "Context", "SphError", "SphParams", "default_params", "make_params",
+__all__ = ["build", "build_driver", "cuda_available", "Context", "SphError", "SphParams", "default_params", "make_params",
            "SPH_WCSPH", "SPH_PCISPH", "SPH_MODE_COMPAT", "SPH_MODE_PHYSICS", "SPH_NEIGH_SCAN", "SPH_NEIGH_LIST"]

@@ -77,6 +77,27 @@ def build(force=False, verbose=False, extra=None):
         return LIB
 
 
+DRIVER_SRC = os.path.join(PKG, "driver", "sph_driver.cpp")
+DRIVER = os.path.join(OUT_DIR, "sph_driver")
+
+
+def build_driver(force=False):
+    """The headless C++ driver (driver/sph_driver.cpp) over include/sph_fluid.hpp, linked
+    against the library with an rpath to its own directory."""
+    lib = build()
+    deps = [DRIVER_SRC, os.path.join(INCLUDE, "sph_fluid.hpp"), os.path.join(INCLUDE, "sph_capi.h"), lib]
+    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(d) for d in deps):
+        return DRIVER
+    tmp = DRIVER + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, DRIVER_SRC, "-o", tmp, "-L", OUT_DIR, "-lsph_gb300",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 def ptxas_report(src="sph_wcsph.cu"):
     """Registers / spills / shared memory per kernel (nvcc -Xptxas -v) for one source."""
     cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", os.devnull, "-std=c++17", "-O3", "-Xptxas", "-v",

@@ -1,0 +1,299 @@
+/*
+ * sph_driver.cpp -- headless driver: runs a reference scene file with a reference settings
+ * file on the GPU solver through the FluidSimulation mirror (include/sph_fluid.hpp).
+ *
+ * Replaces the reference's Scene + Fluid objects (scene/scene.cpp:322-476, scene/fluid.cpp)
+ * without rendering: the settings come from a key=value file (settings/settings.cpp:14-59),
+ * the scene from the reference's JSON format -- "container" {width, height, depth} becomes the
+ * rectangular limits, "fluid_volumes" of type "box" {size, center} become BoxVolumes, and
+ * "rigid_bodies" of type "cube" {size, center, rotation (x, y, z, w quaternion), mass} become
+ * boundary bodies (movable when mass > 0, as scene.cpp:471 passes them).  Sphere and mesh
+ * bodies are not sampled here (reported and skipped).  Options:
+ *
+ *   sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]
+ *              [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]
+ *
+ * Prints one JSON line per K steps with the solver statistics and a final line with the
+ * wall-clock throughput.  --dump writes the final positions ordered by particle id (float32
+ * x, y, z, w per particle).  --dry-run parses and samples the scene without touching a GPU.
+ */
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "sph_fluid.hpp"
+
+using namespace sph_gb300;
+
+namespace {
+
+/* ---- a minimal JSON reader (objects, arrays, numbers, strings, true/false/null) ---------- */
+struct Json {
+    enum Kind { NUL, NUM, STR, BOOL, ARR, OBJ } kind = NUL;
+    double num = 0.0;
+    bool b = false;
+    std::string str;
+    std::vector<Json> arr;
+    std::map<std::string, Json> obj;
+    const Json& operator[](const std::string& k) const {
+        static const Json none;
+        auto it = obj.find(k);
+        return it == obj.end() ? none : it->second;
+    }
+    const Json& operator[](size_t i) const {
+        static const Json none;
+        return i < arr.size() ? arr[i] : none;
+    }
+    double number(double def = 0.0) const { return kind == NUM ? num : def; }
+};
+
+struct Parser {
+    const char* p;
+    const char* end;
+    void ws() {
+        while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) ++p;
+    }
+    [[noreturn]] void fail(const char* what) { throw Error(SPH_E_INVALID, std::string("scene JSON: ") + what); }
+    Json value() {
+        ws();
+        if (p >= end) fail("unexpected end");
+        Json v;
+        if (*p == '{') {
+            v.kind = Json::OBJ;
+            ++p;
+            ws();
+            if (p < end && *p == '}') { ++p; return v; }
+            for (;;) {
+                ws();
+                Json k = value();
+                if (k.kind != Json::STR) fail("object key is not a string");
+                ws();
+                if (p >= end || *p != ':') fail("expected ':'");
+                ++p;
+                v.obj[k.str] = value();
+                ws();
+                if (p < end && *p == ',') { ++p; continue; }
+                if (p < end && *p == '}') { ++p; return v; }
+                fail("expected ',' or '}'");
+            }
+        }
+        if (*p == '[') {
+            v.kind = Json::ARR;
+            ++p;
+            ws();
+            if (p < end && *p == ']') { ++p; return v; }
+            for (;;) {
+                v.arr.push_back(value());
+                ws();
+                if (p < end && *p == ',') { ++p; continue; }
+                if (p < end && *p == ']') { ++p; return v; }
+                fail("expected ',' or ']'");
+            }
+        }
+        if (*p == '"') {
+            v.kind = Json::STR;
+            ++p;
+            while (p < end && *p != '"') {
+                if (*p == '\\' && p + 1 < end) ++p;
+                v.str.push_back(*p++);
+            }
+            if (p >= end) fail("unterminated string");
+            ++p;
+            return v;
+        }
+        if (!strncmp(p, "true", 4)) { v.kind = Json::BOOL; v.b = true; p += 4; return v; }
+        if (!strncmp(p, "false", 5)) { v.kind = Json::BOOL; p += 5; return v; }
+        if (!strncmp(p, "null", 4)) { p += 4; return v; }
+        char* e = nullptr;
+        v.num = std::strtod(p, &e);
+        if (e == p) fail("bad value");
+        v.kind = Json::NUM;
+        p = e;
+        return v;
+    }
+};
+
+Json parse_file(const std::string& path) {
+    std::ifstream in(path);
+    if (!in) throw Error(SPH_E_INVALID, "cannot open scene file '" + path + "'");
+    std::stringstream ss;
+    ss << in.rdbuf();
+    const std::string s = ss.str();
+    Parser ps{s.data(), s.data() + s.size()};
+    return ps.value();
+}
+
+/* rotation matrix (row-major 3x4 with translation c) of a unit quaternion (x, y, z, w) */
+void pose(const double q[4], const double c[3], float out[12]) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    const double n = std::sqrt(x * x + y * y + z * z + w * w);
+    const double a = x / n, b = y / n, cc = z / n, d = w / n;
+    const double m[9] = {1 - 2 * (b * b + cc * cc), 2 * (a * b - cc * d),     2 * (a * cc + b * d),
+                         2 * (a * b + cc * d),     1 - 2 * (a * a + cc * cc), 2 * (b * cc - a * d),
+                         2 * (a * cc - b * d),     2 * (b * cc + a * d),     1 - 2 * (a * a + b * b)};
+    for (int r = 0; r < 3; ++r) {
+        for (int k = 0; k < 3; ++k) out[4 * r + k] = (float)m[3 * r + k];
+        out[4 * r + 3] = (float)c[r];
+    }
+}
+
+struct Scene {
+    float container[3] = {0, 0, 0};
+    std::vector<std::shared_ptr<FluidVolume>> volumes;
+    std::vector<std::pair<std::string, std::shared_ptr<RigidBody>>> bodies;
+};
+
+Scene load_scene(const std::string& path, bool container_boundary) {
+    const Json j = parse_file(path);
+    Scene sc;
+    const Json& c = j["container"];
+    sc.container[0] = (float)c["width"].number();
+    sc.container[1] = (float)c["height"].number();
+    sc.container[2] = (float)c["depth"].number();
+    if (container_boundary)
+        sc.bodies.emplace_back("container",
+                               std::make_shared<FishTank>(sc.container[0], sc.container[1], sc.container[2]));
+    for (const Json& v : j["fluid_volumes"].arr) {
+        if (v["type"].str != "box") {
+            std::fprintf(stderr, "skipping fluid volume of type '%s'\n", v["type"].str.c_str());
+            continue;
+        }
+        sc.volumes.push_back(std::make_shared<BoxVolume>(
+            (float)v["size"][0].number(), (float)v["size"][1].number(), (float)v["size"][2].number(),
+            (float)v["center"][0].number(), (float)v["center"][1].number(), (float)v["center"][2].number()));
+    }
+    for (const Json& r : j["rigid_bodies"].arr) {
+        if (r["type"].str != "cube") {
+            std::fprintf(stderr, "skipping rigid body '%s' of type '%s'\n", r["name"].str.c_str(),
+                         r["type"].str.c_str());
+            continue;
+        }
+        auto cube = std::make_shared<Cube>((float)r["size"].number());
+        const double q[4] = {r["rotation"][0].number(0), r["rotation"][1].number(0), r["rotation"][2].number(0),
+                             r["rotation"][3].number(1)};
+        const double ctr[3] = {r["center"][0].number(), r["center"][1].number(), r["center"][2].number()};
+        pose(q, ctr, cube->rot3x4);
+        cube->mass = (float)r["mass"].number();
+        sc.bodies.emplace_back(r["name"].str, cube);
+    }
+    return sc;
+}
+
+/* A volume whose particles are jittered (splitmix64 stream, amplitude 1e-4 m). */
+class Jittered : public FluidVolume {
+   public:
+    Jittered(std::shared_ptr<FluidVolume> v, uint64_t seed) : v_(std::move(v)), seed_(seed) {}
+    std::vector<Float4> particles(float r) override {
+        std::vector<Float4> p = v_->particles(r);
+        if (!p.empty()) sph_jitter(&p[0].x, (int)p.size(), 1e-4f, seed_);
+        return p;
+    }
+
+   private:
+    std::shared_ptr<FluidVolume> v_;
+    uint64_t seed_;
+};
+
+int usage() {
+    std::fprintf(stderr,
+                 "usage: sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]\n"
+                 "                  [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]\n");
+    return 2;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    std::string config, scene_file, dump, mode = "physics";
+    int steps = 100, every = 0;
+    bool dry = false, container_boundary = false;
+    long long jitter = -1;
+    for (int a = 1; a < argc; ++a) {
+        const std::string k = argv[a];
+        auto next = [&]() -> std::string {
+            if (a + 1 >= argc) throw Error(SPH_E_INVALID, "missing value after " + k);
+            return argv[++a];
+        };
+        try {
+            if (k == "--config") config = next();
+            else if (k == "--scene") scene_file = next();
+            else if (k == "--steps") steps = std::atoi(next().c_str());
+            else if (k == "--every") every = std::atoi(next().c_str());
+            else if (k == "--mode") mode = next();
+            else if (k == "--dump") dump = next();
+            else if (k == "--jitter") jitter = std::atoll(next().c_str());
+            else if (k == "--container-boundary") container_boundary = true;
+            else if (k == "--dry-run") dry = true;
+            else return usage();
+        } catch (const Error& e) {
+            std::fprintf(stderr, "%s\n", e.what());
+            return usage();
+        }
+    }
+    if (config.empty() || scene_file.empty()) return usage();
+    try {
+        PhysicsSettings phys;
+        SimulationSettings sim;
+        load_settings(config, phys, sim);
+        Scene sc = load_scene(scene_file, container_boundary);
+        if (jitter >= 0)
+            for (size_t v = 0; v < sc.volumes.size(); ++v)
+                sc.volumes[v] = std::make_shared<Jittered>(sc.volumes[v], (uint64_t)jitter + v);
+        if (dry) {
+            size_t nf = 0, nb = 0;
+            for (auto& v : sc.volumes) nf += v->particles(sim.fluid_particle_radius).size();
+            for (auto& b : sc.bodies) nb += b.second->surface_sampling(2.0f * sim.fluid_particle_radius).size();
+            std::printf("{\"method\": \"%s\", \"time_step\": %g, \"particles\": %zu, \"boundary_particles\": %zu, "
+                        "\"volumes\": %zu, \"bodies\": %zu, \"container\": [%g, %g, %g]}\n",
+                        sim.sim_method == SimulationSettings::PCISPH ? "pcisph" : "wcsph", sim.time_step, nf, nb,
+                        sc.volumes.size(), sc.bodies.size(), sc.container[0], sc.container[1], sc.container[2]);
+            return 0;
+        }
+        DeviceOptions opt;
+        opt.mode = mode == "compat" ? SPH_MODE_COMPAT : SPH_MODE_PHYSICS;
+        auto fluid = FluidSimulationFactory::build_simulation(phys, sim, opt);
+        fluid->set_rect_limits(sc.container[0], sc.container[1], sc.container[2]);
+        for (auto& b : sc.bodies) fluid->add_boundary(b.second, b.first, b.second->mass > 0.0f);
+        for (auto& v : sc.volumes) fluid->add_volume(v);
+        const char* names[8] = {"mean_compression", "mean_abs_density_error", "max_density_error", "kinetic",
+                                "potential", "com_x", "com_y", "com_z"};
+        fluid->synchronize();
+        const auto t0 = std::chrono::steady_clock::now();
+        for (int s = 1; s <= steps; ++s) {
+            fluid->simulate();
+            if (every > 0 && s % every == 0) {
+                const std::vector<double> st = fluid->stats();
+                std::printf("{\"step\": %d", s);
+                for (int k = 0; k < 8; ++k) std::printf(", \"%s\": %.9g", names[k], st[k]);
+                std::printf(", \"flags\": %u}\n", fluid->device_flags());
+                std::fflush(stdout);
+            }
+        }
+        fluid->synchronize();
+        const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        const int n = fluid->particle_count();
+        std::printf("{\"done\": %d, \"particles\": %d, \"boundary_particles\": %d, \"seconds\": %.6f, "
+                    "\"particle_updates_per_s\": %.6g, \"flags\": %u}\n",
+                    steps, n, fluid->boundary_particle_count(), sec, sec > 0 ? (double)n * steps / sec : 0.0,
+                    fluid->device_flags());
+        if (!dump.empty()) {
+            std::vector<Float4> pos = fluid->positions();
+            std::vector<int32_t> ids = fluid->ids();
+            std::vector<Float4> by_id(pos.size());
+            for (size_t i = 0; i < pos.size(); ++i) by_id[(size_t)ids[i]] = pos[i];
+            std::ofstream out(dump, std::ios::binary);
+            out.write(reinterpret_cast<const char*>(by_id.data()), (std::streamsize)(by_id.size() * sizeof(Float4)));
+        }
+    } catch (const Error& e) {
+        std::fprintf(stderr, "error (status %d): %s\n", e.status(), e.what());
+        return 1;
+    }
+    return 0;
+}

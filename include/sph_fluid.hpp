@@ -1,0 +1,353 @@
+/*
+ * sph_fluid.hpp -- C++ host mirror of the reference's solver interface over the C ABI of
+ * sph_capi.h (header only, C++17).
+ *
+ * The reference's application code talks to its solvers through
+ *   class FluidSimulation            (fluid/simulation/fluidsimulation.h:23-92)
+ *   FluidSimulationFactory           (fluid/simulation/fluidsimulationfactory.h:13-40)
+ *   PhysicsSettings / SimulationSettings (settings/physicssettings.h, simulationsettings.h)
+ *   FluidVolume / BoxVolume          (fluid/simulation/fluidvolume.h, boxvolume.cpp:11-40)
+ *   RigidBody + surface sampling     (scene/rigidbody.h, scene/fishtank.cpp, scene/cube.cpp)
+ *   Settings::load key=value files   (settings/settings.cpp:14-59, settings/fileparser.cpp)
+ * This header keeps those names, method signatures and semantics so the calling code stays
+ * a drop-in.  What changes: OpenCL float4 becomes sph_gb300::Float4, the GL vertex buffer the
+ * reference renders from becomes a device pointer (device_positions()), Bullet rigid bodies
+ * become a plain pose + surface sampling, and errors, reported by the reference as CLError
+ * (a std::runtime_error, clerror.cpp:15-19), are thrown as sph_gb300::Error with the C
+ * ABI's status code.
+ */
+#pragma once
+
+#include <cstdint>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sph_capi.h"
+
+namespace sph_gb300 {
+
+struct Float4 {
+    float x, y, z, w;
+};
+
+/* A failed C-ABI call: status (SPH_E_*) and the context's message. */
+class Error : public std::runtime_error {
+   public:
+    Error(int status, const std::string& msg) : std::runtime_error(msg), status_(status) {}
+    int status() const { return status_; }
+
+   private:
+    int status_;
+};
+
+inline void check(int rc, const sph_ctx* ctx) {
+    if (rc != SPH_OK) throw Error(rc, sph_last_error(ctx));
+}
+
+/* Fluid physical properties; field names and defaults of settings/physicssettings.h. */
+struct PhysicsSettings {
+    float rest_density = 998.29f;
+    float k_viscosity = 0.0035105f;
+    float gravity = 9.8f;
+    float gas_stiffness = 3.0f;
+    float surface_tension = 0.0728f;
+};
+
+/* Simulation parameters; field names and defaults of settings/simulationsettings.h. */
+struct SimulationSettings {
+    enum Method { WCSPH, PCISPH };
+    float time_step = 0.01f;
+    float max_vel = 50.0f;
+    float fluid_particle_radius = 0.008f;
+    float fluid_support_radius = 0.032f;
+    int pcisph_max_iterations = 7;
+    float pcisph_error_ratio = 0.01f;
+    Method sim_method = WCSPH;
+};
+
+/* Options of the GB300 build with no counterpart in the reference's settings. */
+struct DeviceOptions {
+    int mode = SPH_MODE_PHYSICS;          /* SPH_MODE_COMPAT reproduces the kernel text */
+    int neighbor_mode = SPH_NEIGH_LIST;
+    int use_graph = 1;
+    void* cuda_stream = nullptr;          /* null: the context creates its own */
+};
+
+/* Settings::load (settings/settings.cpp:14-59) over FileParser's key=value format
+ * (settings/fileparser.cpp:7-27): '#' starts a comment, every key of the simulation and
+ * physics settings is required, method is wcsph or pcisph. */
+inline void load_settings(const std::string& path, PhysicsSettings& phys, SimulationSettings& sim) {
+    std::ifstream in(path);
+    if (!in) throw Error(SPH_E_INVALID, "cannot open settings file '" + path + "'");
+    std::map<std::string, std::string> kv;
+    std::string line;
+    while (std::getline(in, line)) {
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line.resize(hash);
+        const size_t eq = line.find('=');
+        if (eq == std::string::npos) continue;
+        auto trim = [](std::string s) {
+            const char* ws = " \t\r\n";
+            s.erase(0, s.find_first_not_of(ws));
+            s.erase(s.find_last_not_of(ws) + 1);
+            return s;
+        };
+        kv[trim(line.substr(0, eq))] = trim(line.substr(eq + 1));
+    }
+    auto opt = [&](const char* k) -> const std::string& {
+        auto it = kv.find(k);
+        if (it == kv.end()) throw Error(SPH_E_INVALID, std::string("settings file lacks '") + k + "'");
+        return it->second;
+    };
+    sim.time_step = (float)std::atof(opt("time_step").c_str());
+    sim.max_vel = (float)std::atof(opt("max_vel").c_str());
+    sim.fluid_particle_radius = (float)std::atof(opt("fluid_particle_radius").c_str());
+    sim.fluid_support_radius = (float)std::atof(opt("fluid_support_radius").c_str());
+    sim.pcisph_max_iterations = std::atoi(opt("pcisph_max_iterations").c_str());
+    sim.pcisph_error_ratio = (float)std::atof(opt("pcisph_error_ratio").c_str());
+    const std::string& m = opt("method");
+    if (m == "wcsph") sim.sim_method = SimulationSettings::WCSPH;
+    else if (m == "pcisph") sim.sim_method = SimulationSettings::PCISPH;
+    else throw Error(SPH_E_INVALID, "Unknown simulation method '" + m + "'!");
+    phys.rest_density = (float)std::atof(opt("rest_density").c_str());
+    phys.k_viscosity = (float)std::atof(opt("k_viscosity").c_str());
+    phys.gravity = (float)std::atof(opt("gravity").c_str());
+    phys.gas_stiffness = (float)std::atof(opt("gas_stiffness").c_str());
+    phys.surface_tension = (float)std::atof(opt("surface_tension").c_str());
+}
+
+/* FluidVolume (fluid/simulation/fluidvolume.h): a block of fluid sampled at a radius. */
+class FluidVolume {
+   public:
+    virtual ~FluidVolume() = default;
+    virtual std::vector<Float4> particles(float particle_radius) = 0;
+};
+
+/* BoxVolume (fluid/simulation/boxvolume.cpp:11-40) through sph_scene_box_volume. */
+class BoxVolume : public FluidVolume {
+   public:
+    BoxVolume(float w, float h, float d, float cx, float cy, float cz) : size_{w, h, d}, center_{cx, cy, cz} {}
+    std::vector<Float4> particles(float particle_radius) override {
+        const int n = sph_scene_box_volume(size_, center_, particle_radius, nullptr, 0);
+        std::vector<Float4> out((size_t)(n > 0 ? n : 0));
+        if (n > 0) sph_scene_box_volume(size_, center_, particle_radius, &out[0].x, n);
+        return out;
+    }
+
+   private:
+    float size_[3], center_[3];
+};
+
+/* A volume given as explicit particle positions (jittered lattices, loaded states). */
+class PointVolume : public FluidVolume {
+   public:
+    explicit PointVolume(std::vector<Float4> pts) : pts_(std::move(pts)) {}
+    std::vector<Float4> particles(float) override { return pts_; }
+
+   private:
+    std::vector<Float4> pts_;
+};
+
+/* RigidBody without a physics engine: a pose (row-major 3x4 rotation | translation, linear
+ * and angular velocity) and a surface sampling in body coordinates.  Mass > 0 makes the
+ * solver report fluid forces and torques on it (boundaryhandler.cpp:296-349). */
+class RigidBody {
+   public:
+    virtual ~RigidBody() = default;
+    virtual std::vector<Float4> surface_sampling(float spacing) const = 0;
+    float mass = 0.f;
+    float rot3x4[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    float linear_velocity[4] = {0, 0, 0, 0};
+    float angular_velocity[4] = {0, 0, 0, 0};
+};
+
+/* FishTank (scene/fishtank.cpp:108-141): base and four walls, open top. */
+class FishTank : public RigidBody {
+   public:
+    FishTank(float w, float h, float d) : w_(w), h_(h), d_(d) {}
+    std::vector<Float4> surface_sampling(float spacing) const override {
+        const int n = sph_scene_fishtank(w_, h_, d_, spacing, nullptr, 0);
+        std::vector<Float4> out((size_t)(n > 0 ? n : 0));
+        if (n > 0) sph_scene_fishtank(w_, h_, d_, spacing, &out[0].x, n);
+        return out;
+    }
+
+   private:
+    float w_, h_, d_;
+};
+
+/* Cube (scene/cube.cpp:136-171): hollow shell of the given side. */
+class Cube : public RigidBody {
+   public:
+    explicit Cube(float side) : side_(side) {}
+    std::vector<Float4> surface_sampling(float spacing) const override {
+        const int n = sph_scene_cube(side_, spacing, nullptr, 0);
+        std::vector<Float4> out((size_t)(n > 0 ? n : 0));
+        if (n > 0) sph_scene_cube(side_, spacing, &out[0].x, n);
+        return out;
+    }
+
+   private:
+    float side_;
+};
+
+/* FluidSimulation (fluid/simulation/fluidsimulation.h:23-92): same methods. */
+class FluidSimulation {
+   public:
+    virtual ~FluidSimulation() = default;
+    virtual void simulate() = 0;
+    virtual void reset(const PhysicsSettings& fluid_settings, const SimulationSettings& sim_settings) = 0;
+    virtual int particle_count() const = 0;
+    virtual void add_boundary(const std::shared_ptr<RigidBody> boundary, const std::string& boundary_id,
+                              bool can_move = false) = 0;
+    virtual void set_rect_limits(float width, float height, float depth) = 0;
+    virtual int boundary_particle_count() const = 0;
+    virtual void add_volume(const std::shared_ptr<FluidVolume> volume) = 0;
+};
+
+inline sph_params to_params(const PhysicsSettings& ph, const SimulationSettings& si, const DeviceOptions& o) {
+    sph_params p;
+    const int method = si.sim_method == SimulationSettings::PCISPH ? SPH_PCISPH : SPH_WCSPH;
+    sph_default_params(method, &p);
+    p.mode = o.mode;
+    p.time_step = si.time_step;
+    p.max_vel = si.max_vel;
+    p.particle_radius = si.fluid_particle_radius;
+    p.support_radius = si.fluid_support_radius;
+    p.pcisph_max_iterations = si.pcisph_max_iterations;
+    p.pcisph_error_ratio = si.pcisph_error_ratio;
+    p.rest_density = ph.rest_density;
+    p.k_viscosity = ph.k_viscosity;
+    p.gravity = ph.gravity;
+    p.gas_stiffness = ph.gas_stiffness;
+    p.surface_tension = ph.surface_tension;
+    p.neighbor_mode = o.neighbor_mode;
+    p.use_graph = o.use_graph;
+    return p;
+}
+
+/* The CUDA solver behind FluidSimulation: WCSPHSimulation (wcsphsimluation.cpp) or
+ * PCISPHSimulation (pcisphsimluation.cpp) depending on SimulationSettings::sim_method. */
+class CudaFluidSimulation : public FluidSimulation {
+   public:
+    CudaFluidSimulation(const PhysicsSettings& ph, const SimulationSettings& si, const DeviceOptions& opt = {})
+        : opt_(opt) {
+        params_ = to_params(ph, si, opt);
+        check(sph_create(&params_, &ctx_), nullptr);
+        if (opt_.cuda_stream) check(sph_set_stream(ctx_, opt_.cuda_stream), ctx_);
+    }
+    ~CudaFluidSimulation() override {
+        if (ctx_) sph_destroy(ctx_);
+    }
+    CudaFluidSimulation(const CudaFluidSimulation&) = delete;
+    CudaFluidSimulation& operator=(const CudaFluidSimulation&) = delete;
+
+    void simulate() override { check(sph_simulate(ctx_, 1), ctx_); }
+    /* n steps in one call (one graph replay each, no host round trip in between) */
+    void simulate(int steps) { check(sph_simulate(ctx_, steps), ctx_); }
+    void reset(const PhysicsSettings& ph, const SimulationSettings& si) override {
+        params_ = to_params(ph, si, opt_);
+        check(sph_reset(ctx_, &params_), ctx_);
+    }
+    int particle_count() const override { return sph_particle_count(ctx_); }
+    void add_boundary(const std::shared_ptr<RigidBody> body, const std::string& boundary_id,
+                      bool can_move = false) override {
+        const std::vector<Float4> pts = body->surface_sampling(2.0f * params_.particle_radius);
+        if (pts.empty()) return;
+        check(sph_add_boundary(ctx_, &pts[0].x, (int)pts.size(), can_move ? 1 : 0, body->rot3x4,
+                               body->linear_velocity, body->angular_velocity, body->mass),
+              ctx_);
+        body_ids_.push_back(boundary_id);
+        bodies_.push_back(body);
+    }
+    void set_rect_limits(float w, float h, float d) override { check(sph_set_rect_limits(ctx_, w, h, d), ctx_); }
+    int boundary_particle_count() const override { return sph_boundary_particle_count(ctx_); }
+    void add_volume(const std::shared_ptr<FluidVolume> volume) override {
+        const std::vector<Float4> pts = volume->particles(params_.particle_radius);
+        if (pts.empty()) return;
+        check(sph_add_volume(ctx_, &pts[0].x, nullptr, (int)pts.size()), ctx_);
+    }
+    /* A volume with initial velocities (float4 per particle). */
+    void add_volume(const std::vector<Float4>& pos, const std::vector<Float4>& vel) {
+        if (pos.empty()) return;
+        check(sph_add_volume(ctx_, &pos[0].x, vel.empty() ? nullptr : &vel[0].x, (int)pos.size()), ctx_);
+    }
+
+    /* Moves a movable body (the pose RigidBody::update hands to the solver each frame). */
+    void set_body_transform(const std::string& boundary_id, const float rot3x4[12], const float lin[4],
+                            const float ang[4]) {
+        for (size_t b = 0; b < body_ids_.size(); ++b)
+            if (body_ids_[b] == boundary_id) {
+                check(sph_set_body_transform(ctx_, (int)b, rot3x4, lin, ang), ctx_);
+                return;
+            }
+        throw Error(SPH_E_INVALID, "unknown boundary id '" + boundary_id + "'");
+    }
+    /* Fluid force and torque on every body (zero for bodies of zero mass). */
+    void body_forces(std::vector<Float4>& force, std::vector<Float4>& torque) {
+        force.assign(body_ids_.size(), Float4{0, 0, 0, 0});
+        torque.assign(body_ids_.size(), Float4{0, 0, 0, 0});
+        if (body_ids_.empty()) return;
+        check(sph_body_forces(ctx_, &force[0].x, &torque[0].x, (int)body_ids_.size()), ctx_);
+    }
+
+    /* Host copies of the state, in the solver's current particle order (ids() gives each
+     * particle's id = its index in the order the volumes were added). */
+    std::vector<Float4> positions() { return get4(SPH_F_POS); }
+    std::vector<Float4> velocities() { return get4(SPH_F_VEL); }
+    std::vector<int32_t> ids() {
+        std::vector<int32_t> out((size_t)particle_count());
+        if (!out.empty()) check(sph_get_field(ctx_, SPH_F_ID, out.data(), out.size() * 4), ctx_);
+        return out;
+    }
+    /* The positions buffer on the device: what the reference shares with OpenGL as a VBO. */
+    const void* device_positions() {
+        void* p = nullptr;
+        check(sph_field_device_ptr(ctx_, SPH_F_POS, &p), ctx_);
+        return p;
+    }
+    /* mean compression, mean |density error|, max density error, kinetic and potential
+     * energy, centre of mass (x, y, z) */
+    std::vector<double> stats() {
+        std::vector<double> out(8);
+        check(sph_stats(ctx_, out.data()), ctx_);
+        return out;
+    }
+    unsigned device_flags(bool clear = false) {
+        unsigned f = 0;
+        check(sph_device_flags(ctx_, &f, clear ? 1 : 0), ctx_);
+        return f;
+    }
+    void synchronize() { check(sph_synchronize(ctx_), ctx_); }
+    sph_ctx* handle() { return ctx_; }
+
+   private:
+    std::vector<Float4> get4(int field) {
+        std::vector<Float4> out((size_t)particle_count());
+        if (!out.empty()) check(sph_get_field(ctx_, field, &out[0].x, out.size() * sizeof(Float4)), ctx_);
+        return out;
+    }
+    sph_params params_{};
+    DeviceOptions opt_;
+    sph_ctx* ctx_ = nullptr;
+    std::vector<std::string> body_ids_;
+    std::vector<std::shared_ptr<RigidBody>> bodies_;
+};
+
+/* FluidSimulationFactory::build_simulation (fluidsimulationfactory.h:13-40) without the GL
+ * buffer argument. */
+struct FluidSimulationFactory {
+    static std::unique_ptr<CudaFluidSimulation> build_simulation(const PhysicsSettings& ph,
+                                                                 const SimulationSettings& si,
+                                                                 const DeviceOptions& opt = {}) {
+        return std::unique_ptr<CudaFluidSimulation>(new CudaFluidSimulation(ph, si, opt));
+    }
+};
+
+}  // namespace sph_gb300

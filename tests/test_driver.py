@@ -1,0 +1,102 @@
+"""The C++ host mirror (include/sph_fluid.hpp) and the headless driver built on it: settings
+files in the reference's key=value format, scene files in its JSON format, and on the GPU
+the same result as the Python API on the same scene."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import fluids_gb300
+from fluids_gb300 import capi
+from fluids_gb300.scenes import BoxVolume, Cube, FishTank
+
+CONFIG = """# Simulation settings
+time_step=0.0002
+max_vel=10.0
+fluid_particle_radius=0.0075
+fluid_support_radius=0.03
+pcisph_max_iterations=3
+pcisph_error_ratio=0.01
+method=wcsph
+
+# Physics settings
+rest_density=1000
+k_viscosity=0.01
+gravity=9.81
+gas_stiffness=57142.857
+surface_tension=0.001
+"""
+
+SCENE = {"container": {"width": 0.6, "height": 0.6, "depth": 0.4},
+         "fluid_volumes": [{"type": "box", "name": "fluid_1", "size": [0.24, 0.3, 0.2], "center": [0.15, -0.14, 0.0]}],
+         "rigid_bodies": [{"type": "cube", "name": "cube_1", "mass": 0.0, "size": 0.1, "center": [-0.15, -0.24, 0.0],
+                           "rotation": [0, 0, 0, 1]},
+                          {"type": "sphere", "name": "ball", "mass": 0.0, "size": 0.05, "center": [0, 0, 0]}]}
+
+
+@pytest.fixture(scope="module")
+def driver():
+    return fluids_gb300.build_driver()
+
+
+def write(tmp_path, config=CONFIG, scene=SCENE):
+    c = tmp_path / "config.wc"
+    c.write_text(config)
+    s = tmp_path / "scene.json"
+    s.write_text(json.dumps(scene))
+    return str(c), str(s)
+
+
+def test_driver_parses_reference_formats(driver, tmp_path):
+    c, s = write(tmp_path)
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run", "--container-boundary"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = json.loads(r.stdout)
+    n = len(BoxVolume((0.24, 0.3, 0.2), (0.15, -0.14, 0.0)).particles(0.0075))
+    nb = len(FishTank(0.6, 0.6, 0.4).surface_sampling(0.015)) + len(Cube(0.1).surface_sampling(0.015))
+    assert out["particles"] == n and out["boundary_particles"] == nb
+    assert out["method"] == "wcsph" and out["bodies"] == 2 and "sphere" in r.stderr
+
+
+def test_driver_rejects_incomplete_settings(driver, tmp_path):
+    c, s = write(tmp_path, config=CONFIG.replace("gas_stiffness=57142.857\n", ""))
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run"], capture_output=True, text=True)
+    assert r.returncode == 1 and "gas_stiffness" in r.stderr
+    c, s = write(tmp_path, config=CONFIG.replace("method=wcsph", "method=flip"))
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run"], capture_output=True, text=True)
+    assert r.returncode == 1 and "flip" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_matches_python_api(gpu_lib, driver, tmp_path):
+    c, s = write(tmp_path)
+    dump = str(tmp_path / "pos.bin")
+    steps = 30
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--steps", str(steps), "--every", "10",
+                        "--container-boundary", "--dump", dump], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(x) for x in r.stdout.splitlines()]
+    assert [x["step"] for x in lines[:-1]] == [10, 20, 30] and lines[-1]["done"] == steps
+    got = np.fromfile(dump, np.float32).reshape(-1, 4)
+    # the driver runs PHYSICS mode unless --mode compat (the C ABI's default is COMPAT)
+    p = capi.make_params(capi.SPH_WCSPH, mode=capi.SPH_MODE_PHYSICS, time_step=2e-4, max_vel=10.0, particle_radius=0.0075,
+                         support_radius=0.03, pcisph_max_iterations=3, pcisph_error_ratio=0.01, rest_density=1000.0,
+                         k_viscosity=0.01, gravity=9.81, gas_stiffness=57142.857, surface_tension=0.001)
+    ctx = capi.Context(p)
+    ctx.set_rect_limits(0.6, 0.6, 0.4)
+    ctx.add_boundary(FishTank(0.6, 0.6, 0.4).surface_sampling(0.015))
+    cube = Cube(0.1, position=(-0.15, -0.24, 0.0))
+    ctx.add_boundary(cube.surface_sampling(0.015), rot3x4=cube.rot3x4())
+    ctx.add_volume(BoxVolume((0.24, 0.3, 0.2), (0.15, -0.14, 0.0)).particles(0.0075))
+    ctx.simulate(steps)
+    ctx.synchronize()
+    pos = ctx.get("POS").reshape(-1, 4)
+    ids = ctx.get("ID")
+    ref = np.empty_like(pos)
+    ref[ids] = pos
+    assert np.array_equal(got, ref)
+    st = ctx.stats()
+    assert lines[-2]["kinetic"] == pytest.approx(st["kinetic"], rel=1e-8)   # printed with 9 digits
