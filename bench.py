@@ -34,16 +34,23 @@ UNIT = "particle-updates/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
-# Algorithmic HBM bytes per fluid particle of each kernel (compulsory traffic; neighbour reads
-# are assumed to hit L1/L2).  The derivation is tabulated in the design doc.
+# Algorithmic HBM bytes per fluid particle of each kernel (compulsory traffic; neighbour data
+# is assumed to come from L1/L2).  The list-based kernels also move their neighbour lists:
+# LIST_BYTES[k] = (bytes per fluid-list entry, bytes per boundary-list entry, fixed bytes),
+# multiplied by the step's mean list lengths.  The derivation is tabulated in the design doc.
 ALG_BYTES = {
     "k_hashes": 16 + 4 + 4 + 4 + 8,          # pos in; key, mask out; cell_prev in; clear 8 B/cell (upper bound)
     "k_gather": 4 + 3 * 16 * 2 + 4 * 2,      # perm; pos/vel/vhalf gathered and written; ids
     "k_cell_ranges": 16 + 8 + 4 + 8,         # sorted pos, 2 keys, cell id out, range writes (per cell)
     "k_wc_density": 16 + 8,                  # own position; density and pressure out
-    "k_lists_density": 16 + 8,               # same compulsory bytes; the lists it writes are scratch
-    "k_normals": 16 + 16,                    # own position; normal out
+    "k_lists_density": 16 + 8 + 16,          # own position; density, pressure, aux out (+ the lists it writes)
+    "k_normals": 16 + 16,                    # own position; normal out (+ the fluid list it reads)
     "k_wc_forces": 16 * 3 + 4 + 4 + 16 + 4 + 16 * 3 + 4,   # pos,vel,vhalf,rho,p,normal,id in; pos,vel,vhalf,id out
+}
+LIST_BYTES = {
+    "k_lists_density": (4, 4, 8),            # entries written, two lengths written
+    "k_normals": (4, 0, 4),                  # fluid entries read, its length read
+    "k_wc_forces": (4, 4, 8),                # both lists read, both lengths read
 }
 
 
@@ -422,13 +429,18 @@ def main():
     peak, peak_kind = measured_hbm_peak()
     alg = ALG_BYTES.get(top)
     roof = None
+    mean_len = (float(ctx.get("NEIGH_LEN").mean()), float(ctx.get("SB_NEIGH_LEN").mean()) if nb > 0 else 0.0)
     if alg is not None:
         bnd_extra = 20.0 * nb if top in ("k_wc_density", "k_wc_forces") else 0.0
+        lb = LIST_BYTES.get(top)
+        if lb is not None and params.neighbor_mode == 1:
+            alg = alg + lb[0] * mean_len[0] + lb[1] * mean_len[1] + lb[2]
         bytes_launch = alg * n + bnd_extra
         achieved = bytes_launch / (kern[top] / 1000.0) / 1e9
         tr = measured_traffic(top, w["name"])
         roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes": bytes_launch,
+                "mean_list_lengths": {"fluid": mean_len[0], "boundary": mean_len[1]},
                 "traffic": tr, "ms_per_launch": kern[top]}
     passes = (d["key_bits"] + 7) // 8
     launches_per_step = sum(1 for k in kern) + (passes if "sort" in kern else 0)
