@@ -334,7 +334,7 @@ int run_stage_impl(sph_ctx* x, int stage) {
     case SPH_S_NEIGH_LIST:
     case SPH_S_SB_NEIGH_LIST:
         sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
-                                b.scenes, b.scene_of);
+                                b.scenes, b.scene_of, b.bnear);
         break;
     case SPH_S_WC_DENSITY:
         sph::launch_wc_density(s, c, b, x->p.neighbor_mode == SPH_NEIGH_LIST, bs);
@@ -425,7 +425,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
         mark(x, "k_wc_forces");
     } else {
         sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
-                                b.scenes, b.scene_of);
+                                b.scenes, b.scene_of, b.bnear);
         mark(x, "k_neigh_lists");
         sph::launch_pci_init_density(s, c, b, bs);
         mark(x, "k_pci_init_density");

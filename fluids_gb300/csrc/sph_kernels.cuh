@@ -74,7 +74,7 @@ void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, cons
                         const int32_t* scene_of);
 void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, const int2* tab, const float4* bpos_s,
                         const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs,
-                        const SceneDev* scenes, const int32_t* scene_of);
+                        const SceneDev* scenes, const int32_t* scene_of, const uint8_t* bnear);
 
 /* sph_wcsph.cu */
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);
