@@ -97,7 +97,8 @@ def describe_workload(w, n, nb, params):
         "container_m": list(w["container"]),
         "mode": "physics" if p.mode == 1 else "compat",
         "neighbors": "list" if p.neighbor_mode == 1 or p.method == 1 else "cell-scan",
-        "l2": "inputs larger than L2 every step (particle state %.0f MB > 129 MB)" % (n * 200 / 1e6),
+        "l2": ("inputs larger than L2 every step (particle state %.0f MB > 129 MB)" if n * 200 > 129e6 else
+               "particle state %.0f MB (fits the 129 MB L2)") % (n * 200 / 1e6),
     }
 
 
