@@ -222,20 +222,38 @@ __device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py
  * comes from the caller.  No cell is skipped by distance: in a warp the lanes that share a
  * cell would skip different cells, so the warp walks their union anyway, and measured on
  * GB300 the skipping test cost more than it saved. */
+#ifndef SPH_BUILD_UNROLL
+#define SPH_BUILD_UNROLL 2
+#endif
+constexpr int kBuildUnroll = SPH_BUILD_UNROLL;
+/* CELL_NEIGH_OFFSET order as (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4, one byte per offset. */
+static __constant__ uint8_t kNeighCode[27] = {
+    0x15, 0x00, 0x10, 0x20, 0x04, 0x14, 0x24, 0x08, 0x18, 0x28, 0x01, 0x11, 0x21,
+    0x05, 0x25, 0x09, 0x19, 0x29, 0x02, 0x12, 0x22, 0x06, 0x16, 0x26, 0x0a, 0x1a, 0x2a};
 template <class F>
 __device__ __forceinline__ int build_scan(const Const& c, float px, float py, float pz, int cx, int cy, int cz,
                                           const int2* __restrict__ tab, const float4* __restrict__ npos, F&& f) {
     const float h2 = c.h2_list;
     int cnt = 0;
+    /* PHYSICS grid: 32-bit cell ids (the grid has < 2^31 cells) and no bounds test for a cell
+     * whose 26 neighbours are all inside the grid */
+    const bool interior = !c.wrap && cx > 0 && cy > 0 && cz > 0 && cx < c.nx - 1 && cy < c.ny - 1 &&
+                          cz < c.nz - 1;
+    const int sy = c.nx, sz = c.nx * c.ny;
+    const int base = cx + sy * cy + sz * cz;
 #pragma unroll 1
     for (int o = 0; o < 27 && cnt < c.cap; ++o) {
-        int ox, oy, oz;
-        neigh_offset(o, ox, oy, oz);
+        const int code = kNeighCode[o];
+        const int ox = (code & 3) - 1, oy = ((code >> 2) & 3) - 1, oz = ((code >> 4) & 3) - 1;
         long long id;
-        if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) continue;
+        if (interior) {
+            id = base + ox + sy * oy + sz * oz;
+        } else if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) {
+            continue;
+        }
         const int2 r = __ldg(&tab[id]);
         if (cnt + (r.y - r.x) <= c.cap) {
-#pragma unroll 4
+#pragma unroll kBuildUnroll
             for (int j = r.x; j < r.y; ++j) {
                 const float4 pj = __ldg(&npos[j]);
                 const float r2 = r2_exact(__fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
