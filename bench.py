@@ -191,12 +191,17 @@ def cpu_baseline(wl_name, mode, sample_steps, sample_desc_prefix, crop=None):
                 sample_desc_prefix, sample_steps, n, sum(len(b[0]) for b in w["bodies"]), dt)}
 
 
-def bench_batched(steps, warmup, torch, nscenes=256):
+def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
     """256 independent dam breaks (N log-uniform in [2048, 65536], containers a x 1 x 1 with
     a ~ U[1, 3], per-scene viscosity and c0): one batched context against looping the plain
-    single-scene solver over the same scenes, both on one stream, same steps."""
-    from fluids_gb300 import capi, workloads
+    single-scene solver over the same scenes, both on one stream, same steps.  With several
+    ranks the scenes are split by particle count (replicas.partition_scenes) and the
+    throughputs are whole-job (sum of particles / slowest rank)."""
+    from fluids_gb300 import capi, replicas, workloads
     scenes = workloads.batched_scenes(nscenes, seed=0)
+    if world > 1:
+        mine = replicas.partition_scenes([len(s["fluid"]) for s in scenes], world)[rank]
+        scenes = [scenes[i] for i in mine]
     shared = workloads.batched_params()
     stream = torch.cuda.Stream()
     b = capi.BatchContext(shared, scenes)
@@ -230,8 +235,12 @@ def bench_batched(steps, warmup, torch, nscenes=256):
     sl = np.array([[c.stats()[k] for k in ("mean_compression", "mean_abs_density_error")] for c in singles])
     for c in singles:
         c.close()
-    return {"scenes": nscenes, "particles": n, "boundary_particles": int(sum(len(s["boundary"]) for s in scenes)),
-            "steps": steps, "batched_updates_per_s": n * steps / tb, "looped_updates_per_s": n * steps / tl,
+    tb, units = replicas.aggregate(tb, n * steps, device="cuda")
+    tl, _ = replicas.aggregate(tl, n * steps, device="cuda")
+    n_all = int(round(units / steps))
+    return {"scenes": nscenes, "particles": n_all, "ranks": world,
+            "boundary_particles": int(sum(len(s["boundary"]) for s in scenes)),
+            "steps": steps, "batched_updates_per_s": units / tb, "looped_updates_per_s": units / tl,
             "speedup": tl / tb, "batched_ms_per_step": 1000 * tb / steps, "looped_ms_per_step": 1000 * tl / steps,
             "mean_density_error_batched": float(sb[:, 0].mean()), "mean_density_error_looped": float(sl[:, 0].mean()),
             "mean_abs_density_error_batched": float(sb[:, 1].mean()),
@@ -385,7 +394,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     torch.cuda.set_device(local_rank)
     import fluids_gb300
-    from fluids_gb300 import capi, workloads
+    from fluids_gb300 import capi, replicas, workloads
     fluids_gb300.build()
     w = load_workload(args.workload, capi.SPH_MODE_PHYSICS, seed=rank)
     params = w["params"]
@@ -417,12 +426,9 @@ def main():
         dist.barrier()
     clk = clocks.stop() if clocks else None
     t = e0.elapsed_time(e1) / 1000.0
-    if world > 1:
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t, units = replicas.aggregate(t, n * args.steps, device="cuda")   # max time, sum over ranks
     flags = ctx.device_flags()
-    value = n * args.steps * world / t
+    value = units / t
 
     # per-kernel device time of the same step (events between the kernels, no graph)
     kern = ctx.profile_step(min(args.steps, 20))
@@ -466,16 +472,13 @@ def main():
             for f, a in (("POS", hp), ("VEL", hv), ("VEL_HALF", hh)):
                 capi.check(L.sph_get_field(ctx.h, capi.FIELDS[f], a.ctypes.data, a.nbytes), ctx.h)
         te = time.perf_counter() - t0
-        if world > 1:
-            tt = torch.tensor([te], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
-        e2e = {"value": n * k_e2e * world / te, "unit": UNIT, "h2d_bytes_per_step": 48 * n,
+        te, units_e = replicas.aggregate(te, n * k_e2e, device="cuda")
+        e2e = {"value": units_e / te, "unit": UNIT, "h2d_bytes_per_step": 48 * n,
                "d2h_bytes_per_step": 48 * n, "steps": k_e2e, "host_buffers": "pinned"}
     ctx.close()
     batched = None
     if args.batched_steps > 0 and args.workload == "wcsph4m":
-        batched = bench_batched(args.batched_steps, max(args.warmup, 3), torch)
+        batched = bench_batched(args.batched_steps, max(args.warmup, 3), torch, rank=rank, world=world)
     adjoint = pcisph = None
     if args.adjoint_steps > 0 and args.workload == "wcsph4m":
         adjoint = bench_adjoint(torch, args.adjoint_steps)
