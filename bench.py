@@ -197,7 +197,7 @@ def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
     single-scene solver over the same scenes, both on one stream, same steps.  With several
     ranks the scenes are split by particle count (replicas.partition_scenes) and the
     throughputs are whole-job (sum of particles / slowest rank)."""
-    from fluids_gb300 import capi, replicas, workloads
+    from fluids_gb300 import autotune, capi, replicas, workloads
     scenes = workloads.batched_scenes(nscenes, seed=0)
     if world > 1:
         mine = replicas.partition_scenes([len(s["fluid"]) for s in scenes], world)[rank]
@@ -207,6 +207,7 @@ def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
     b = capi.BatchContext(shared, scenes)
     b.set_stream(stream.cuda_stream)
     n = b.particle_count()
+    tuned_b = autotune.tune(b, shared.method, shared.mode, True)
     b.simulate(warmup)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -219,9 +220,12 @@ def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
     flags_b = b.device_flags()
     b.close()
     singles = []
+    tuned_l = {}
     for s in scenes:
         c = workloads.build_scene_context(shared, s)
         c.set_stream(stream.cuda_stream)
+        r = autotune.tune(c, shared.method, shared.mode, False)
+        tuned_l[r["key"].split("|")[-1]] = r["block_size"]
         singles.append(c)
     for c in singles:
         c.simulate(warmup)
@@ -244,7 +248,8 @@ def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
             "speedup": tl / tb, "batched_ms_per_step": 1000 * tb / steps, "looped_ms_per_step": 1000 * tl / steps,
             "mean_density_error_batched": float(sb[:, 0].mean()), "mean_density_error_looped": float(sl[:, 0].mean()),
             "mean_abs_density_error_batched": float(sb[:, 1].mean()),
-            "mean_abs_density_error_looped": float(sl[:, 1].mean()), "device_flags": flags_b}
+            "mean_abs_density_error_looped": float(sl[:, 1].mean()), "device_flags": flags_b,
+            "block_size_batched": tuned_b["block_size"], "block_size_looped_by_size": tuned_l}
 
 
 def bench_adjoint(torch, steps=200, every=20):
@@ -408,6 +413,8 @@ def main():
     ctx.add_volume(w["fluid"], w.get("velocities"))
     n, nb = ctx.particle_count(), ctx.boundary_particle_count()
     d = capi.describe(params, w["container"])
+    from fluids_gb300 import autotune
+    tuned = autotune.tune(ctx, params.method, params.mode, False)
 
     ctx.simulate(max(args.warmup, 3))
     ctx.synchronize()
@@ -494,6 +501,7 @@ def main():
         cfg = describe_workload(w, n, nb, params)
         cfg["grid_cells"] = d["grid_dims"]
         cfg["parallelism"] = "replicas" if world > 1 else "single GPU"
+        cfg["block_size"] = tuned["block_size"]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + jitter)",

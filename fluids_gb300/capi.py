@@ -42,7 +42,7 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc", "sph_batch_create",
            "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid",
            "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
-           "sph_adj_flags", "sph_adj_tape_bytes"]
+           "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size"]
 
 
 class SphParams(C.Structure):
@@ -143,6 +143,7 @@ def lib():
                                       C.POINTER(C.c_double)]),
             "sph_adj_flags": (ip, [vp, C.POINTER(C.c_uint)]),
             "sph_adj_tape_bytes": (ip, [vp, C.POINTER(C.c_size_t)]),
+            "sph_set_block_size": (ip, [vp, ip]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -246,6 +247,9 @@ class Context:
     def set_stream(self, cuda_stream):
         """Runs this context's work on a caller stream (an integer cudaStream_t)."""
         self._c(self._lib.sph_set_stream(self.h, C.c_void_p(int(cuda_stream))))
+
+    def set_block_size(self, block_size):
+        self._c(self._lib.sph_set_block_size(self.h, int(block_size)))
 
     def set_rect_limits(self, w, h, d):
         self._c(self._lib.sph_set_rect_limits(self.h, w, h, d))

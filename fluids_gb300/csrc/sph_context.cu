@@ -943,6 +943,18 @@ int sph_set_stream(sph_ctx* x, void* stream) {
     return SPH_OK;
 }
 
+int sph_set_block_size(sph_ctx* x, int block_size) {
+    if (check_ctx(x)) return SPH_E_INVALID;
+    if (block_size % 32 != 0 || block_size < 32 || block_size > 256)
+        return fail(x, SPH_E_INVALID, "block_size must be a multiple of 32 from 32 to 256");
+    cudaStreamSynchronize(x->stream);
+    x->p.block_size = block_size;
+    x->bs = block_size;
+    x->coop_blocks = sph::pci_loop_blocks(x->num_sms, x->bs);
+    drop_graph(x);
+    return SPH_OK;
+}
+
 int sph_reset(sph_ctx* x, const sph_params* params) {
     if (check_ctx(x) || !params) return SPH_E_INVALID;
     if (params->block_size % 32 != 0 || params->block_size > 256 || params->block_size < 0)

@@ -238,6 +238,12 @@ int sph_batch_scene_grid(const sph_ctx* ctx, int scene, float* origin3, int* dim
 /* sph_stats for every scene: out8[8 * scene + k]; synchronises. */
 int sph_batch_stats(sph_ctx* ctx, double* out8, int nscenes);
 
+/* Threads per block of the step's kernels (a multiple of 32 from 32 to 256), keeping the
+ * particle state; the captured step graph is rebuilt on the next sph_simulate.  The launch
+ * shape never changes results.  Used by the autotuner (fluids_gb300/autotune.py); the
+ * reference fixes its local sizes in the host code (e.g. grid.cpp:53 runs with 32). */
+int sph_set_block_size(sph_ctx* ctx, int block_size);
+
 /* ---- differentiable WCSPH (adjoint) ----------------------------------------------------
  * No counterpart in the reference, which has no gradients.  The forward step is the WCSPH
  * step of WCSPHSimulation::simulate (wcsphsimluation.cpp:40-106) in PHYSICS mode; the
