@@ -237,6 +237,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.f_other = cv.take<float4>(n); b.f_press = cv.take<float4>(n);
     b.density = cv.take<float>(n); b.pressure = cv.take<float>(n); b.dens_var = cv.take<float>(n);
     b.aux = cv.take<float4>(n);
+    b.nrec = cv.take<float4>(2 * n);
     b.keys = cv.take<uint32_t>(n); b.keys_alt = cv.take<uint32_t>(n);
     b.mask = cv.take<int32_t>(n); b.mask_alt = cv.take<int32_t>(n);
     b.ids = cv.take<int32_t>(n); b.ids_s = cv.take<int32_t>(n);
@@ -413,15 +414,16 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
             sph::launch_wc_density(s, c, b, false, bs);
             mark(x, "k_wc_density");
         }
+        const bool pack = lists && c.sigma != 0.f;
         if (c.sigma != 0.f) {
-            sph::launch_normals(s, c, b, lists, bs);
+            sph::launch_normals(s, c, b, lists, bs, pack);
             mark(x, "k_normals");
         }
         if (x->any_massive) {
             sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
             mark(x, "k_bnd_forces");
         }
-        sph::launch_wc_forces(s, c, b, lists, true, false, bs);
+        sph::launch_wc_forces(s, c, b, lists, true, false, bs, pack);
         mark(x, "k_wc_forces");
     } else {
         sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,

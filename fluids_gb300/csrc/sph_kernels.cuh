@@ -17,6 +17,7 @@ struct Bufs {
     float4 *normal, *accel, *pos_pred, *f_other, *f_press;
     float *density, *pressure, *dens_var;
     float4* aux;                           /* per particle (p/rho^2, 1/rho, rho, p) */
+    float4* nrec;                          /* 2 per particle: (v, p/rho^2), (normal, 1/rho) for the force pass */
     uint32_t *keys, *keys_alt;
     int32_t *mask, *mask_alt;
     uint32_t* keys_sorted;                 /* where the sort left the keys */
@@ -78,9 +79,11 @@ void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, cons
 
 /* sph_wcsph.cu */
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);
-void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);
+/* pack: also write nrec (the force pass then reads 2 adjacent float4 per neighbour instead of
+ * velocity, aux and normal); only the fused step uses it */
+void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs, bool pack = false);
 void launch_wc_forces(cudaStream_t s, const Const& c, const Bufs& b, bool lists, bool fuse_integrate,
-                      bool write_acc, int bs);
+                      bool write_acc, int bs, bool pack = false);
 void launch_wc_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs);
 void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs);
 void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs);

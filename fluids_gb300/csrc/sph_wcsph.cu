@@ -144,7 +144,9 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
 template <bool LIST, bool EXACT, bool BATCH>
 __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl, const float4* __restrict__ aux,
                                                  float4* __restrict__ normal, const SceneDev* __restrict__ scenes,
-                                                 const int32_t* __restrict__ scene_of) {
+                                                 const int32_t* __restrict__ scene_of,
+                                                 const float4* __restrict__ vel_s = nullptr,
+                                                 float4* __restrict__ nrec = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
@@ -161,7 +163,13 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
         nz += dz * k;
     });
     const float k = (c.poly6_grad * c.mass_def) * H;
-    normal[i] = make_float4(nx * k, ny * k, nz * k, 0.f);
+    const float4 nv = make_float4(nx * k, ny * k, nz * k, 0.f);
+    normal[i] = nv;
+    if (nrec != nullptr) {
+        const float4 v = __ldg(&vel_s[i]), a = __ldg(&aux[i]);
+        nrec[2 * (size_t)i] = make_float4(v.x, v.y, v.z, a.x);
+        nrec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, a.y);
+    }
 }
 
 /* predict_vel_n_pos (kernels/wcsph.cl:176-224) for one particle. */
@@ -201,7 +209,11 @@ __device__ __forceinline__ void wc_integrate_one(const Const& c, float4 p, float
 #ifndef SPH_FORCES_MIN_BLOCKS
 #define SPH_FORCES_MIN_BLOCKS 4
 #endif
-template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST, bool BATCH>
+/* PACK (fused step with lists and surface tension): each neighbour's velocity, p/rho^2,
+ * normal and 1/rho come from nrec as two adjacent float4 (one 32-byte sector) instead of
+ * three separate loads; rho_j = 1/(1/rho_j) enters only the symmetrised surface-tension
+ * factor 2 rho0 / (rho_i + rho_j) = 2 rho0 R_j / (rho_i R_j + 1). */
+template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST, bool BATCH, bool PACK = false>
 __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
@@ -235,11 +247,18 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
     fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
         const float r2 = dx * dx + dy * dy + dz * dz;
         /* loaded ahead of the guard so that the list loop can issue them early */
-        const float4 aj = __ldg(&b.aux[j]);
-        const float4 vj = __ldg(&b.vel_s[j]);
-        float4 nj = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (ST) nj = __ldg(&b.normal[j]);
-        if (di > 0.f && aj.z > 0.f && r2 > rmin2) {
+        float4 aj, vj, nj = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (PACK) {
+            vj = __ldg(&b.nrec[2 * (size_t)j]);
+            nj = __ldg(&b.nrec[2 * (size_t)j + 1]);
+            aj = make_float4(vj.w, nj.w, 1.0f, 0.f);   /* (C_j, R_j, -, -); the guard uses R_j > 0 */
+        } else {
+            aj = __ldg(&b.aux[j]);
+            vj = __ldg(&b.vel_s[j]);
+            if (ST) nj = __ldg(&b.normal[j]);
+        }
+        const bool pos_j = PACK ? aj.y > 0.f : aj.z > 0.f;
+        if (di > 0.f && pos_j && r2 > rmin2) {
             const float irn = rsqrtf(r2);
             const float rn = r2 * irn;
             const float w = h - rn;
@@ -252,7 +271,7 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
             vay += (vj.y - vi.y) * vw;
             vaz += (vj.z - vi.z) * vw;
             if (ST) {
-                const float K = __fdividef(two_rho0, di + aj.z);
+                const float K = PACK ? __fdividef(two_rho0 * aj.y, di * aj.y + 1.0f) : __fdividef(two_rho0, di + aj.z);
                 cux += (ni.x - nj.x) * K;
                 cuy += (ni.y - nj.y) * K;
                 cuz += (ni.z - nj.z) * K;
@@ -369,16 +388,17 @@ void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     k_aux<<<nblk(c.n, bs), bs, 0, s>>>(c.n, b.density, b.pressure, b.aux);
 }
 
-void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs) {
+void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs, bool pack) {
     if (c.n <= 0) return;
     const int g = nblk(c.n, bs);
+    float4* nrec = pack ? b.nrec : nullptr;
     if (lists) {
         if (c.batched)
             k_normals<true, true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes,
-                                                         b.scene_of);
+                                                         b.scene_of, b.vel_s, nrec);
         else
             k_normals<true, true, false><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes,
-                                                          b.scene_of);
+                                                          b.scene_of, b.vel_s, nrec);
     } else if (c.compat) {
         k_normals<false, true, false><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.normal, b.scenes,
                                                        b.scene_of);
@@ -392,11 +412,18 @@ void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, i
 }
 
 template <bool COMPAT, bool LIST, bool BATCH>
-static void forces_launch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs) {
+static void forces_launch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs,
+                          bool pack) {
     const int g = nblk(c.n, bs);
     const bool st = c.sigma != 0.f;
     auto fs = fluid_src<LIST, COMPAT>(b);
     auto bsrc = bnd_src<LIST, COMPAT>(b);
+    if constexpr (LIST) {
+        if (pack && st && fuse && !write_acc) {
+            k_wc_forces<COMPAT, LIST, true, false, true, BATCH, true><<<g, bs, 0, s>>>(c, fs, bsrc, b);
+            return;
+        }
+    }
 #define SPH_WCF(F, W, S) k_wc_forces<COMPAT, LIST, F, W, S, BATCH><<<g, bs, 0, s>>>(c, fs, bsrc, b)
     if (fuse) {
         if (write_acc) { if (st) SPH_WCF(true, true, true); else SPH_WCF(true, true, false); }
@@ -408,22 +435,23 @@ static void forces_launch(cudaStream_t s, const Const& c, const Bufs& b, bool fu
 }
 
 template <bool COMPAT, bool LIST>
-static void forces_dispatch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs) {
+static void forces_dispatch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs,
+                            bool pack) {
     if constexpr (!COMPAT) {
-        if (c.batched) { forces_launch<false, LIST, true>(s, c, b, fuse, write_acc, bs); return; }
+        if (c.batched) { forces_launch<false, LIST, true>(s, c, b, fuse, write_acc, bs, pack); return; }
     }
-    forces_launch<COMPAT, LIST, false>(s, c, b, fuse, write_acc, bs);
+    forces_launch<COMPAT, LIST, false>(s, c, b, fuse, write_acc, bs, pack);
 }
 
 void launch_wc_forces(cudaStream_t s, const Const& c, const Bufs& b, bool lists, bool fuse_integrate,
-                      bool write_acc, int bs) {
+                      bool write_acc, int bs, bool pack) {
     if (c.n <= 0) return;
     if (c.compat) {
-        if (lists) forces_dispatch<true, true>(s, c, b, fuse_integrate, write_acc, bs);
-        else forces_dispatch<true, false>(s, c, b, fuse_integrate, write_acc, bs);
+        if (lists) forces_dispatch<true, true>(s, c, b, fuse_integrate, write_acc, bs, pack);
+        else forces_dispatch<true, false>(s, c, b, fuse_integrate, write_acc, bs, pack);
     } else {
-        if (lists) forces_dispatch<false, true>(s, c, b, fuse_integrate, write_acc, bs);
-        else forces_dispatch<false, false>(s, c, b, fuse_integrate, write_acc, bs);
+        if (lists) forces_dispatch<false, true>(s, c, b, fuse_integrate, write_acc, bs, pack);
+        else forces_dispatch<false, false>(s, c, b, fuse_integrate, write_acc, bs, pack);
     }
 }
 
