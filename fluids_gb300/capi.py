@@ -42,7 +42,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc", "sph_batch_create",
            "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid",
            "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
-           "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size"]
+           "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size", "sph_get_field_async",
+           "sph_set_field_async"]
 
 
 class SphParams(C.Structure):
@@ -144,6 +145,8 @@ def lib():
             "sph_adj_flags": (ip, [vp, C.POINTER(C.c_uint)]),
             "sph_adj_tape_bytes": (ip, [vp, C.POINTER(C.c_size_t)]),
             "sph_set_block_size": (ip, [vp, ip]),
+            "sph_get_field_async": (ip, [vp, ip, vp, C.c_size_t]),
+            "sph_set_field_async": (ip, [vp, ip, vp, C.c_size_t]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

@@ -1140,6 +1140,28 @@ int sph_get_field(sph_ctx* x, int field, void* host, size_t bytes) {
     return SPH_OK;
 }
 
+int sph_get_field_async(sph_ctx* x, int field, void* host, size_t bytes) {
+    if (check_ctx(x) || !host) return SPH_E_INVALID;
+    if (field < 0 || field >= SPH_F_COUNT) return fail(x, SPH_E_INVALID, "unknown field id");
+    long long n;
+    void* p = field_ptr(x, field, n);
+    if (!p || n < 0) return fail(x, SPH_E_STATE, "field not allocated");
+    if (bytes != (size_t)n * 4) return fail(x, SPH_E_INVALID, "byte count does not match the field size");
+    if (n > 0) SPH_CUDA(x, cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, x->stream));
+    return SPH_OK;
+}
+
+int sph_set_field_async(sph_ctx* x, int field, const void* host, size_t bytes) {
+    if (check_ctx(x) || !host) return SPH_E_INVALID;
+    if (field < 0 || field >= SPH_F_COUNT) return fail(x, SPH_E_INVALID, "unknown field id");
+    long long n;
+    void* p = field_ptr(x, field, n);
+    if (!p || n < 0) return fail(x, SPH_E_STATE, "field not allocated");
+    if (bytes != (size_t)n * 4) return fail(x, SPH_E_INVALID, "byte count does not match the field size");
+    if (n > 0) SPH_CUDA(x, cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, x->stream));
+    return SPH_OK;
+}
+
 int sph_set_field(sph_ctx* x, int field, const void* host, size_t bytes) {
     if (check_ctx(x) || !host) return SPH_E_INVALID;
     if (field < 0 || field >= SPH_F_COUNT) return fail(x, SPH_E_INVALID, "unknown field id");

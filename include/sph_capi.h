@@ -198,6 +198,12 @@ int sph_field_kind(int field);
 /* Copies a field to / from host memory (bytes must equal elems * 4); synchronises. */
 int sph_get_field(sph_ctx* ctx, int field, void* host, size_t bytes);
 int sph_set_field(sph_ctx* ctx, int field, const void* host, size_t bytes);
+/* The same copies enqueued on the context's stream, ordered with sph_simulate and returning
+ * at once: the host memory must stay valid until sph_synchronize (pinned memory makes the
+ * copy asynchronous; pageable memory is copied synchronously by the driver).  For a host
+ * program that uploads and reads back state every frame without a host wait per array. */
+int sph_get_field_async(sph_ctx* ctx, int field, void* host, size_t bytes);
+int sph_set_field_async(sph_ctx* ctx, int field, const void* host, size_t bytes);
 /* Device address of a field (replaces the cl_mem / GL VBO buffers of clallocator.h). */
 int sph_field_device_ptr(sph_ctx* ctx, int field, void** dptr);
 /* Sum of fluid force / torque per body (boundaryhandler.cpp:338-346), float[4*bodies]. */
