@@ -43,7 +43,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid",
            "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
            "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size", "sph_get_field_async",
-           "sph_set_field_async"]
+           "sph_set_field_async",
+           "sph_set_body_dynamics", "sph_get_body_state"]
 
 
 class SphParams(C.Structure):
@@ -147,6 +148,8 @@ def lib():
             "sph_set_block_size": (ip, [vp, ip]),
             "sph_get_field_async": (ip, [vp, ip, vp, C.c_size_t]),
             "sph_set_field_async": (ip, [vp, ip, vp, C.c_size_t]),
+            "sph_set_body_dynamics": (ip, [vp, ip, ip, fp, C.c_float]),
+            "sph_get_body_state": (ip, [vp, ip, fp, fp, fp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -320,6 +323,18 @@ class Context:
         p = C.c_void_p()
         self._c(self._lib.sph_field_device_ptr(self.h, fid, C.byref(p)))
         return int(p.value or 0)
+
+    def set_body_dynamics(self, body, enabled=True, inv_inertia=(0.0, 0.0, 0.0), radius=0.0):
+        ii = np.ascontiguousarray(inv_inertia, dtype=np.float32)
+        self._c(self._lib.sph_set_body_dynamics(self.h, int(body), int(bool(enabled)), ptr(ii), float(radius)))
+
+    def body_state(self, body):
+        """(rot3x4 (3, 4), linear velocity (3,), angular velocity (3,))"""
+        rot = np.zeros(12, np.float32)
+        lin = np.zeros(4, np.float32)
+        ang = np.zeros(4, np.float32)
+        self._c(self._lib.sph_get_body_state(self.h, int(body), ptr(rot), ptr(lin), ptr(ang)))
+        return rot.reshape(3, 4), lin[:3], ang[:3]
 
     def body_forces(self, nbodies):
         f = np.zeros((nbodies, 4), np.float32)

@@ -283,6 +283,81 @@ void launch_bnd_near(cudaStream_t s, const Const& c, const Bufs& b, int nb, int 
     k_bnd_near<<<nblk(nb, bs), bs, 0, s>>>(c, nb, b.bpos_s, b.bnear, b.scenes, b.scene_of ? b.bbody_s : nullptr);
 }
 
+/* One step of a dynamic body (semi-implicit Euler, the default of the reference's rigid-body
+ * engine without collisions): v += dt (F / m + g), x += dt v; w += dt R I^-1 R^T tau; the
+ * orientation turns by |w| dt about w (Rodrigues) and is re-orthonormalised; with a radius
+ * r > 0 the centre is kept r inside the container (the velocity into the wall is dropped).
+ * The force and torque are the fluid's (k_bnd_forces, boundaryhandler.cpp:296-349). */
+__device__ __forceinline__ void body_step(float* t, const float* d, float4 F, float4 T, float g, float dt,
+                                          float lx, float ly, float lz) {
+    const float m = d[1];
+    const float ax = F.x / m, ay = F.y / m + g, az = F.z / m;
+    t[12] = t[12] + dt * ax;
+    t[13] = t[13] + dt * ay;
+    t[14] = t[14] + dt * az;
+    t[3] = t[3] + dt * t[12];
+    t[7] = t[7] + dt * t[13];
+    t[11] = t[11] + dt * t[14];
+    float r[9] = {t[0], t[1], t[2], t[4], t[5], t[6], t[8], t[9], t[10]};
+    float y[3];
+    for (int k = 0; k < 3; ++k) y[k] = (r[k] * T.x + r[3 + k] * T.y + r[6 + k] * T.z) * d[2 + k];
+    for (int i = 0; i < 3; ++i) t[16 + i] = t[16 + i] + dt * (r[3 * i] * y[0] + r[3 * i + 1] * y[1] + r[3 * i + 2] * y[2]);
+    const float wx = t[16], wy = t[17], wz = t[18];
+    const float wn = sqrtf(wx * wx + wy * wy + wz * wz);
+    const float th = wn * dt;
+    if (th > 0.f) {
+        const float kx = wx / wn, ky = wy / wn, kz = wz / wn;
+        const float cs = cosf(th), sn = sinf(th), C = 1.0f - cs;
+        const float q[9] = {cs + kx * kx * C, kx * ky * C - kz * sn, kx * kz * C + ky * sn,
+                            ky * kx * C + kz * sn, cs + ky * ky * C, ky * kz * C - kx * sn,
+                            kz * kx * C - ky * sn, kz * ky * C + kx * sn, cs + kz * kz * C};
+        float n[9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) n[3 * i + j] = q[3 * i] * r[j] + q[3 * i + 1] * r[3 + j] + q[3 * i + 2] * r[6 + j];
+        const float l0 = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int j = 0; j < 3; ++j) n[j] /= l0;
+        const float p = n[3] * n[0] + n[4] * n[1] + n[5] * n[2];
+        for (int j = 0; j < 3; ++j) n[3 + j] -= p * n[j];
+        const float l1 = sqrtf(n[3] * n[3] + n[4] * n[4] + n[5] * n[5]);
+        for (int j = 0; j < 3; ++j) n[3 + j] /= l1;
+        n[6] = n[1] * n[5] - n[2] * n[4];
+        n[7] = n[2] * n[3] - n[0] * n[5];
+        n[8] = n[0] * n[4] - n[1] * n[3];
+        t[0] = n[0]; t[1] = n[1]; t[2] = n[2];
+        t[4] = n[3]; t[5] = n[4]; t[6] = n[5];
+        t[8] = n[6]; t[9] = n[7]; t[10] = n[8];
+    }
+    const float rad = d[5];
+    if (rad > 0.f) {
+        const float lo[3] = {-lx / 2.0f + rad, -ly / 2.0f + rad, -lz / 2.0f + rad};
+        const float hi[3] = {lx / 2.0f - rad, 10.0f - rad, lz / 2.0f - rad};
+        const int ci[3] = {3, 7, 11};
+        for (int a = 0; a < 3; ++a) {
+            if (t[ci[a]] < lo[a]) {
+                t[ci[a]] = lo[a];
+                if (t[12 + a] < 0.f) t[12 + a] = 0.f;
+            } else if (t[ci[a]] > hi[a]) {
+                t[ci[a]] = hi[a];
+                if (t[12 + a] > 0.f) t[12 + a] = 0.f;
+            }
+        }
+    }
+}
+
+__global__ void k_body_integrate(Const c, int nbodies, float* __restrict__ xf, const float* __restrict__ dyn,
+                                 const float4* __restrict__ force, const float4* __restrict__ torque) {
+    for (int k = threadIdx.x; k < nbodies; k += blockDim.x) {
+        const float* d = dyn + 8 * k;
+        if (d[0] == 0.f) continue;
+        body_step(xf + 20 * k, d, force[k], torque[k], c.g, c.dt, c.lim_x, c.lim_y, c.lim_z);
+    }
+}
+
+void launch_body_integrate(cudaStream_t s, const Const& c, const Bufs& b, int nbodies) {
+    if (nbodies <= 0) return;
+    k_body_integrate<<<1, 32, 0, s>>>(c, nbodies, b.body_xf, b.body_dyn, b.body_force, b.body_torque);
+}
+
 void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs) {
     if (c.nb <= 0 || nbodies <= 0) return;
     cudaMemsetAsync(b.body_force, 0, sizeof(float4) * nbodies, s);

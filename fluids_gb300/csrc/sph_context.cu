@@ -259,6 +259,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.body_xf = cv.take<float>(20 * nbod);
     b.body_range = cv.take<int32_t>(4 * nbod);
     b.body_force = cv.take<float4>(nbod); b.body_torque = cv.take<float4>(nbod);
+    b.body_dyn = cv.take<float>(8 * nbod);
     b.flags = cv.take<unsigned>(4);
     b.pci_iters = cv.take<int32_t>(4);
     b.pci_maxerr = cv.take<float>((size_t)x->max_iter_slots);
@@ -369,6 +370,7 @@ int run_stage_impl(sph_ctx* x, int stage) {
         break;
     case SPH_S_BOUNDARY_FORCES:
         if (x->any_massive) sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
+        if (x->any_dynamic) sph::launch_body_integrate(s, c, b, (int)x->bodies.size());
         break;
     default:
         return fail(x, SPH_E_INVALID, "unknown stage id");
@@ -421,6 +423,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
         }
         if (x->any_massive) {
             sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
+            if (x->any_dynamic) sph::launch_body_integrate(s, c, b, (int)x->bodies.size());
             mark(x, "k_bnd_forces");
         }
         sph::launch_wc_forces(s, c, b, lists, true, false, bs, pack);
@@ -444,6 +447,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
             if (e != cudaSuccess) return cuda_fail(x, e, "cooperative launch of the PCISPH loop");
             mark(x, "k_pci_loop");
             sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
+            if (x->any_dynamic) sph::launch_body_integrate(s, c, b, (int)x->bodies.size());
             mark(x, "k_bnd_forces");
             sph::launch_pci_integrate(s, c, b, bs);
             mark(x, "k_pci_integrate");
@@ -507,6 +511,13 @@ int rebuild(sph_ctx* x, bool keep) {
         SPH_CUDA(x, cudaMemcpy(kid.data(), x->b.ids, kid.size() * 4, cudaMemcpyDeviceToHost));
     } else {
         keep = false;
+    }
+    if (x->any_dynamic && x->b.body_xf) {
+        /* dynamic bodies moved on the device: keep their current pose and velocities */
+        SPH_CUDA(x, cudaStreamSynchronize(x->stream));
+        for (size_t k = 0; k < x->bodies.size(); ++k)
+            SPH_CUDA(x, cudaMemcpy(x->bodies[k].xf, x->b.body_xf + 20 * k, sizeof x->bodies[k].xf,
+                                   cudaMemcpyDeviceToHost));
     }
     free_arena(x);
     x->N = (int)(x->vol_pos.size() / 4);
@@ -588,9 +599,10 @@ int rebuild(sph_ctx* x, bool keep) {
     /* boundary: raw particles, body table, transform all bodies (sync(true)), sort, Psi */
     x->any_movable = false;
     x->any_massive = false;
+    x->any_dynamic = false;
     if (x->NB > 0) {
         std::vector<int32_t> body(x->NB), range(4 * x->bodies.size());
-        std::vector<float> xf(20 * x->bodies.size());
+        std::vector<float> xf(20 * x->bodies.size()), dyn(8 * x->bodies.size(), 0.f);
         std::vector<float> raw(x->braw_host);
         for (size_t k = 0; k < x->bodies.size(); ++k) {
             const SphBody& bd = x->bodies[k];
@@ -603,7 +615,13 @@ int rebuild(sph_ctx* x, bool keep) {
             std::memcpy(&xf[20 * k], bd.xf, sizeof bd.xf);
             x->any_movable |= bd.can_move != 0;
             x->any_massive |= bd.mass > 0.f;
+            dyn[8 * k] = bd.dynamic ? 1.f : 0.f;
+            dyn[8 * k + 1] = bd.mass;
+            for (int a = 0; a < 3; ++a) dyn[8 * k + 2 + a] = bd.inv_inertia[a];
+            dyn[8 * k + 5] = bd.radius;
+            x->any_dynamic |= bd.dynamic != 0;
         }
+        SPH_CUDA(x, cudaMemcpyAsync(b.body_dyn, dyn.data(), 4 * dyn.size(), cudaMemcpyHostToDevice, s));
         SPH_CUDA(x, cudaMemcpyAsync(b.braw, raw.data(), 16 * (size_t)x->NB, cudaMemcpyHostToDevice, s));
         SPH_CUDA(x, cudaMemcpyAsync(b.bbody, body.data(), 4 * (size_t)x->NB, cudaMemcpyHostToDevice, s));
         SPH_CUDA(x, cudaMemcpyAsync(b.body_range, range.data(), 4 * range.size(), cudaMemcpyHostToDevice, s));
@@ -1023,6 +1041,50 @@ int sph_set_body_transform(sph_ctx* x, int body, const float* rot3x4, const floa
     }
     if (x->b.body_xf)
         SPH_CUDA(x, cudaMemcpyAsync(x->b.body_xf + 20 * body, bd.xf, sizeof bd.xf, cudaMemcpyHostToDevice, x->stream));
+    return SPH_OK;
+}
+
+int sph_set_body_dynamics(sph_ctx* x, int body, int enabled, const float* inv_inertia3, float radius) {
+    if (check_ctx(x)) return SPH_E_INVALID;
+    if (!x->scene_in.empty()) return fail(x, SPH_E_STATE, "a batched context has static boundaries only");
+    if (body < 0 || body >= (int)x->bodies.size()) return fail(x, SPH_E_INVALID, "bad body index");
+    SphBody& bd = x->bodies[body];
+    if (enabled && (!bd.can_move || !(bd.mass > 0.f)))
+        return fail(x, SPH_E_INVALID, "a dynamic body must be movable and have a mass > 0");
+    if (enabled && (!inv_inertia3 || !(inv_inertia3[0] >= 0.f) || !(inv_inertia3[1] >= 0.f) ||
+                    !(inv_inertia3[2] >= 0.f) || !(radius >= 0.f)))
+        return fail(x, SPH_E_INVALID, "inverse inertia and radius must be >= 0");
+    if (x->any_dynamic && x->b.body_xf) {
+        SPH_CUDA(x, cudaStreamSynchronize(x->stream));
+        SPH_CUDA(x, cudaMemcpy(bd.xf, x->b.body_xf + 20 * body, sizeof bd.xf, cudaMemcpyDeviceToHost));
+    }
+    bd.dynamic = enabled ? 1 : 0;
+    for (int a = 0; a < 3; ++a) bd.inv_inertia[a] = enabled ? inv_inertia3[a] : 0.f;
+    bd.radius = enabled ? radius : 0.f;
+    x->any_dynamic = false;
+    for (const SphBody& o : x->bodies) x->any_dynamic |= o.dynamic != 0;
+    if (x->b.body_dyn) {
+        const float d[8] = {bd.dynamic ? 1.f : 0.f, bd.mass, bd.inv_inertia[0], bd.inv_inertia[1], bd.inv_inertia[2],
+                            bd.radius, 0.f, 0.f};
+        SPH_CUDA(x, cudaMemcpyAsync(x->b.body_dyn + 8 * body, d, sizeof d, cudaMemcpyHostToDevice, x->stream));
+        SPH_CUDA(x, cudaStreamSynchronize(x->stream));
+    }
+    drop_graph(x);
+    return SPH_OK;
+}
+
+int sph_get_body_state(sph_ctx* x, int body, float* rot3x4, float* lin4, float* ang4) {
+    if (check_ctx(x)) return SPH_E_INVALID;
+    if (body < 0 || body >= (int)x->bodies.size()) return fail(x, SPH_E_INVALID, "bad body index");
+    float xf[20];
+    std::memcpy(xf, x->bodies[body].xf, sizeof xf);
+    if (x->b.body_xf) {
+        SPH_CUDA(x, cudaStreamSynchronize(x->stream));
+        SPH_CUDA(x, cudaMemcpy(xf, x->b.body_xf + 20 * body, sizeof xf, cudaMemcpyDeviceToHost));
+    }
+    if (rot3x4) std::memcpy(rot3x4, xf, 12 * sizeof(float));
+    if (lin4) std::memcpy(lin4, xf + 12, 4 * sizeof(float));
+    if (ang4) std::memcpy(ang4, xf + 16, 4 * sizeof(float));
     return SPH_OK;
 }
 

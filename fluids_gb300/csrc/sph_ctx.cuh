@@ -16,6 +16,10 @@ struct SphBody {
     int origin = 0, count = 0, can_move = 0;
     float mass = 0.f;
     float xf[20];   /* rot3x4 (row-major), lin4, ang4 */
+    /* rigid-body dynamics (sph_set_body_dynamics): integrated on the device every step */
+    int dynamic = 0;
+    float inv_inertia[3] = {0.f, 0.f, 0.f};
+    float radius = 0.f;
 };
 
 struct sph_ctx {
@@ -32,7 +36,7 @@ struct sph_ctx {
     std::vector<float> braw_host;
     std::vector<SphBody> bodies;
     int N = 0, NB = 0;
-    bool any_movable = false, any_massive = false;
+    bool any_movable = false, any_massive = false, any_dynamic = false;
     char* arena = nullptr;
     size_t arena_bytes = 0;
     int max_iter_slots = 1;

@@ -43,6 +43,7 @@ struct Bufs {
     float* body_xf;                        /* 20 floats per body: rot3x4, lin4, ang4 */
     int32_t* body_range;                   /* origin, count, can_move, has_mass per body */
     float4 *body_force, *body_torque;
+    float* body_dyn;                       /* 8 floats per body: dynamic, mass, inv inertia xyz, radius */
     /* batched contexts: scene table and the scene of each fluid particle (ranges never move) */
     const SceneDev* scenes;
     const int32_t* scene_of;
@@ -105,6 +106,8 @@ void launch_bnd_phi(cudaStream_t s, const Const& c, const Bufs& b, float phi_coe
 /* marks bnear for the 27 cells around every sorted boundary particle (after clearing it) */
 void launch_bnd_near(cudaStream_t s, const Const& c, const Bufs& b, int nb, int bs);
 void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs);
+/* advances every dynamic body by one step under the fluid force and torque and gravity */
+void launch_body_integrate(cudaStream_t s, const Const& c, const Bufs& b, int nbodies);
 void launch_stats(cudaStream_t s, const Const& c, const Bufs& b);
 void launch_scene_stats(cudaStream_t s, const Const& c, const Bufs& b, double* out, int nscenes);
 

@@ -166,6 +166,18 @@ int sph_add_boundary(sph_ctx* ctx, const float* pos4, int n, int can_move, const
  * boundaryhandler.cpp:259-274). */
 int sph_set_body_transform(sph_ctx* ctx, int body, const float* rot3x4, const float* lin4,
                            const float* ang4);
+/* Two-way coupling without a physics engine: the reference hands the fluid's force and
+ * torque on each body to Bullet (boundaryhandler.cpp:296-349, scene.cpp:471 makes bodies with
+ * mass dynamic).  With enabled != 0 the context itself advances the body every step on the
+ * device (semi-implicit Euler under fluid force, fluid torque and gravity; orientation by
+ * the angular velocity), so the body moves inside the captured step.  inv_inertia3: inverse
+ * principal moments in body coordinates (a solid cube of side s: 6 / (m s^2)); radius > 0
+ * keeps the body's centre that far inside the container.  Bodies do not collide with each
+ * other.  The body must be movable (can_move) with mass > 0. */
+int sph_set_body_dynamics(sph_ctx* ctx, int body, int enabled, const float* inv_inertia3, float radius);
+/* Current transform and velocities of a body (the pose RigidBody reports for rendering);
+ * synchronises. */
+int sph_get_body_state(sph_ctx* ctx, int body, float* rot3x4, float* lin4, float* ang4);
 /* FluidSimulation::particle_count / boundary_particle_count (fluidsimulation.h:54,84). */
 int sph_particle_count(const sph_ctx* ctx);
 int sph_boundary_particle_count(const sph_ctx* ctx);

@@ -110,6 +110,8 @@ def _load():
         lib.orc_morton3.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
         lib.orc_stable_sort_pairs.argtypes = [vp, vp, ip]
         lib.orc_stats.argtypes = [vp, C.POINTER(C.c_double)]
+        lib.orc_set_body_dynamics.argtypes = [vp, ip, ip, fp, C.c_float]
+        lib.orc_body_state.argtypes = [vp, ip, fp, fp, fp]
         _lib = lib
         return lib
 
@@ -203,6 +205,19 @@ class Oracle:
         d = OrcDerived()
         self._lib.orc_derived(self._h, C.byref(d))
         return d.as_dict()
+
+    def set_body_dynamics(self, body, enabled=True, inv_inertia=(0.0, 0.0, 0.0), radius=0.0):
+        ii = np.ascontiguousarray(inv_inertia, dtype=np.float32)
+        rc = self._lib.orc_set_body_dynamics(self._h, int(body), int(bool(enabled)), _fptr(ii), float(radius))
+        if rc != 0:
+            raise ValueError("body %d cannot be dynamic (needs can_move and mass > 0)" % body)
+
+    def body_state(self, body):
+        rot = np.zeros(12, np.float32)
+        lin = np.zeros(4, np.float32)
+        ang = np.zeros(4, np.float32)
+        self._lib.orc_body_state(self._h, int(body), _fptr(rot), _fptr(lin), _fptr(ang))
+        return rot.reshape(3, 4), lin[:3], ang[:3]
 
     def stats(self):
         out = (C.c_double * 8)()

@@ -146,6 +146,9 @@ struct Body {
     float rot[12];
     float lin[4], ang[4];
     float mass = 0;
+    int dynamic = 0;
+    float inv_inertia[3] = {0, 0, 0};
+    float radius = 0;
 };
 
 struct OracleBase {
@@ -161,6 +164,8 @@ struct OracleBase {
     virtual int set(int f, const void* in) = 0;
     virtual void derived(OrcDerived* d) = 0;
     virtual void stats(double* out) = 0;
+    virtual int set_body_dynamics(int body, int enabled, const float* inv_inertia, float radius) = 0;
+    virtual int body_state(int body, float* rot, float* lin, float* ang) = 0;
 };
 
 /* Stable LSD radix sort of (uint key, int value) pairs, 8-bit digits, all 32 key bits.
@@ -809,6 +814,83 @@ struct Oracle : OracleBase {
         }
     }
 
+    /* Rigid-body step of every dynamic body (the GPU's k_body_integrate, same float
+     * operations in the same order): semi-implicit Euler under the fluid force and torque
+     * and gravity, orientation turned by |w| dt about w (Rodrigues), re-orthonormalised,
+     * centre kept radius inside the container. */
+    void integrate_bodies() {
+        const float dt = cfg.time_step, g = -cfg.gravity;
+        const float lx = cfg.container[0], ly = cfg.container[1], lz = cfg.container[2];
+        for (size_t k = 0; k < bodies.size(); ++k) {
+            Body& b = bodies[k];
+            if (!b.dynamic) continue;
+            float F[3], T[3];
+            for (int a = 0; a < 3; ++a) { F[a] = float(body_force[4 * k + a]); T[a] = float(body_torque[4 * k + a]); }
+            float* t = b.rot;     /* rot3x4 with the centre in t[3], t[7], t[11] */
+            float* v = b.lin;
+            float* w = b.ang;
+            const float m = b.mass;
+            const float ax = F[0] / m, ay = F[1] / m + g, az = F[2] / m;
+            v[0] = v[0] + dt * ax; v[1] = v[1] + dt * ay; v[2] = v[2] + dt * az;
+            t[3] = t[3] + dt * v[0]; t[7] = t[7] + dt * v[1]; t[11] = t[11] + dt * v[2];
+            float r[9] = {t[0], t[1], t[2], t[4], t[5], t[6], t[8], t[9], t[10]};
+            float y[3];
+            for (int q = 0; q < 3; ++q) y[q] = (r[q] * T[0] + r[3 + q] * T[1] + r[6 + q] * T[2]) * b.inv_inertia[q];
+            for (int i = 0; i < 3; ++i) w[i] = w[i] + dt * (r[3 * i] * y[0] + r[3 * i + 1] * y[1] + r[3 * i + 2] * y[2]);
+            const float wn = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            const float th = wn * dt;
+            if (th > 0.f) {
+                const float kx = w[0] / wn, ky = w[1] / wn, kz = w[2] / wn;
+                const float cs = std::cos(th), sn = std::sin(th), C = 1.0f - cs;
+                const float q[9] = {cs + kx * kx * C, kx * ky * C - kz * sn, kx * kz * C + ky * sn,
+                                    ky * kx * C + kz * sn, cs + ky * ky * C, ky * kz * C - kx * sn,
+                                    kz * kx * C - ky * sn, kz * ky * C + kx * sn, cs + kz * kz * C};
+                float n[9];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) n[3 * i + j] = q[3 * i] * r[j] + q[3 * i + 1] * r[3 + j] + q[3 * i + 2] * r[6 + j];
+                const float l0 = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+                for (int j = 0; j < 3; ++j) n[j] /= l0;
+                const float p = n[3] * n[0] + n[4] * n[1] + n[5] * n[2];
+                for (int j = 0; j < 3; ++j) n[3 + j] -= p * n[j];
+                const float l1 = std::sqrt(n[3] * n[3] + n[4] * n[4] + n[5] * n[5]);
+                for (int j = 0; j < 3; ++j) n[3 + j] /= l1;
+                n[6] = n[1] * n[5] - n[2] * n[4];
+                n[7] = n[2] * n[3] - n[0] * n[5];
+                n[8] = n[0] * n[4] - n[1] * n[3];
+                t[0] = n[0]; t[1] = n[1]; t[2] = n[2];
+                t[4] = n[3]; t[5] = n[4]; t[6] = n[5];
+                t[8] = n[6]; t[9] = n[7]; t[10] = n[8];
+            }
+            if (b.radius > 0.f) {
+                const float rad = b.radius;
+                const float lo[3] = {-lx / 2.0f + rad, -ly / 2.0f + rad, -lz / 2.0f + rad};
+                const float hi[3] = {lx / 2.0f - rad, 10.0f - rad, lz / 2.0f - rad};
+                const int ci[3] = {3, 7, 11};
+                for (int a = 0; a < 3; ++a) {
+                    if (t[ci[a]] < lo[a]) { t[ci[a]] = lo[a]; if (v[a] < 0.f) v[a] = 0.f; }
+                    else if (t[ci[a]] > hi[a]) { t[ci[a]] = hi[a]; if (v[a] > 0.f) v[a] = 0.f; }
+                }
+            }
+        }
+    }
+    int set_body_dynamics(int body, int enabled, const float* ii, float radius) override {
+        if (body < 0 || body >= (int)bodies.size()) return 1;
+        Body& b = bodies[body];
+        if (enabled && (!b.can_move || !(b.mass > 0))) return 1;
+        b.dynamic = enabled ? 1 : 0;
+        for (int a = 0; a < 3; ++a) b.inv_inertia[a] = enabled && ii ? ii[a] : 0.f;
+        b.radius = enabled ? radius : 0.f;
+        return 0;
+    }
+    int body_state(int body, float* rot, float* lin, float* ang) override {
+        if (body < 0 || body >= (int)bodies.size()) return 1;
+        const Body& b = bodies[body];
+        if (rot) std::memcpy(rot, b.rot, sizeof b.rot);
+        if (lin) std::memcpy(lin, b.lin, sizeof b.lin);
+        if (ang) std::memcpy(ang, b.ang, sizeof b.ang);
+        return 0;
+    }
+
     int run_stage(int s) override {
         switch (s) {
         case ORC_S_BOUNDARY_SYNC: boundary_sync(false); break;
@@ -835,7 +917,7 @@ struct Oracle : OracleBase {
         case ORC_S_PCI_INIT_FORCES: f_press.assign(4 * (size_t)N, 0); pci_init_forces(); break;
         case ORC_S_PCI_LOOP: pci_loop(cfg.pci_min_iter, cfg.pci_max_iter); break;
         case ORC_S_PCI_INTEGRATE: pci_integrate(); break;
-        case ORC_S_BOUNDARY_FORCES: boundary_forces(); break;
+        case ORC_S_BOUNDARY_FORCES: boundary_forces(); integrate_bodies(); break;
         default: return 1;
         }
         return 0;
@@ -1023,5 +1105,11 @@ int orc_derived(void* o, OrcDerived* d) { static_cast<OracleBase*>(o)->derived(d
 uint32_t orc_morton3(uint32_t x, uint32_t y, uint32_t z) { return morton3(x, y, z); }
 void orc_stable_sort_pairs(uint32_t* k, int32_t* v, int n) { radix_sort_pairs(k, v, n); }
 int orc_stats(void* o, double* out) { static_cast<OracleBase*>(o)->stats(out); return 0; }
+int orc_set_body_dynamics(void* o, int body, int enabled, const float* inv_inertia3, float radius) {
+    return static_cast<OracleBase*>(o)->set_body_dynamics(body, enabled, inv_inertia3, radius);
+}
+int orc_body_state(void* o, int body, float* rot12, float* lin4, float* ang4) {
+    return static_cast<OracleBase*>(o)->body_state(body, rot12, lin4, ang4);
+}
 
 }  // extern "C"

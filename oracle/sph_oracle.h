@@ -99,6 +99,9 @@ void  orc_stable_sort_pairs(uint32_t* keys, int32_t* vals, int n);
  * [mean max(rho-rho0,0)/rho0, mean |rho-rho0|/rho0, max (rho-rho0)/rho0,
  *  kinetic energy, potential energy (m g y), centre of mass x, y, z]. */
 int   orc_stats(void* o, double* out8);
+/* rigid-body dynamics of a movable body with mass (integrated in the BOUNDARY_FORCES stage) */
+int   orc_set_body_dynamics(void* o, int body, int enabled, const float* inv_inertia3, float radius);
+int   orc_body_state(void* o, int body, float* rot12, float* lin4, float* ang4);
 
 #ifdef __cplusplus
 }
