@@ -7,8 +7,10 @@
  * the scene from the reference's JSON format -- "container" {width, height, depth} becomes the
  * rectangular limits, "fluid_volumes" of type "box" {size, center} become BoxVolumes, and
  * "rigid_bodies" of type "cube" {size, center, rotation (x, y, z, w quaternion), mass} become
- * boundary bodies (movable when mass > 0, as scene.cpp:471 passes them).  Sphere and mesh
- * bodies are not sampled here (reported and skipped).  Options:
+ * boundary bodies (movable when mass > 0, as scene.cpp:471 passes them, and then moved by the
+ * solver's own rigid-body step under the fluid's force and torque and gravity; bodies do not
+ * collide with each other).  Sphere and mesh bodies are not sampled here (reported and
+ * skipped).  Options:
  *
  *   sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]
  *              [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]
@@ -272,7 +274,17 @@ int main(int argc, char** argv) {
                 const std::vector<double> st = fluid->stats();
                 std::printf("{\"step\": %d", s);
                 for (int k = 0; k < 8; ++k) std::printf(", \"%s\": %.9g", names[k], st[k]);
-                std::printf(", \"flags\": %u}\n", fluid->device_flags());
+                std::printf(", \"bodies\": {");
+                bool first = true;
+                for (auto& b : sc.bodies) {
+                    if (!(b.second->mass > 0.f)) continue;
+                    float rot[12], lin[4], ang[4];
+                    fluid->body_pose(b.first, rot, lin, ang);
+                    std::printf("%s\"%s\": [%.7g, %.7g, %.7g]", first ? "" : ", ", b.first.c_str(), rot[3], rot[7],
+                                rot[11]);
+                    first = false;
+                }
+                std::printf("}, \"flags\": %u}\n", fluid->device_flags());
                 std::fflush(stdout);
             }
         }

@@ -161,6 +161,10 @@ class RigidBody {
    public:
     virtual ~RigidBody() = default;
     virtual std::vector<Float4> surface_sampling(float spacing) const = 0;
+    /* Inverse principal moments of inertia in body coordinates and the distance from the
+     * centre kept to the container walls; used when the body has mass and can move. */
+    virtual void inverse_inertia(float out[3]) const { out[0] = out[1] = out[2] = 0.f; }
+    virtual float bounding_radius() const { return 0.f; }
     float mass = 0.f;
     float rot3x4[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
     float linear_velocity[4] = {0, 0, 0, 0};
@@ -186,6 +190,12 @@ class FishTank : public RigidBody {
 class Cube : public RigidBody {
    public:
     explicit Cube(float side) : side_(side) {}
+    /* solid cube: I = m s^2 / 6 about every principal axis */
+    void inverse_inertia(float out[3]) const override {
+        const float v = mass > 0.f ? 6.0f / (mass * side_ * side_) : 0.f;
+        out[0] = out[1] = out[2] = v;
+    }
+    float bounding_radius() const override { return 0.5f * side_; }
     std::vector<Float4> surface_sampling(float spacing) const override {
         const int n = sph_scene_cube(side_, spacing, nullptr, 0);
         std::vector<Float4> out((size_t)(n > 0 ? n : 0));
@@ -265,6 +275,13 @@ class CudaFluidSimulation : public FluidSimulation {
               ctx_);
         body_ids_.push_back(boundary_id);
         bodies_.push_back(body);
+        if (can_move && body->mass > 0.f) {
+            /* the reference hands movable bodies with mass to Bullet (scene.cpp:471); here the
+             * solver integrates them itself */
+            float ii[3];
+            body->inverse_inertia(ii);
+            check(sph_set_body_dynamics(ctx_, (int)body_ids_.size() - 1, 1, ii, body->bounding_radius()), ctx_);
+        }
     }
     void set_rect_limits(float w, float h, float d) override { check(sph_set_rect_limits(ctx_, w, h, d), ctx_); }
     int boundary_particle_count() const override { return sph_boundary_particle_count(ctx_); }
@@ -285,6 +302,15 @@ class CudaFluidSimulation : public FluidSimulation {
         for (size_t b = 0; b < body_ids_.size(); ++b)
             if (body_ids_[b] == boundary_id) {
                 check(sph_set_body_transform(ctx_, (int)b, rot3x4, lin, ang), ctx_);
+                return;
+            }
+        throw Error(SPH_E_INVALID, "unknown boundary id '" + boundary_id + "'");
+    }
+    /* Current pose of a body: rot3x4 (rotation | centre), linear and angular velocity. */
+    void body_pose(const std::string& boundary_id, float rot3x4[12], float lin[4], float ang[4]) {
+        for (size_t b = 0; b < body_ids_.size(); ++b)
+            if (body_ids_[b] == boundary_id) {
+                check(sph_get_body_state(ctx_, (int)b, rot3x4, lin, ang), ctx_);
                 return;
             }
         throw Error(SPH_E_INVALID, "unknown boundary id '" + boundary_id + "'");

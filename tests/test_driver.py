@@ -100,3 +100,21 @@ def test_driver_matches_python_api(gpu_lib, driver, tmp_path):
     assert np.array_equal(got, ref)
     st = ctx.stats()
     assert lines[-2]["kinetic"] == pytest.approx(st["kinetic"], rel=1e-8)   # printed with 9 digits
+
+
+@pytest.mark.gpu
+def test_driver_moves_bodies_with_mass(gpu_lib, driver, tmp_path):
+    """A cube with mass in the scene file is dynamic: it falls under gravity (no fluid near)."""
+    scene = {"container": {"width": 0.6, "height": 0.6, "depth": 0.4},
+             "fluid_volumes": [{"type": "box", "name": "f", "size": [0.12, 0.12, 0.12], "center": [0.2, -0.2, 0.0]}],
+             "rigid_bodies": [{"type": "cube", "name": "falling", "mass": 0.4, "size": 0.1,
+                               "center": [-0.15, 0.1, 0.0], "rotation": [0, 0, 0, 1]}]}
+    c, s = write(tmp_path, scene=scene)
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--steps", "100", "--every", "50"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(x) for x in r.stdout.splitlines()]
+    y = [x["bodies"]["falling"][1] for x in lines[:-1]]
+    dt, g = np.float32(2e-4), 9.81
+    for n, yy in zip((50, 100), y):
+        assert yy == pytest.approx(0.1 - g * dt * dt * n * (n + 1) / 2, abs=1e-5)
