@@ -14,7 +14,8 @@
  *                 as the epilogue, so the acceleration never round-trips through HBM.
  * One thread per particle in Morton order: the 32 particles of a warp share most of their
  * 27 neighbour cells, so neighbour data comes from L1/L2 rather than HBM.  Inside the
- * neighbour loops 1/r comes from rsqrtf and 1/rho_j from aux (FP32 results differ from the
+ * neighbour loops 1/r comes from rsqrtf and 1/rho_j from aux or the correctly rounded
+ * reciprocal of the density (FP32 results differ from the
  * reference's IEEE divisions by a few ulp, inside the parity tolerance).
  */
 #include "sph_kernels.cuh"
@@ -143,7 +144,8 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
 
 template <bool LIST, bool EXACT, bool BATCH>
 __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl, const float4* __restrict__ aux,
-                                                 float4* __restrict__ normal, const SceneDev* __restrict__ scenes,
+                                                 const float* __restrict__ dens, float4* __restrict__ normal,
+                                                 const SceneDev* __restrict__ scenes,
                                                  const int32_t* __restrict__ scene_of,
                                                  const float4* __restrict__ vel_s = nullptr,
                                                  float4* __restrict__ nrec = nullptr) {
@@ -155,7 +157,10 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
     fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
-        const float inv_rho = __ldg(&aux[j].y);
+        /* 1/rho_j from the dense density array (8 particles per 32-byte sector instead of 2
+         * for aux; the pass is bound by L1 throughput); __frcp_rn is the correctly rounded
+         * reciprocal, the value aux holds */
+        const float inv_rho = __frcp_rn(__ldg(&dens[j]));
         const float t = HH - (dx * dx + dy * dy + dz * dz);
         const float k = (t * t) * inv_rho;
         nx += dx * k;
@@ -394,19 +399,24 @@ void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, i
     float4* nrec = pack ? b.nrec : nullptr;
     if (lists) {
         if (c.batched)
-            k_normals<true, true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes,
+            k_normals<true, true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,
+                                                      b.scenes,
                                                          b.scene_of, b.vel_s, nrec);
         else
-            k_normals<true, true, false><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.normal, b.scenes,
+            k_normals<true, true, false><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,
+                                                      b.scenes,
                                                           b.scene_of, b.vel_s, nrec);
     } else if (c.compat) {
-        k_normals<false, true, false><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.normal, b.scenes,
+        k_normals<false, true, false><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.density, b.normal,
+                                                      b.scenes,
                                                        b.scene_of);
     } else if (c.batched) {
-        k_normals<false, false, true><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal, b.scenes,
+        k_normals<false, false, true><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.density, b.normal,
+                                                      b.scenes,
                                                        b.scene_of);
     } else {
-        k_normals<false, false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.normal, b.scenes,
+        k_normals<false, false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.density, b.normal,
+                                                      b.scenes,
                                                         b.scene_of);
     }
 }
