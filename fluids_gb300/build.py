@@ -19,7 +19,10 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libsph_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["sph_sort.cu", "sph_grid.cu", "sph_wcsph.cu", "sph_pcisph.cu", "sph_boundary.cu", "sph_context.cu",
-           "sph_scene.cpp", "sph_sort_noalloc.cu", "sph_adjoint.cu"]
+           "sph_scene.cpp", "sph_sort_noalloc.cu", "sph_adjoint.cu", "sph_render.cu"]
+# The screen-space surface kernels round every multiply and add separately (no FMA
+# contraction) so their depth and normal images are reproducible operation for operation.
+SOURCE_FLAGS = {"sph_render.cu": ["-fmad=false"]}
 _lock = threading.Lock()
 
 
@@ -44,7 +47,7 @@ def _compile(src, extra):
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj
     cmd = [nvcc(), "-c", path, "-o", obj + ".tmp", "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
-           "-I", INCLUDE, "-I", CSRC] + ARCH + extra
+           "-I", INCLUDE, "-I", CSRC] + ARCH + SOURCE_FLAGS.get(src, []) + extra
     if src.endswith(".cpp"):
         cmd += ["-x", "c++"]
     r = subprocess.run(cmd, capture_output=True, text=True)

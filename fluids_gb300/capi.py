@@ -44,7 +44,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
            "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size", "sph_get_field_async",
            "sph_set_field_async",
-           "sph_set_body_dynamics", "sph_get_body_state"]
+           "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
+           "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals"]
 
 
 class SphParams(C.Structure):
@@ -80,6 +81,27 @@ class SceneDesc(C.Structure):
     _fields_ = [("container", C.c_float * 3), ("k_viscosity", C.c_float), ("gas_stiffness", C.c_float),
                 ("fluid_pos4", C.c_void_p), ("fluid_vel4", C.c_void_p), ("n_fluid", C.c_int),
                 ("boundary_pos4", C.c_void_p), ("n_boundary", C.c_int)]
+
+
+class SphView(C.Structure):
+    _fields_ = [("modelview", C.c_float * 16), ("projection", C.c_float * 16), ("point_radius", C.c_float),
+                ("point_scale", C.c_float), ("width", C.c_int), ("height", C.c_int)]
+
+
+def make_view(modelview, projection, point_radius, point_scale, width, height):
+    """sph_view from 4x4 matrices in mathematical (row, column) layout; the struct holds
+    them column-major like GL uniforms."""
+    v = SphView()
+    mv = np.asarray(modelview, np.float32).reshape(4, 4).T.reshape(-1)
+    pr = np.asarray(projection, np.float32).reshape(4, 4).T.reshape(-1)
+    for k in range(16):
+        v.modelview[k] = float(mv[k])
+        v.projection[k] = float(pr[k])
+    v.point_radius = float(point_radius)
+    v.point_scale = float(point_scale)
+    v.width = int(width)
+    v.height = int(height)
+    return v
 
 
 class SphError(RuntimeError):
@@ -150,6 +172,11 @@ def lib():
             "sph_set_field_async": (ip, [vp, ip, vp, C.c_size_t]),
             "sph_set_body_dynamics": (ip, [vp, ip, ip, fp, C.c_float]),
             "sph_get_body_state": (ip, [vp, ip, fp, fp, fp]),
+            "sph_render_depth": (ip, [vp, C.POINTER(SphView), vp]),
+            "sph_filter_bilateral": (ip, [vp, vp, ip, ip, vp]),
+            "sph_render_smooth": (ip, [vp, vp, ip, ip, ip, vp]),
+            "sph_filter_curvature_flow": (ip, [vp, vp, ip, ip, C.c_float, C.c_float, vp]),
+            "sph_render_normals": (ip, [vp, vp, ip, ip, C.POINTER(C.c_float), vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -336,6 +363,10 @@ class Context:
         self._c(self._lib.sph_get_body_state(self.h, int(body), ptr(rot), ptr(lin), ptr(ang)))
         return rot.reshape(3, 4), lin[:3], ang[:3]
 
+    def render_depth(self, view, d_depth):
+        """sph_render_depth into the device image at address d_depth (view: SphView)."""
+        self._c(self._lib.sph_render_depth(self.h, C.byref(view), C.c_void_p(int(d_depth))))
+
     def body_forces(self, nbodies):
         f = np.zeros((nbodies, 4), np.float32)
         t = np.zeros((nbodies, 4), np.float32)
@@ -485,3 +516,26 @@ def sort_pairs_device(d_keys, d_vals, n, key_bits=32, stream=None):
     """sph_sort_pairs on device addresses (ints)."""
     check(lib().sph_sort_pairs(C.c_void_p(d_keys), C.c_void_p(d_vals), int(n), int(key_bits),
                                C.c_void_p(stream or 0)))
+
+
+def filter_bilateral(d_in, d_out, width, height, stream=None):
+    """sph_filter_bilateral on device addresses (ints)."""
+    check(lib().sph_filter_bilateral(C.c_void_p(d_in), C.c_void_p(d_out), int(width), int(height),
+                                     C.c_void_p(stream or 0)))
+
+
+def render_smooth(d_depth, d_tmp, width, height, iterations, stream=None):
+    check(lib().sph_render_smooth(C.c_void_p(d_depth), C.c_void_p(d_tmp), int(width), int(height),
+                                  int(iterations), C.c_void_p(stream or 0)))
+
+
+def filter_curvature_flow(d_in, d_out, width, height, inv_proj_x, inv_proj_y, stream=None):
+    check(lib().sph_filter_curvature_flow(C.c_void_p(d_in), C.c_void_p(d_out), int(width), int(height),
+                                          float(inv_proj_x), float(inv_proj_y), C.c_void_p(stream or 0)))
+
+
+def render_normals(d_depth, d_normals4, width, height, inv_projection, stream=None):
+    """inv_projection: 4x4 in mathematical layout (passed column-major)."""
+    ip = np.ascontiguousarray(np.asarray(inv_projection, np.float32).reshape(4, 4).T.reshape(-1))
+    check(lib().sph_render_normals(C.c_void_p(d_depth), C.c_void_p(d_normals4), int(width), int(height),
+                                   ip.ctypes.data_as(C.POINTER(C.c_float)), C.c_void_p(stream or 0)))

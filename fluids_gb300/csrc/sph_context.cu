@@ -943,6 +943,7 @@ int sph_destroy(sph_ctx* x) {
     cudaSetDevice(x->device);
     if (x->stream) cudaStreamSynchronize(x->stream);
     free_arena(x);
+    cudaFree(x->render_buf);
     if (x->own_stream && x->stream) cudaStreamDestroy(x->stream);
     delete x;
     return SPH_OK;

@@ -61,6 +61,9 @@ struct sph_ctx {
     sph::SceneDev* d_scenes = nullptr;
     int32_t* d_scene_of = nullptr;
     double* d_scene_stats = nullptr;
+    /* depth-test scratch of sph_render_depth: 8 bytes per pixel */
+    void* render_buf = nullptr;
+    size_t render_pixels = 0;
 };
 
 /* Records msg as the context's last error (or the last creation error) and returns code. */

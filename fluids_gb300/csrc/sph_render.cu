@@ -1,0 +1,333 @@
+/*
+ * sph_render.cu -- the screen-space fluid surface of the reference's renderer as CUDA
+ * kernels writing device images (no graphics API): particle depth sprites, the two
+ * smoothing filters, and view-space normals.
+ *
+ *   k_splat_*        shaders/sspace_fluid_rendering/depth_stage.{vert,frag}: each particle
+ *                    is a point sprite of gl_PointSize = point_radius * point_scale / |p_eye|;
+ *                    a fragment inside the sprite's disc lies on the sphere of radius
+ *                    point_radius around the particle; its normalised depth is written where
+ *                    it is the nearest (GL_LESS on (z_ndc + 1) / 2, the lowest particle index
+ *                    winning a tie as the first primitive does), 0 elsewhere.  The fragment
+ *                    shader's depth uses `sphere_pos_eye * pr_matrix` (vector on the left:
+ *                    the transpose of the projection), kept as written.  No background
+ *                    texture: fragments beyond the far plane are dropped.
+ *   k_bilateral      kernels/bilateral.cl (window -4..3 in x and y, depth gate 0.015).
+ *   k_curvature_flow kernels/curvatureflow.cl (one explicit step of the mean-curvature flow).
+ *   k_depth_normals  shaders/sspace_fluid_rendering/normals_stage.frag: eye-space positions
+ *                    from the inverse projection, one-sided differences with the smaller
+ *                    depth jump, normal = normalize(ddx x ddy).
+ * Images are row-major, row 0 at the bottom (window coordinates), single-channel float
+ * (depth) or float4 (normals); reads outside the image clamp to the edge.
+ */
+#include <cstring>
+
+#include "sph_ctx.cuh"
+
+namespace sph {
+namespace {
+
+struct View {
+    float mv[16], pr[16];   /* column-major 4x4, as GL uniforms */
+    float radius, scale;
+    int w, h;
+};
+
+__device__ __forceinline__ void mat_vec(const float* m, const float v[4], float o[4]) {
+    for (int r = 0; r < 4; ++r) o[r] = m[r] * v[0] + m[4 + r] * v[1] + m[8 + r] * v[2] + m[12 + r] * v[3];
+}
+
+/* A particle's sprite: eye position, window centre and size; false when GL clips it. */
+__device__ __forceinline__ bool sprite(const View& v, float4 p, float e[4], float& wx, float& wy, float& size) {
+    const float x[4] = {p.x, p.y, p.z, 1.0f};
+    mat_vec(v.mv, x, e);
+    float c[4];
+    mat_vec(v.pr, e, c);
+    if (!(c[3] > 0.f) || fabsf(c[0]) > c[3] || fabsf(c[1]) > c[3] || fabsf(c[2]) > c[3]) return false;
+    const float dist = sqrtf(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+    size = fmaxf(v.radius * (v.scale / dist), 1.0f);   /* GL's smallest point size */
+    wx = (c[0] / c[3] + 1.0f) * 0.5f * (float)v.w;
+    wy = (c[1] / c[3] + 1.0f) * 0.5f * (float)v.h;
+    return size > 0.f;
+}
+
+/* Depth of the sprite fragment at pixel (px, py): false outside the disc or beyond far. */
+__device__ __forceinline__ bool fragment(const View& v, const float e[4], float wx, float wy, float size, int px,
+                                         int py, float& nd, float& lin) {
+    /* gl_PointCoord has its origin at the sprite's upper left; the shader maps it to
+       (2s - 1, 1 - 2t) and then negates y, so y grows downwards on the screen */
+    float nx = 2.0f * ((float)px + 0.5f - wx) / size;
+    float ny = -2.0f * ((float)py + 0.5f - wy) / size;
+    const float mag = nx * nx + ny * ny;
+    if (mag > 1.0f) return false;
+    float nz = sqrtf(1.0f - mag);
+    const float nl = sqrtf(nx * nx + ny * ny + nz * nz);
+    nx /= nl; ny /= nl; nz /= nl;
+    const float s[4] = {e[0] + nx * v.radius, e[1] + ny * v.radius, e[2] + nz * v.radius, 1.0f};
+    /* sphere_pos_eye * pr_matrix: component j = dot(s, column j) */
+    const float cz = s[0] * v.pr[8] + s[1] * v.pr[9] + s[2] * v.pr[10] + s[3] * v.pr[11];
+    const float cw = s[0] * v.pr[12] + s[1] * v.pr[13] + s[2] * v.pr[14] + s[3] * v.pr[15];
+    nd = cz / cw;
+    lin = (nd + 1.0f) * 0.5f;
+    if (!(lin < 1.0f)) return false;   /* background (depth 1) and GL_LESS against the cleared buffer */
+    if (lin < 0.0f) lin = 0.0f;
+    return true;
+}
+
+/* pass 1: nearest depth per pixel (depth values in [0, 1] order like their bit patterns) */
+__global__ void k_splat_depth(View v, int n, const float4* __restrict__ pos, unsigned* __restrict__ zbuf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float e[4], wx, wy, size;
+    if (!sprite(v, pos[i], e, wx, wy, size)) return;
+    const int x0 = max(0, (int)floorf(wx - 0.5f * size)), x1 = min(v.w - 1, (int)ceilf(wx + 0.5f * size));
+    const int y0 = max(0, (int)floorf(wy - 0.5f * size)), y1 = min(v.h - 1, (int)ceilf(wy + 0.5f * size));
+    for (int py = y0; py <= y1; ++py)
+        for (int px = x0; px <= x1; ++px) {
+            float nd, lin;
+            if (fragment(v, e, wx, wy, size, px, py, nd, lin))
+                atomicMin(&zbuf[(size_t)py * v.w + px], __float_as_uint(lin));
+        }
+}
+
+/* pass 2: the lowest particle index among the fragments at the nearest depth */
+__global__ void k_splat_owner(View v, int n, const float4* __restrict__ pos, const unsigned* __restrict__ zbuf,
+                              int* __restrict__ owner) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float e[4], wx, wy, size;
+    if (!sprite(v, pos[i], e, wx, wy, size)) return;
+    const int x0 = max(0, (int)floorf(wx - 0.5f * size)), x1 = min(v.w - 1, (int)ceilf(wx + 0.5f * size));
+    const int y0 = max(0, (int)floorf(wy - 0.5f * size)), y1 = min(v.h - 1, (int)ceilf(wy + 0.5f * size));
+    for (int py = y0; py <= y1; ++py)
+        for (int px = x0; px <= x1; ++px) {
+            float nd, lin;
+            const size_t k = (size_t)py * v.w + px;
+            if (fragment(v, e, wx, wy, size, px, py, nd, lin) && __float_as_uint(lin) == zbuf[k])
+                atomicMin(&owner[k], i);
+        }
+}
+
+/* pass 3: the owner writes its normalised depth */
+__global__ void k_splat_write(View v, int n, const float4* __restrict__ pos, const int* __restrict__ owner,
+                              float* __restrict__ depth) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float e[4], wx, wy, size;
+    if (!sprite(v, pos[i], e, wx, wy, size)) return;
+    const int x0 = max(0, (int)floorf(wx - 0.5f * size)), x1 = min(v.w - 1, (int)ceilf(wx + 0.5f * size));
+    const int y0 = max(0, (int)floorf(wy - 0.5f * size)), y1 = min(v.h - 1, (int)ceilf(wy + 0.5f * size));
+    for (int py = y0; py <= y1; ++py)
+        for (int px = x0; px <= x1; ++px) {
+            const size_t k = (size_t)py * v.w + px;
+            float nd, lin;
+            if (owner[k] == i && fragment(v, e, wx, wy, size, px, py, nd, lin)) depth[k] = nd;
+        }
+}
+
+__global__ void k_splat_clear(int npix, unsigned* __restrict__ zbuf, int* __restrict__ owner, float* __restrict__ depth) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npix) return;
+    zbuf[k] = 0x7f800000u;   /* +inf */
+    owner[k] = 0x7fffffff;
+    depth[k] = 0.0f;
+}
+
+__device__ __forceinline__ float texel(const float* img, int w, int h, int x, int y) {
+    x = x < 0 ? 0 : (x >= w ? w - 1 : x);
+    y = y < 0 ? 0 : (y >= h ? h - 1 : y);
+    return img[(size_t)y * w + x];
+}
+
+/* kernels/bilateral.cl */
+__global__ void k_bilateral(const float* __restrict__ in, float* __restrict__ out, int w, int h) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const float depth = texel(in, w, h, x, y);
+    float o = 0.0f;
+    if (depth > 0.0f) {
+        float sum = 0.0f, wsum = 0.0f;
+        for (int dx = -4; dx < 4; ++dx)
+            for (int dy = -4; dy < 4; ++dy) {
+                const float s = texel(in, w, h, x + dx, y + dy);
+                if (fabsf(s - depth) < 0.015f) {
+                    const float fx = (float)dx, fy = (float)dy;
+                    const float r = sqrtf(fx * fx + fy * fy) * 0.0001f;
+                    const float wt = expf(-r * r);
+                    sum += s * wt;
+                    wsum += wt;
+                }
+            }
+        o = sum / wsum;
+    }
+    out[(size_t)y * w + x] = o;
+}
+
+/* kernels/curvatureflow.cl */
+__global__ void k_curvature_flow(const float* __restrict__ in, float* __restrict__ out, int w, int h, float ipx,
+                                 float ipy) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const float depth = texel(in, w, h, x, y);
+    float o = 0.0f;
+    if (depth > 0.0f) {
+        const float dt = 0.00055f, dzt = 1000.0f;
+        const float zc = depth;
+        const float zdxp = texel(in, w, h, x + 1, y), zdxn = texel(in, w, h, x - 1, y);
+        float zdx = 0.5f * (zdxp - zdxn);
+        zdx = (zdxp == 0.0f || zdxn == 0.0f) ? 0.0f : zdx;
+        const float zdyp = texel(in, w, h, x, y + 1), zdyn = texel(in, w, h, x, y - 1);
+        float zdy = 0.5f * (zdyp - zdyn);
+        zdy = (zdyp == 0.0f || zdyn == 0.0f) ? 0.0f : zdy;
+        const float zdx2 = zdxp + zdxn - 2.0f * zc;
+        const float zdy2 = zdyp + zdyn - 2.0f * zc;
+        const float zdxpyp = texel(in, w, h, x + 1, y + 1), zdxnyn = texel(in, w, h, x - 1, y - 1);
+        const float zdxpyn = texel(in, w, h, x + 1, y - 1), zdxnyp = texel(in, w, h, x - 1, y + 1);
+        const float zdxy = (zdxpyp + zdxnyn - zdxpyn - zdxnyp) / 4.0f;
+        const float cx = 2.0f / ((float)w * -ipx);
+        const float cy = 2.0f / ((float)h * -ipy);
+        const float d = cy * cy * zdx * zdx + cx * cx * zdy * zdy + cx * cx * cy * cy * zc * zc;
+        const float ddx = cy * cy * 2.0f * zdx * zdx2 + cx * cx * 2.0f * zdy * zdxy + cx * cx * cy * cy * 2.0f * zc * zdx;
+        const float ddy = cy * cy * 2.0f * zdx * zdxy + cx * cx * 2.0f * zdy * zdy2 + cx * cx * cy * cy * 2.0f * zc * zdy;
+        const float ex = 0.5f * zdx * ddx - zdx2 * d;
+        const float ey = 0.5f * zdy * ddy - zdy2 * d;
+        const float hm = 0.5f * ((cy * ex + cx * ey) / powf(d, 1.5f));
+        o = depth + hm * dt * (1.0f + (fabsf(zdx) + fabsf(zdy)) * dzt);
+    }
+    out[(size_t)y * w + x] = o;
+}
+
+struct Inv {
+    float m[16];
+};
+
+__device__ __forceinline__ void uv_to_eye(const Inv& ip, float u, float v, float depth, float o[3]) {
+    const float c[4] = {u * 2.0f - 1.0f, v * 2.0f - 1.0f, depth, 1.0f};
+    float e[4];
+    mat_vec(ip.m, c, e);
+    o[0] = e[0] / e[3];
+    o[1] = e[1] / e[3];
+    o[2] = e[2] / e[3];
+}
+
+/* shaders/sspace_fluid_rendering/normals_stage.frag */
+__global__ void k_depth_normals(const float* __restrict__ depth, float4* __restrict__ nrm, int w, int h, Inv ip) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const float d = texel(depth, w, h, x, y);
+    if (d <= 0.0f) {
+        nrm[(size_t)y * w + x] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float tx = 1.0f / (float)w, ty = 1.0f / (float)h;
+    const float u = ((float)x + 0.5f) * tx, v = ((float)y + 0.5f) * ty;
+    float p[3], a[3], b[3], ddx[3], ddy[3];
+    uv_to_eye(ip, u, v, d, p);
+    uv_to_eye(ip, u + tx, v, texel(depth, w, h, x + 1, y), a);
+    uv_to_eye(ip, u - tx, v, texel(depth, w, h, x - 1, y), b);
+    for (int k = 0; k < 3; ++k) {
+        ddx[k] = a[k] - p[k];
+        b[k] = -b[k] + p[k];
+    }
+    if (fabsf(ddx[2]) > fabsf(b[2]))
+        for (int k = 0; k < 3; ++k) ddx[k] = b[k];
+    uv_to_eye(ip, u, v + ty, texel(depth, w, h, x, y + 1), a);
+    uv_to_eye(ip, u, v - ty, texel(depth, w, h, x, y - 1), b);
+    for (int k = 0; k < 3; ++k) {
+        ddy[k] = a[k] - p[k];
+        b[k] = -b[k] + p[k];
+    }
+    if (fabsf(ddy[2]) > fabsf(b[2]))
+        for (int k = 0; k < 3; ++k) ddy[k] = b[k];
+    float cx = ddx[1] * ddy[2] - ddx[2] * ddy[1];
+    float cy = ddx[2] * ddy[0] - ddx[0] * ddy[2];
+    float cz = ddx[0] * ddy[1] - ddx[1] * ddy[0];
+    const float l = sqrtf(cx * cx + cy * cy + cz * cz);
+    nrm[(size_t)y * w + x] = make_float4(cx / l, cy / l, cz / l, 1.0f);
+}
+
+inline dim3 grid2(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
+
+}  // namespace
+}  // namespace sph
+
+extern "C" {
+
+int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
+    if (!x || !view || !d_depth) return SPH_E_INVALID;
+    if (view->width <= 0 || view->height <= 0 || (long long)view->width * view->height > (1LL << 28))
+        return sph_ctx_fail(x, SPH_E_INVALID, "render: width and height must be > 0 (at most 2^28 pixels)");
+    if (!(view->point_radius > 0.f) || !(view->point_scale > 0.f))
+        return sph_ctx_fail(x, SPH_E_INVALID, "render: point_radius and point_scale must be > 0");
+    if (!x->has_state || x->N <= 0) return sph_ctx_fail(x, SPH_E_STATE, "render: no particles added");
+    const size_t npix = (size_t)view->width * view->height;
+    if (x->render_pixels < npix) {
+        cudaStreamSynchronize(x->stream);
+        cudaFree(x->render_buf);
+        x->render_buf = nullptr;
+        x->render_pixels = 0;
+        if (cudaMalloc(&x->render_buf, 8 * npix) != cudaSuccess) {
+            cudaGetLastError();
+            return sph_ctx_fail(x, SPH_E_NOMEM, "render: depth-test buffers");
+        }
+        x->render_pixels = npix;
+    }
+    sph::View v;
+    std::memcpy(v.mv, view->modelview, sizeof v.mv);
+    std::memcpy(v.pr, view->projection, sizeof v.pr);
+    v.radius = view->point_radius;
+    v.scale = view->point_scale;
+    v.w = view->width;
+    v.h = view->height;
+    unsigned* zbuf = reinterpret_cast<unsigned*>(x->render_buf);
+    int* owner = reinterpret_cast<int*>(zbuf + npix);
+    const cudaStream_t s = x->stream;
+    const int bs = 256, n = x->N;
+    sph::k_splat_clear<<<(int)((npix + bs - 1) / bs), bs, 0, s>>>((int)npix, zbuf, owner, d_depth);
+    sph::k_splat_depth<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, zbuf);
+    sph::k_splat_owner<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, zbuf, owner);
+    sph::k_splat_write<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, owner, d_depth);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return sph_ctx_fail(x, SPH_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
+    return SPH_OK;
+}
+
+int sph_filter_bilateral(const float* d_in, float* d_out, int width, int height, void* stream) {
+    if (!d_in || !d_out || width <= 0 || height <= 0 || d_in == d_out) return SPH_E_INVALID;
+    const dim3 b(16, 16);
+    sph::k_bilateral<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(d_in, d_out, width, height);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}
+
+int sph_render_smooth(float* d_depth, float* d_tmp, int width, int height, int iterations, void* stream) {
+    if (!d_depth || !d_tmp || width <= 0 || height <= 0 || iterations < 0 || d_depth == d_tmp) return SPH_E_INVALID;
+    const dim3 b(16, 16);
+    const cudaStream_t s = (cudaStream_t)stream;
+    for (int it = 0; it < iterations; ++it) {
+        sph::k_bilateral<<<sph::grid2(width, height, b), b, 0, s>>>(d_depth, d_tmp, width, height);
+        sph::k_bilateral<<<sph::grid2(width, height, b), b, 0, s>>>(d_tmp, d_depth, width, height);
+    }
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}
+
+int sph_filter_curvature_flow(const float* d_in, float* d_out, int width, int height, float inv_proj_x,
+                              float inv_proj_y, void* stream) {
+    if (!d_in || !d_out || width <= 0 || height <= 0 || d_in == d_out) return SPH_E_INVALID;
+    const dim3 b(16, 16);
+    sph::k_curvature_flow<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(d_in, d_out, width, height,
+                                                                                         inv_proj_x, inv_proj_y);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}
+
+int sph_render_normals(const float* d_depth, float* d_normals4, int width, int height, const float inv_projection[16],
+                       void* stream) {
+    if (!d_depth || !d_normals4 || !inv_projection || width <= 0 || height <= 0) return SPH_E_INVALID;
+    sph::Inv ip;
+    std::memcpy(ip.m, inv_projection, sizeof ip.m);
+    const dim3 b(16, 16);
+    sph::k_depth_normals<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(
+        d_depth, reinterpret_cast<float4*>(d_normals4), width, height, ip);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}
+
+}  // extern "C"

@@ -294,6 +294,41 @@ int sph_adj_flags(sph_adj* adj, unsigned* flags);
 /* Device bytes the adjoint holds (checkpoints, one segment's tape, scratch). */
 int sph_adj_tape_bytes(const sph_adj* adj, size_t* bytes);
 
+/* ---- screen-space surface ------------------------------------------------------------ */
+
+/* The depth, blur and normals stages of SSpaceFluidRenderer (fluid/render/
+ * sspacefluidrenderer.cpp:35-53) as CUDA kernels writing plain device images instead of
+ * GL textures: row-major, row 0 at the bottom, width * height floats (depth) or float4
+ * (normals).  Reads outside an image clamp to its edge.  All asynchronous. */
+typedef struct sph_view {
+    float modelview[16];   /* mv_matrix, column-major like a GL uniform */
+    float projection[16];  /* pr_matrix (camera.projection()), column-major */
+    float point_radius;    /* sprite sphere radius; the renderer uses 0.0625 (:365) */
+    float point_scale;     /* viewport width * tan(fov / 2) (:366) */
+    int width, height;     /* image size in pixels (at most 2^28 pixels) */
+} sph_view;
+/* _render_depth_stage (:355-388) with shaders/sspace_fluid_rendering/depth_stage.vert and
+ * .frag: every fluid particle of the context is a sphere sprite; d_depth receives at each
+ * pixel the NDC depth of the nearest sprite fragment (GL_LESS on the normalised depth, the
+ * lower particle index winning a tie) and 0 where no sprite covers it.  No background
+ * depth texture: fragments beyond the far plane are dropped.  Runs on the context stream;
+ * holds 8 bytes per pixel of scratch in the context. */
+int sph_render_depth(sph_ctx* ctx, const sph_view* view, float* d_depth);
+/* One pass of kernels/bilateral.cl (BilateralFilter::filter, filters/bilateralfilter.cpp:
+ * 28-41): d_in and d_out must differ. */
+int sph_filter_bilateral(const float* d_in, float* d_out, int width, int height, void* cuda_stream);
+/* _render_blur_stage (:390-408): iterations times bilateral d_depth -> d_tmp -> d_depth. */
+int sph_render_smooth(float* d_depth, float* d_tmp, int width, int height, int iterations, void* cuda_stream);
+/* One explicit step of kernels/curvatureflow.cl (screen-space mean-curvature flow; the
+ * reference ships the kernel without a host caller).  inv_proj_x, inv_proj_y: the inverse
+ * projection's x and y scale terms. */
+int sph_filter_curvature_flow(const float* d_in, float* d_out, int width, int height, float inv_proj_x,
+                              float inv_proj_y, void* cuda_stream);
+/* _render_normals_stage (:410-434) with normals_stage.frag: view-space normals (x, y, z, 1)
+ * of the depth image, (0, 0, 0, 0) where depth <= 0.  inv_projection: column-major. */
+int sph_render_normals(const float* d_depth, float* d_normals4, int width, int height,
+                       const float inv_projection[16], void* cuda_stream);
+
 /* ---- primitives ---------------------------------------------------------------------- */
 
 /* clsort<cl_uint, cl_int> (opencl/algorithms/clsort.h:13-35): stable ascending sort of n

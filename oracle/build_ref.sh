@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/libref_kernels.so: the reference's own OpenCL kernels
-# (kernels/grid.cl, wcsph.cl, normals.cl, pcisph.cl, boundary.cl and their headers)
+# (kernels/grid.cl, wcsph.cl, normals.cl, pcisph.cl, boundary.cl, bilateral.cl,
+# curvatureflow.cl and their headers)
 # compiled for the CPU through oracle/ref_shim/clshim.hpp.  Used only to pin the oracle
 # and to generate tests/golden/ fixtures, in a container where the reference is mounted.
 #
@@ -21,9 +22,9 @@ for f in "$ref"/kernels/*.cl "$ref"/kernels/*.h; do
     sed -E 's/\((int4|float4)\)[[:space:]]*\(/make_\1(/g' "$f" > "$out/src/$(basename "$f")"
 done
 CXX="${CXX:-g++}"
-flags=(-O1 -std=c++17 -fPIC -ffp-contract=off -Wall -Wno-sign-compare -Wno-unused -I "$here/ref_shim" -I "$out/src")
+flags=(-O1 -std=c++17 -fPIC -ffp-contract=off -Wall -Wno-sign-compare -Wno-unused -Wno-narrowing -I "$here/ref_shim" -I "$out/src")
 pids=()
-for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary; do
+for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary ref_render; do
     "$CXX" "${flags[@]}" -c "$here/ref_shim/$u.cpp" -o "$out/obj/$u.o" &
     pids+=($!)
 done

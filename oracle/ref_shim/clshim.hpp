@@ -1,5 +1,5 @@
 /*
- * clshim.hpp -- lets g++ compile the reference's OpenCL C kernels (kernels/*.cl) for the
+ * clshim.hpp -- lets g++ compile the reference's OpenCL C kernels (kernels/NAME.cl) for the
  * CPU so the oracle can be pinned against the reference's own kernel text.
  * TEST INFRASTRUCTURE: built only by oracle/build_ref.sh into oracle/_ref/.
  *
@@ -10,7 +10,9 @@
  *     oracle restates them (dot left to right over x,y,z,w; length = sqrt(dot);
  *     normalize = v / length with the zero vector mapped to itself; pown = repeated
  *     multiplication; clamp = min(max()); sign per the OpenCL spec);
- *   - image1d_buffer_t + read_imagef over a plain array (CL_RGBA or CL_R);
+ *   - image1d_buffer_t + read_imagef over a plain array (CL_RGBA or CL_R), and a
+ *     single-channel image2d_t with the clamp-to-edge / nearest sampler and write_imagef
+ *     (kernels/bilateral.cl, kernels/curvatureflow.cl), run by a 2-D NDRange runner;
  *   - the -D program constants as runtime globals (PARTICLE_COUNT, SUPPORT_RADIUS, ...);
  *   - an NDRange runner: work-items of one work-group run as ucontext fibers, and
  *     barrier() switches back to the group scheduler, so local-memory caches and the
@@ -41,7 +43,7 @@ extern float g_cell_size;
 extern float g_grid_size;
 extern int g_cells_per_side;
 
-struct WorkItem { size_t gid, lid, lsize, group; };
+struct WorkItem { size_t gid, lid, lsize, group, gid1 = 0; };
 extern thread_local WorkItem* tl_cur;
 void barrier_impl();
 
@@ -49,12 +51,19 @@ void barrier_impl();
  * multiple of local, as the reference's launches are). With fibers=false, a barrier()
  * aborts: use it only for kernels that have none. */
 void run_ndrange(size_t global, size_t local, bool fibers, const std::function<void()>& body);
+/* A 2-D NDRange of independent work-items (no barrier), dimension 0 fastest. */
+void run_ndrange_2d(size_t gx, size_t gy, const std::function<void()>& body);
 }  // namespace clshim
 
 typedef unsigned int uint;
 
 struct float2 { float x, y; };
 struct int2 { int x, y; };
+struct float3 { float x, y, z; };
+inline int2 operator+(const int2& a, const int2& b) { return int2{a.x + b.x, a.y + b.y}; }
+inline int2 operator-(const int2& a, const int2& b) { return int2{a.x - b.x, a.y - b.y}; }
+inline float2 convert_float2(const int2& a) { return float2{(float)a.x, (float)a.y}; }
+inline float fast_length(const float2& a) { return std::sqrt(a.x * a.x + a.y * a.y); }
 
 template <int A, int B>
 struct swz2f {
@@ -136,7 +145,20 @@ inline float4 read_imagef(const image1d_buffer_t& im, int i) {
     return make_float4(im.data[i], 0.0f, 0.0f, 1.0f);
 }
 
-inline size_t get_global_id(int) { return clshim::tl_cur->gid; }
+/* single-channel float image; the sampler is always clamp-to-edge, nearest, unnormalised */
+typedef int sampler_t;
+#define CLK_NORMALIZED_COORDS_FALSE 0
+#define CLK_ADDRESS_CLAMP_TO_EDGE 0
+#define CLK_FILTER_NEAREST 0
+struct image2d_t { float* data; int w, h; };
+inline float4 read_imagef(const image2d_t& im, sampler_t, int2 p) {
+    const int x = p.x < 0 ? 0 : (p.x >= im.w ? im.w - 1 : p.x);
+    const int y = p.y < 0 ? 0 : (p.y >= im.h ? im.h - 1 : p.y);
+    return make_float4(im.data[(size_t)y * im.w + x], 0.0f, 0.0f, 1.0f);
+}
+inline void write_imagef(const image2d_t& im, int2 p, float4 v) { im.data[(size_t)p.y * im.w + p.x] = v.x; }
+
+inline size_t get_global_id(int d) { return d == 0 ? clshim::tl_cur->gid : clshim::tl_cur->gid1; }
 inline size_t get_local_id(int) { return clshim::tl_cur->lid; }
 inline size_t get_local_size(int) { return clshim::tl_cur->lsize; }
 inline size_t get_group_id(int) { return clshim::tl_cur->group; }

@@ -13,6 +13,9 @@
 #define constant static const
 #define read_only
 #define write_only
+#define __read_only
+#define __write_only
+#define __constant static const
 
 /* -D program constants (opencl/clcompiler.cpp:38-54) as runtime values */
 #define PARTICLE_COUNT (::clshim::g_particle_count)

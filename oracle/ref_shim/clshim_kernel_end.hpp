@@ -11,3 +11,6 @@
 #undef constant
 #undef read_only
 #undef write_only
+#undef __read_only
+#undef __write_only
+#undef __constant

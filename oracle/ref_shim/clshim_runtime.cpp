@@ -89,4 +89,14 @@ void run_ndrange(size_t global, size_t local, bool fibers, const std::function<v
     tl_body = nullptr;
     tl_sched = nullptr;
 }
+void run_ndrange_2d(size_t gx, size_t gy, const std::function<void()>& body) {
+    for (size_t y = 0; y < gy; ++y)
+        for (size_t x = 0; x < gx; ++x) {
+            WorkItem wi{x, x, gx, 0, y};
+            tl_cur = &wi;
+            body();
+        }
+    tl_cur = nullptr;
+}
+
 }  // namespace clshim

@@ -198,3 +198,19 @@ def fluid_force(bpos4, bphi, fpos4, fdens, fpres, intervals, mass, spiky_grad, s
                           f(size), f(h), i(cps), i(n), P(force), P(torque), P(c4), P(fvel4), P(bvel4), f(visc_lapl),
                           f(h_define))
     return force, torque
+
+
+def bilateral_filter(depth):
+    """kernels/bilateral.cl over a (height, width) float32 image."""
+    img = np.ascontiguousarray(depth, np.float32)
+    out = np.zeros_like(img)
+    lib().ref_bilateral_filter(P(img), P(out), i(img.shape[1]), i(img.shape[0]))
+    return out
+
+
+def curvature_flow(depth, inv_proj_x, inv_proj_y):
+    """kernels/curvatureflow.cl over a (height, width) float32 image."""
+    img = np.ascontiguousarray(depth, np.float32)
+    out = np.zeros_like(img)
+    lib().ref_curvature_flow(P(img), P(out), i(img.shape[1]), i(img.shape[0]), f(inv_proj_x), f(inv_proj_y))
+    return out

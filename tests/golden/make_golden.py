@@ -4,6 +4,8 @@ mounted:
 
     python tests/golden/make_golden.py
 
+    python tests/golden/make_golden.py render    # only render_small.npz
+
 Every stage output is produced by chaining reference kernels only (the key sort is the
 stable ascending sort clogs performs, numpy's stable argsort; the shuffle is a gather).  The
 kernel constants are the host-side derivation restated by the oracle (stored with the
@@ -22,6 +24,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from oracle import Oracle  # noqa: E402  (derived constants only)
 from oracle import refkernels as rk  # noqa: E402
+from oracle import render as orender  # noqa: E402
 from scenes_np import small_scene  # noqa: E402
 
 GRID_SIZE = 5.0
@@ -137,9 +140,41 @@ def save(name, sc, out, kw, d):
     print("wrote", name, os.path.getsize(os.path.join(HERE, name)), "bytes")
 
 
+def render_fixture():
+    """Screen-space surface of a seeded particle blob seen by the reference's default camera
+    (fov 45, near 0.5, far 30: gui/glwidget.cpp:82-88; point size uniforms:
+    fluid/render/sspacefluidrenderer.cpp:365-366).  The depth and normals images come from the
+    restatement (the GLSL stages cannot run here); the smoothing filters from the
+    reference's own OpenCL kernels compiled for the CPU."""
+    w, h = 128, 96
+    rng = np.random.default_rng(20250601)
+    pos = np.zeros((2500, 4), np.float32)
+    pos[:, :3] = rng.uniform(0.1, 0.9, (2500, 3))   # inside a container of side 1
+    mv = orender.look_at([1.3, 1.5, 2.2], [0.5, 0.5, 0.5], [0.0, 1.0, 0.0])
+    pr = orender.perspective(45.0, w / h, 0.5, 30.0)
+    ipr = np.linalg.inv(pr.astype(np.float64)).astype(np.float32)
+    radius, scale = 0.0625, w * np.tan(np.radians(22.5))
+    depth = orender.splat_depth(pos, mv, pr, radius, scale, w, h)
+    bil = rk.bilateral_filter(depth)
+    smooth = depth
+    for _ in range(2):
+        smooth = rk.bilateral_filter(rk.bilateral_filter(smooth))
+    curv = rk.curvature_flow(depth, ipr[0, 0], ipr[1, 1])
+    nrm = orender.depth_normals(smooth, ipr)
+    path = os.path.join(HERE, "render_small.npz")
+    np.savez_compressed(path, pos=pos, modelview=mv, projection=pr, inv_projection=ipr,
+                        point_radius=np.float32(radius), point_scale=np.float32(scale), width=w, height=h,
+                        depth=depth, bilateral=bil, smooth2=smooth, curvature=curv, normals=nrm)
+    print("wrote render_small.npz", os.path.getsize(path), "bytes; covered", float((depth != 0).mean()))
+
+
 def main():
     if rk.build() is None:
         raise SystemExit("the reference kernels are not available here")
+    if sys.argv[1:] == ["render"]:
+        render_fixture()
+        return
+    render_fixture()
     sc = small_scene()
     out, kw, d = wcsph(sc)
     save("wcsph_compat_small.npz", sc, out, kw, d)

@@ -1,0 +1,191 @@
+"""Screen-space fluid surface (fluids_gb300/csrc/sph_render.cu) against the restatement in
+oracle/render.py and the golden images of tests/golden/render_small.npz (depth and normals
+from the restatement; bilateral, two blur iterations and curvature flow from the reference's
+own kernels/bilateral.cl and kernels/curvatureflow.cl compiled for the CPU).
+
+Tolerances: the depth and normals images bit for bit (the kernels round every operation
+like the restatement); the filters within 2e-6 of the depth scale for the bilateral filter
+(exp differs in its last bits) and 1e-5 relative to each pixel's magnitude for the curvature
+flow (pow(d, 1.5) likewise)."""
+import os
+
+import numpy as np
+import pytest
+
+from fluids_gb300 import capi
+from oracle import refkernels
+from oracle import render as orender
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "render_small.npz")
+
+
+def golden():
+    return dict(np.load(GOLDEN))
+
+
+def assert_curvature(name, got, want):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    err = np.abs(got - want) / np.maximum(np.abs(want), 1.0)
+    assert np.isfinite(got).all() == np.isfinite(want).all(), name
+    assert err.max() <= 1e-5, "%s: max rel err %.3g at %s" % (name, err.max(), np.unravel_index(err.argmax(), err.shape))
+
+
+def assert_bilateral(name, got, want):
+    err = np.abs(np.asarray(got, np.float64) - want).max()
+    assert err <= 2e-6, "%s: max err %.3g" % (name, err)
+
+
+def describe_mismatch(got, want):
+    bad = got != want
+    if not bad.any():
+        return "equal"
+    idx = np.argwhere(bad)[:5]
+    return "%d of %d differ, first %s: %s vs %s, max |diff| %.3g" % (
+        bad.sum(), bad.size, idx.tolist(), got[bad][:5], want[bad][:5], np.nanmax(np.abs(got - want)))
+
+
+# ---- the restatement (CPU) ------------------------------------------------------------
+
+def test_restatement_reproduces_golden():
+    g = golden()
+    d = orender.splat_depth(g["pos"], g["modelview"], g["projection"], g["point_radius"], g["point_scale"],
+                            int(g["width"]), int(g["height"]))
+    assert np.array_equal(d, g["depth"]), describe_mismatch(d, g["depth"])
+    assert_bilateral("bilateral", orender.bilateral(g["depth"]), g["bilateral"])
+    s = g["depth"]
+    for _ in range(4):
+        s = orender.bilateral(s)
+    assert_bilateral("smooth2", s, g["smooth2"])
+    ip = g["inv_projection"]
+    assert_curvature("curvature", orender.curvature_flow(g["depth"], ip[0, 0], ip[1, 1]), g["curvature"])
+    n = orender.depth_normals(g["smooth2"], ip)
+    assert np.array_equal(n, g["normals"]), describe_mismatch(n, g["normals"])
+
+
+@pytest.mark.skipif(not refkernels.available(), reason="reference kernels not available")
+def test_filter_restatement_matches_reference_kernels():
+    rng = np.random.default_rng(7)
+    img = np.zeros((40, 56), np.float32)
+    img[5:33, 8:50] = 0.6 + 0.01 * rng.random((28, 42)).astype(np.float32)
+    img[12:18, 20:30] = 0.62                  # a step inside the 0.015 gate
+    img[20:24, 30:34] = 0.7                   # a step outside it
+    img[0:3, 0:4] = 0.5                       # touching the clamped edge
+    assert_bilateral("bilateral", orender.bilateral(img), refkernels.bilateral_filter(img))
+    for ipx, ipy in ((-0.55, -0.41), (0.9, 0.7)):
+        assert_curvature("curvature", orender.curvature_flow(img, ipx, ipy), refkernels.curvature_flow(img, ipx, ipy))
+
+
+def test_single_sprite_is_a_disc_at_the_sphere_depth():
+    w, h = 96, 96
+    pr = orender.perspective(45.0, 1.0, 0.5, 30.0)
+    mv = np.eye(4, dtype=np.float32)
+    pos = np.array([[0.0, 0.0, -3.0, 0.0]], np.float32)
+    radius, scale = 1.0, w * np.tan(np.radians(22.5))
+    d = orender.splat_depth(pos, mv, pr, radius, scale, w, h)
+    size = radius * scale / 3.0
+    area = (d != 0).sum()
+    assert abs(area - np.pi * (size / 2) ** 2) < 0.1 * area
+    # the centre fragment lies on the sphere at eye z = -3 + radius; the depth uses the
+    # transposed projection (sphere_pos_eye * pr_matrix)
+    z = np.float64(-3.0 + radius)
+    nd = (pr[0, 2] * 0 + pr[2, 2] * z + pr[3, 2]) / (pr[2, 3] * z + pr[3, 3])
+    assert abs(d[h // 2, w // 2] - nd) < 2e-3
+
+
+def test_nearer_sprite_wins_and_ties_keep_the_first():
+    w, h = 48, 48
+    pr = orender.perspective(45.0, 1.0, 0.5, 30.0)
+    mv = np.eye(4, dtype=np.float32)
+    far = np.array([[0.0, 0.0, -4.0, 0.0]], np.float32)
+    near = np.array([[0.0, 0.0, -3.0, 0.0]], np.float32)
+    args = (mv, pr, 0.3, w * np.tan(np.radians(22.5)), w, h)
+    a = orender.splat_depth(np.concatenate([far, near]), *args)
+    b = orender.splat_depth(np.concatenate([near, far]), *args)
+    n = orender.splat_depth(near, *args)
+    assert np.array_equal(a, b)
+    assert a[h // 2, w // 2] == n[h // 2, w // 2]
+    twice = orender.splat_depth(np.concatenate([near, near]), *args)
+    assert np.array_equal(twice, n)
+
+
+def test_filters_leave_empty_pixels_empty():
+    img = np.zeros((16, 16), np.float32)
+    img[4:8, 4:8] = 0.5
+    out = orender.bilateral(img)
+    assert (out[img == 0] == 0).all()
+    # a flat patch is a fixed point of the bilateral filter
+    assert np.allclose(out[img != 0], 0.5, atol=1e-7)
+
+
+# ---- the CUDA kernels (GPU) -------------------------------------------------------------
+
+def _context(pos4):
+    p = capi.make_params(0, mode=capi.SPH_MODE_COMPAT, relax_on_add=0, neighbor_mode=capi.SPH_NEIGH_LIST)
+    ctx = capi.Context(p)
+    ctx.set_rect_limits(1.0, 1.0, 1.0)
+    ctx.add_volume(pos4)
+    return ctx
+
+
+@pytest.mark.gpu
+def test_gpu_depth_matches_restatement(gpu_lib):
+    import torch
+    g = golden()
+    w, h = int(g["width"]), int(g["height"])
+    ctx = _context(g["pos"])
+    pos = ctx.get("POS").reshape(-1, 4)
+    view = capi.make_view(g["modelview"], g["projection"], g["point_radius"], g["point_scale"], w, h)
+    img = torch.full((h, w), 7.0, dtype=torch.float32, device="cuda")
+    ctx.render_depth(view, img.data_ptr())
+    ctx.synchronize()
+    got = img.cpu().numpy()
+    want = orender.splat_depth(pos, g["modelview"], g["projection"], g["point_radius"], g["point_scale"], w, h)
+    if np.array_equal(pos, g["pos"]):
+        assert np.array_equal(want, g["depth"])
+    assert np.array_equal(got, want), describe_mismatch(got, want)
+    # a second, larger image reallocates the depth-test scratch
+    view2 = capi.make_view(g["modelview"], g["projection"], g["point_radius"], g["point_scale"], 2 * w, 2 * h)
+    img2 = torch.empty((2 * h, 2 * w), dtype=torch.float32, device="cuda")
+    ctx.render_depth(view2, img2.data_ptr())
+    ctx.synchronize()
+    want2 = orender.splat_depth(pos, g["modelview"], g["projection"], g["point_radius"], g["point_scale"], 2 * w,
+                                2 * h)
+    got2 = img2.cpu().numpy()
+    assert np.array_equal(got2, want2), describe_mismatch(got2, want2)
+
+
+@pytest.mark.gpu
+def test_gpu_filters_match_reference_golden(gpu_lib):
+    import torch
+    g = golden()
+    w, h = int(g["width"]), int(g["height"])
+    src = torch.from_numpy(g["depth"]).cuda()
+    out = torch.empty_like(src)
+    capi.filter_bilateral(src.data_ptr(), out.data_ptr(), w, h)
+    torch.cuda.synchronize()
+    assert_bilateral("bilateral", out.cpu().numpy(), g["bilateral"])
+    work = src.clone()
+    tmp = torch.empty_like(src)
+    capi.render_smooth(work.data_ptr(), tmp.data_ptr(), w, h, 2)
+    torch.cuda.synchronize()
+    assert_bilateral("smooth2", work.cpu().numpy(), g["smooth2"])
+    ip = g["inv_projection"]
+    capi.filter_curvature_flow(src.data_ptr(), out.data_ptr(), w, h, ip[0, 0], ip[1, 1])
+    torch.cuda.synchronize()
+    assert_curvature("curvature", out.cpu().numpy(), g["curvature"])
+    with pytest.raises(capi.SphError):
+        capi.filter_bilateral(src.data_ptr(), src.data_ptr(), w, h)
+
+
+@pytest.mark.gpu
+def test_gpu_normals_match_restatement(gpu_lib):
+    import torch
+    g = golden()
+    w, h = int(g["width"]), int(g["height"])
+    src = torch.from_numpy(g["smooth2"]).cuda()
+    nrm = torch.full((h, w, 4), 9.0, dtype=torch.float32, device="cuda")
+    capi.render_normals(src.data_ptr(), nrm.data_ptr(), w, h, g["inv_projection"])
+    torch.cuda.synchronize()
+    got = nrm.cpu().numpy()
+    assert np.array_equal(got, g["normals"]), describe_mismatch(got, g["normals"])
