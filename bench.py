@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--batched-steps", type=int, default=500, help="0 skips the batched comparison")
     ap.add_argument("--adjoint-steps", type=int, default=200, help="0 skips the adjoint comparison")
     ap.add_argument("--pcisph-steps", type=int, default=100, help="0 skips the PCISPH line")
+    ap.add_argument("--render-frames", type=int, default=20, help="0 skips the screen-space surface line")
     return ap.parse_args()
 
 
@@ -354,6 +355,41 @@ def bench_pcisph(torch, steps, warmup):
     return out
 
 
+def bench_render(torch, ctx, stream, frames, width=1920, height=1080):
+    """Screen-space surface of the context's particles (depth sprites, two blur iterations,
+    normals) at width x height with the reference's default camera and sprite radius; device
+    time per stage from CUDA events on the context stream, averaged over `frames` frames."""
+    from fluids_gb300 import capi, render
+    cam = render.Camera(width, height)
+    mv = render.look_at((1.0, 1.3, 3.2), (1.0, 0.25, 0.5), (0.0, 1.0, 0.0))
+    r = render.SSpaceFluidRenderer(width, height)
+    s = stream.cuda_stream
+    for _ in range(3):
+        r.render(ctx, cam, mv, s)
+    pr = cam.projection()
+    ipr = np.linalg.inv(pr.astype(np.float64)).astype(np.float32)
+    view = capi.make_view(mv, pr, r.point_radius, cam.point_scale(), width, height)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    tot = np.zeros(3)
+    torch.cuda.synchronize()
+    for _ in range(frames):
+        ev[0].record(stream)
+        ctx.render_depth(view, r.depth.data_ptr())
+        ev[1].record(stream)
+        capi.render_smooth(r.depth.data_ptr(), r.blurred.data_ptr(), width, height, r.filter_iterations, s)
+        ev[2].record(stream)
+        capi.render_normals(r.depth.data_ptr(), r.normals.data_ptr(), width, height, ipr, s)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        tot += [ev[k].elapsed_time(ev[k + 1]) for k in range(3)]
+    ms = tot / frames
+    return {"image": [width, height], "particles": ctx.particle_count(), "point_radius": r.point_radius,
+            "filter_iterations": r.filter_iterations, "frames": frames, "ms_per_frame": float(ms.sum()),
+            "ms_depth": float(ms[0]), "ms_blur": float(ms[1]), "ms_normals": float(ms[2]),
+            "coverage": float((r.depth != 0).float().mean().item()),
+            "kernels_per_frame": 3 + 2 * r.filter_iterations + 1}
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -487,6 +523,9 @@ def main():
         e2e = {"value": units_e / te, "unit": UNIT, "h2d_bytes_per_step": 48 * n,
                "d2h_bytes_per_step": 48 * n, "steps": k_e2e, "host_buffers": "pinned",
                "copies": "pos, vel, vel_half in and out on the context stream; one host wait per step"}
+    rend = None
+    if args.render_frames > 0:
+        rend = bench_render(torch, ctx, stream, args.render_frames)
     ctx.close()
     batched = None
     if args.batched_steps > 0 and args.workload == "wcsph4m":
@@ -513,7 +552,7 @@ def main():
                 "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk,
                 "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched, "adjoint": adjoint,
-                "pcisph": pcisph}
+                "pcisph": pcisph, "render": rend}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -3,7 +3,7 @@
  * kernels writing device images (no graphics API): particle depth sprites, the two
  * smoothing filters, and view-space normals.
  *
- *   k_splat_*        shaders/sspace_fluid_rendering/depth_stage.{vert,frag}: each particle
+ *   k_splat_*        shaders/sspace_fluid_rendering/depth_stage.vert and .frag: each particle
  *                    is a point sprite of gl_PointSize = point_radius * point_scale / |p_eye|;
  *                    a fragment inside the sprite's disc lies on the sphere of radius
  *                    point_radius around the particle; its normalised depth is written where
@@ -74,8 +74,12 @@ __device__ __forceinline__ bool fragment(const View& v, const float e[4], float 
     return true;
 }
 
-/* pass 1: nearest depth per pixel (depth values in [0, 1] order like their bit patterns) */
-__global__ void k_splat_depth(View v, int n, const float4* __restrict__ pos, unsigned* __restrict__ zbuf) {
+/* Depth test of every sprite fragment: one 64-bit key per pixel, (normalised depth bits << 32)
+ * | particle index, so atomicMin keeps the nearest fragment and, among equal depths, the
+ * lowest index (the first primitive GL_LESS lets through).  Depths are >= 0, so their bit
+ * patterns order like the values.  A plain read first skips fragments that already lose:
+ * keys only decrease, so a stale read can only cost an unneeded atomic. */
+__global__ void k_splat_keys(View v, int n, const float4* __restrict__ pos, unsigned long long* __restrict__ key) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float e[4], wx, wy, size;
@@ -85,52 +89,31 @@ __global__ void k_splat_depth(View v, int n, const float4* __restrict__ pos, uns
     for (int py = y0; py <= y1; ++py)
         for (int px = x0; px <= x1; ++px) {
             float nd, lin;
-            if (fragment(v, e, wx, wy, size, px, py, nd, lin))
-                atomicMin(&zbuf[(size_t)py * v.w + px], __float_as_uint(lin));
+            if (!fragment(v, e, wx, wy, size, px, py, nd, lin)) continue;
+            const unsigned long long k = ((unsigned long long)__float_as_uint(lin) << 32) | (unsigned)i;
+            unsigned long long* dst = &key[(size_t)py * v.w + px];
+            if (k < *reinterpret_cast<volatile unsigned long long*>(dst)) atomicMin(dst, k);
         }
 }
 
-/* pass 2: the lowest particle index among the fragments at the nearest depth */
-__global__ void k_splat_owner(View v, int n, const float4* __restrict__ pos, const unsigned* __restrict__ zbuf,
-                              int* __restrict__ owner) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float e[4], wx, wy, size;
-    if (!sprite(v, pos[i], e, wx, wy, size)) return;
-    const int x0 = max(0, (int)floorf(wx - 0.5f * size)), x1 = min(v.w - 1, (int)ceilf(wx + 0.5f * size));
-    const int y0 = max(0, (int)floorf(wy - 0.5f * size)), y1 = min(v.h - 1, (int)ceilf(wy + 0.5f * size));
-    for (int py = y0; py <= y1; ++py)
-        for (int px = x0; px <= x1; ++px) {
-            float nd, lin;
-            const size_t k = (size_t)py * v.w + px;
-            if (fragment(v, e, wx, wy, size, px, py, nd, lin) && __float_as_uint(lin) == zbuf[k])
-                atomicMin(&owner[k], i);
-        }
+/* Per pixel: the winning particle's fragment depth, recomputed with the same arithmetic. */
+__global__ void k_splat_resolve(View v, const float4* __restrict__ pos, const unsigned long long* __restrict__ key,
+                                float* __restrict__ depth) {
+    const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= v.w || py >= v.h) return;
+    const size_t k = (size_t)py * v.w + px;
+    const unsigned long long kk = key[k];
+    float out = 0.0f;
+    if (kk != ~0ull) {
+        float e[4], wx, wy, size, nd, lin;
+        if (sprite(v, pos[(unsigned)kk], e, wx, wy, size) && fragment(v, e, wx, wy, size, px, py, nd, lin)) out = nd;
+    }
+    depth[k] = out;
 }
 
-/* pass 3: the owner writes its normalised depth */
-__global__ void k_splat_write(View v, int n, const float4* __restrict__ pos, const int* __restrict__ owner,
-                              float* __restrict__ depth) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float e[4], wx, wy, size;
-    if (!sprite(v, pos[i], e, wx, wy, size)) return;
-    const int x0 = max(0, (int)floorf(wx - 0.5f * size)), x1 = min(v.w - 1, (int)ceilf(wx + 0.5f * size));
-    const int y0 = max(0, (int)floorf(wy - 0.5f * size)), y1 = min(v.h - 1, (int)ceilf(wy + 0.5f * size));
-    for (int py = y0; py <= y1; ++py)
-        for (int px = x0; px <= x1; ++px) {
-            const size_t k = (size_t)py * v.w + px;
-            float nd, lin;
-            if (owner[k] == i && fragment(v, e, wx, wy, size, px, py, nd, lin)) depth[k] = nd;
-        }
-}
-
-__global__ void k_splat_clear(int npix, unsigned* __restrict__ zbuf, int* __restrict__ owner, float* __restrict__ depth) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= npix) return;
-    zbuf[k] = 0x7f800000u;   /* +inf */
-    owner[k] = 0x7fffffff;
-    depth[k] = 0.0f;
+__global__ void k_splat_clear(size_t npix, unsigned long long* __restrict__ key) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < npix) key[k] = ~0ull;
 }
 
 __device__ __forceinline__ float texel(const float* img, int w, int h, int x, int y) {
@@ -279,14 +262,13 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
     v.scale = view->point_scale;
     v.w = view->width;
     v.h = view->height;
-    unsigned* zbuf = reinterpret_cast<unsigned*>(x->render_buf);
-    int* owner = reinterpret_cast<int*>(zbuf + npix);
+    unsigned long long* key = reinterpret_cast<unsigned long long*>(x->render_buf);
     const cudaStream_t s = x->stream;
     const int bs = 256, n = x->N;
-    sph::k_splat_clear<<<(int)((npix + bs - 1) / bs), bs, 0, s>>>((int)npix, zbuf, owner, d_depth);
-    sph::k_splat_depth<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, zbuf);
-    sph::k_splat_owner<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, zbuf, owner);
-    sph::k_splat_write<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, owner, d_depth);
+    const dim3 b2(16, 16);
+    sph::k_splat_clear<<<(unsigned)((npix + bs - 1) / bs), bs, 0, s>>>(npix, key);
+    sph::k_splat_keys<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, key);
+    sph::k_splat_resolve<<<sph::grid2(v.w, v.h, b2), b2, 0, s>>>(v, x->b.pos, key, d_depth);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return sph_ctx_fail(x, SPH_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
     return SPH_OK;

@@ -1,0 +1,89 @@
+"""Host side of the screen-space fluid surface: the camera of scene/camera.cpp and the stage
+sequence of SSpaceFluidRenderer (fluid/render/sspacefluidrenderer.cpp), over the C ABI of
+include/sph_capi.h (sph_render_depth, sph_render_smooth, sph_render_normals).  Images are
+device tensors (torch is only the allocator here); the final shading pass of the reference
+(final_stage.frag: background, cube map, lights) belongs to its GL window and is not part
+of this module.
+"""
+import math
+
+import numpy as np
+
+from . import capi
+
+
+def perspective(fov_deg, aspect, near, far):
+    """QMatrix4x4::perspective as Camera::set_perspective uses it (scene/camera.cpp:32-36),
+    in mathematical (row, column) layout."""
+    f = 1.0 / math.tan(math.radians(fov_deg) / 2.0)
+    m = np.zeros((4, 4), np.float64)
+    m[0, 0] = f / aspect
+    m[1, 1] = f
+    m[2, 2] = -(far + near) / (far - near)
+    m[2, 3] = -2.0 * far * near / (far - near)
+    m[3, 2] = -1.0
+    return m.astype(np.float32)
+
+
+def look_at(eye, center, up):
+    """QMatrix4x4::lookAt: world to eye coordinates, in mathematical layout."""
+    eye, center, up = (np.asarray(a, np.float64) for a in (eye, center, up))
+    f = center - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
+    m[:3, 3] = -m[:3, :3] @ eye
+    return m.astype(np.float32)
+
+
+class Camera:
+    """The reference's default camera (gui/glwidget.cpp:82-88): fov 45 degrees, near 0.5,
+    far 30, aspect = width / height."""
+
+    def __init__(self, width, height, fov=45.0, near=0.5, far=30.0):
+        self.width, self.height = int(width), int(height)
+        self.fov, self.near, self.far = float(fov), float(near), float(far)
+
+    def projection(self):
+        return perspective(self.fov, self.width / max(self.height, 1), self.near, self.far)
+
+    def point_scale(self):
+        """The depth stage's point_scale uniform (sspacefluidrenderer.cpp:366)."""
+        return self.width * math.tan(math.radians(self.fov) * 0.5)
+
+
+class SSpaceFluidRenderer:
+    """Depth, blur and normals stages of SSpaceFluidRenderer::render (:35-53) for one
+    context.  filter_iterations: the blur stage runs the bilateral filter twice per
+    iteration (:390-408).  point_radius: the depth stage's sprite radius (0.0625 in the
+    reference, :365)."""
+
+    def __init__(self, width, height, filter_iterations=2, point_radius=0.125 * 0.5):
+        import torch
+        self.width, self.height = int(width), int(height)
+        self.filter_iterations = int(filter_iterations)
+        self.point_radius = float(point_radius)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.depth = torch.zeros((self.height, self.width), dtype=torch.float32, device=dev)
+        self.blurred = torch.zeros_like(self.depth)
+        self.normals = torch.zeros((self.height, self.width, 4), dtype=torch.float32, device=dev)
+
+    def render(self, ctx, camera, mv_matrix, stream=None):
+        """Renders ctx's fluid particles; returns (depth after the blur stage, normals).
+        stream: the integer cudaStream_t the context runs on (Context.set_stream); all
+        stages are then queued on it.  With None the host waits for the depth stage and the
+        filters run on the default stream."""
+        pr = camera.projection()
+        view = capi.make_view(mv_matrix, pr, self.point_radius, camera.point_scale(), self.width, self.height)
+        ctx.render_depth(view, self.depth.data_ptr())
+        if stream is None:
+            ctx.synchronize()
+        s = int(stream or 0)
+        capi.render_smooth(self.depth.data_ptr(), self.blurred.data_ptr(), self.width, self.height,
+                           self.filter_iterations, s)
+        capi.render_normals(self.depth.data_ptr(), self.normals.data_ptr(), self.width, self.height,
+                            np.linalg.inv(pr.astype(np.float64)).astype(np.float32), s)
+        return self.depth, self.normals

@@ -189,3 +189,25 @@ def test_gpu_normals_match_restatement(gpu_lib):
     torch.cuda.synchronize()
     got = nrm.cpu().numpy()
     assert np.array_equal(got, g["normals"]), describe_mismatch(got, g["normals"])
+
+
+@pytest.mark.gpu
+def test_gpu_renderer_stage_sequence(gpu_lib):
+    """SSpaceFluidRenderer.render: depth, two blur iterations and normals on the context's
+    stream reproduce the golden blurred depth; the normals follow the restatement."""
+    import torch
+    from fluids_gb300 import render
+    g = golden()
+    w, h = int(g["width"]), int(g["height"])
+    ctx = _context(g["pos"])
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    cam = render.Camera(w, h)
+    assert np.array_equal(cam.projection(), g["projection"])
+    r = render.SSpaceFluidRenderer(w, h, filter_iterations=2, point_radius=float(g["point_radius"]))
+    depth, normals = r.render(ctx, cam, g["modelview"], stream.cuda_stream)
+    torch.cuda.synchronize()
+    assert_bilateral("blurred depth", depth.cpu().numpy(), g["smooth2"])
+    want = orender.depth_normals(depth.cpu().numpy(), g["inv_projection"])
+    got = normals.cpu().numpy()
+    assert np.array_equal(got, want), describe_mismatch(got, want)
