@@ -22,6 +22,8 @@ SPH_NEIGH_SCAN, SPH_NEIGH_LIST = 0, 1
 FLAGS = dict(NAN=1, ESCAPED=2, TIMEOUT=4, OVERFLOW=8, NONCONVERGED=16, NONSMOOTH=32)
 STATUS = {0: "SPH_OK", 1: "SPH_E_INVALID", 2: "SPH_E_CUDA", 3: "SPH_E_NONCONVERGED", 4: "SPH_E_ESCAPED",
           5: "SPH_E_NAN", 6: "SPH_E_TIMEOUT", 7: "SPH_E_OVERFLOW", 8: "SPH_E_STATE", 9: "SPH_E_NOMEM"}
+(SPH_OK, SPH_E_INVALID, SPH_E_CUDA, SPH_E_NONCONVERGED, SPH_E_ESCAPED, SPH_E_NAN, SPH_E_TIMEOUT, SPH_E_OVERFLOW,
+ SPH_E_STATE, SPH_E_NOMEM) = range(10)
 STAGES = dict(BOUNDARY_SYNC=0, HASHES=1, SORT=2, SHUFFLE=3, CELL_INTERVALS=4, NEIGH_LIST=5, SB_NEIGH_LIST=6,
               WC_DENSITY=7, NORMALS=8, WC_ACCEL=9, WC_INTEGRATE=10, PCI_INIT_DENSITY=11, PCI_INIT_FORCES=12,
               PCI_LOOP=13, PCI_INTEGRATE=14, BOUNDARY_FORCES=15)
@@ -45,7 +47,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size", "sph_get_field_async",
            "sph_set_field_async",
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
-           "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals"]
+           "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
+           "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere"]
 
 
 class SphParams(C.Structure):
@@ -177,6 +180,10 @@ def lib():
             "sph_render_smooth": (ip, [vp, vp, ip, ip, ip, vp]),
             "sph_filter_curvature_flow": (ip, [vp, vp, ip, ip, C.c_float, C.c_float, vp]),
             "sph_render_normals": (ip, [vp, vp, ip, ip, C.POINTER(C.c_float), vp]),
+            "sph_scene_load_obj": (ip, [C.c_char_p, fp, ip, fp, ip, C.POINTER(ip), C.POINTER(ip)]),
+            "sph_scene_voxelize": (ip, [fp, ip, fp, ip, C.c_float, C.c_float, fp, ip]),
+            "sph_scene_icosphere": (ip, [C.c_float, ip, fp, ip, fp, ip, C.POINTER(ip), C.POINTER(ip)]),
+            "sph_scene_sphere": (ip, [C.c_float, C.c_float, fp, ip]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

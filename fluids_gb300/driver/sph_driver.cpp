@@ -6,18 +6,22 @@
  * without rendering: the settings come from a key=value file (settings/settings.cpp:14-59),
  * the scene from the reference's JSON format -- "container" {width, height, depth} becomes the
  * rectangular limits, "fluid_volumes" of type "box" {size, center} become BoxVolumes, and
- * "rigid_bodies" of type "cube" {size, center, rotation (x, y, z, w quaternion), mass} become
- * boundary bodies (movable when mass > 0, as scene.cpp:471 passes them, and then moved by the
- * solver's own rigid-body step under the fluid's force and torque and gravity; bodies do not
- * collide with each other).  Sphere and mesh bodies are not sampled here (reported and
- * skipped).  Options:
+ * "rigid_bodies" of type "cube" {size, center, rotation (x, y, z, w quaternion), mass},
+ * "sphere" {size (the radius), center, mass} and "model" {obj_filename, center, rotation,
+ * mass} become boundary bodies (movable when mass > 0, as scene.cpp:471 passes them, and then
+ * moved by the solver's own rigid-body step under the fluid's force and torque and gravity;
+ * bodies do not collide with each other).  A model's OBJ path is taken as written when it
+ * exists, else under --data-root, else under the directory two levels above the scene file
+ * (the reference's data/scenes/ layout).  "wall" bodies are reported and skipped.  Options:
  *
  *   sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]
  *              [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]
+ *              [--data-root DIR]
  *
  * Prints one JSON line per K steps with the solver statistics and a final line with the
  * wall-clock throughput.  --dump writes the final positions ordered by particle id (float32
- * x, y, z, w per particle).  --dry-run parses and samples the scene without touching a GPU.
+ * x, y, z, w per particle).  --dry-run parses and samples the scene without touching a GPU
+ * (models are read but not voxelized: their particle counts are not included).
  */
 #include <chrono>
 #include <cmath>
@@ -152,7 +156,25 @@ struct Scene {
     std::vector<std::pair<std::string, std::shared_ptr<RigidBody>>> bodies;
 };
 
-Scene load_scene(const std::string& path, bool container_boundary) {
+bool file_exists(const std::string& p) {
+    std::ifstream f(p);
+    return f.good();
+}
+
+std::string parent_dir(const std::string& p) {
+    const size_t k = p.find_last_of('/');
+    return k == std::string::npos ? std::string(".") : (k == 0 ? std::string("/") : p.substr(0, k));
+}
+
+std::string resolve_model(const std::string& obj, const std::string& scene_path, const std::string& data_root) {
+    if (obj.empty() || obj[0] == '/' || file_exists(obj)) return obj;
+    if (!data_root.empty() && file_exists(data_root + "/" + obj)) return data_root + "/" + obj;
+    const std::string up2 = parent_dir(parent_dir(scene_path));
+    if (file_exists(up2 + "/" + obj)) return up2 + "/" + obj;
+    return obj;
+}
+
+Scene load_scene(const std::string& path, bool container_boundary, const std::string& data_root) {
     const Json j = parse_file(path);
     Scene sc;
     const Json& c = j["container"];
@@ -172,18 +194,24 @@ Scene load_scene(const std::string& path, bool container_boundary) {
             (float)v["center"][0].number(), (float)v["center"][1].number(), (float)v["center"][2].number()));
     }
     for (const Json& r : j["rigid_bodies"].arr) {
-        if (r["type"].str != "cube") {
-            std::fprintf(stderr, "skipping rigid body '%s' of type '%s'\n", r["name"].str.c_str(),
-                         r["type"].str.c_str());
+        const std::string type = r["type"].str;
+        std::shared_ptr<RigidBody> body;
+        if (type == "cube") body = std::make_shared<Cube>((float)r["size"].number());
+        else if (type == "sphere") body = std::make_shared<Sphere>((float)r["size"].number());
+        else if (type == "model")
+            body = std::make_shared<Model>(resolve_model(r["obj_filename"].str, path, data_root));
+        if (!body) {
+            std::fprintf(stderr, "skipping rigid body '%s' of type '%s'\n", r["name"].str.c_str(), type.c_str());
             continue;
         }
-        auto cube = std::make_shared<Cube>((float)r["size"].number());
-        const double q[4] = {r["rotation"][0].number(0), r["rotation"][1].number(0), r["rotation"][2].number(0),
-                             r["rotation"][3].number(1)};
+        /* a sphere has no rotation in the scene format (identity, scene.cpp:418-426) */
+        const bool rot = type != "sphere";
+        const double q[4] = {rot ? r["rotation"][0].number(0) : 0.0, rot ? r["rotation"][1].number(0) : 0.0,
+                             rot ? r["rotation"][2].number(0) : 0.0, rot ? r["rotation"][3].number(1) : 1.0};
         const double ctr[3] = {r["center"][0].number(), r["center"][1].number(), r["center"][2].number()};
-        pose(q, ctr, cube->rot3x4);
-        cube->mass = (float)r["mass"].number();
-        sc.bodies.emplace_back(r["name"].str, cube);
+        pose(q, ctr, body->rot3x4);
+        body->mass = (float)r["mass"].number();
+        sc.bodies.emplace_back(r["name"].str, body);
     }
     return sc;
 }
@@ -206,14 +234,15 @@ class Jittered : public FluidVolume {
 int usage() {
     std::fprintf(stderr,
                  "usage: sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]\n"
-                 "                  [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]\n");
+                 "                  [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]\n"
+                 "                  [--data-root DIR]\n");
     return 2;
 }
 
 }  // namespace
 
 int main(int argc, char** argv) {
-    std::string config, scene_file, dump, mode = "physics";
+    std::string config, scene_file, dump, mode = "physics", data_root;
     int steps = 100, every = 0;
     bool dry = false, container_boundary = false;
     long long jitter = -1;
@@ -233,6 +262,7 @@ int main(int argc, char** argv) {
             else if (k == "--jitter") jitter = std::atoll(next().c_str());
             else if (k == "--container-boundary") container_boundary = true;
             else if (k == "--dry-run") dry = true;
+            else if (k == "--data-root") data_root = next();
             else return usage();
         } catch (const Error& e) {
             std::fprintf(stderr, "%s\n", e.what());
@@ -244,18 +274,22 @@ int main(int argc, char** argv) {
         PhysicsSettings phys;
         SimulationSettings sim;
         load_settings(config, phys, sim);
-        Scene sc = load_scene(scene_file, container_boundary);
+        Scene sc = load_scene(scene_file, container_boundary, data_root);
         if (jitter >= 0)
             for (size_t v = 0; v < sc.volumes.size(); ++v)
                 sc.volumes[v] = std::make_shared<Jittered>(sc.volumes[v], (uint64_t)jitter + v);
         if (dry) {
-            size_t nf = 0, nb = 0;
+            size_t nf = 0, nb = 0, ndev = 0;
             for (auto& v : sc.volumes) nf += v->particles(sim.fluid_particle_radius).size();
-            for (auto& b : sc.bodies) nb += b.second->surface_sampling(2.0f * sim.fluid_particle_radius).size();
+            for (auto& b : sc.bodies) {
+                if (b.second->samples_on_device()) ++ndev;
+                else nb += b.second->surface_sampling(2.0f * sim.fluid_particle_radius).size();
+            }
             std::printf("{\"method\": \"%s\", \"time_step\": %g, \"particles\": %zu, \"boundary_particles\": %zu, "
-                        "\"volumes\": %zu, \"bodies\": %zu, \"container\": [%g, %g, %g]}\n",
+                        "\"volumes\": %zu, \"bodies\": %zu, \"device_sampled_bodies\": %zu, "
+                        "\"container\": [%g, %g, %g]}\n",
                         sim.sim_method == SimulationSettings::PCISPH ? "pcisph" : "wcsph", sim.time_step, nf, nb,
-                        sc.volumes.size(), sc.bodies.size(), sc.container[0], sc.container[1], sc.container[2]);
+                        sc.volumes.size(), sc.bodies.size(), ndev, sc.container[0], sc.container[1], sc.container[2]);
             return 0;
         }
         DeviceOptions opt;

@@ -1,8 +1,9 @@
 """Scene objects of the reference (fluid volumes and rigid bodies) for the headless driver.
 
-``BoxVolume.particles``, ``FishTank.surface_sampling`` and ``Cube.surface_sampling`` call the
-C-ABI samplers that restate fluid/simulation/boxvolume.cpp:11-40, scene/fishtank.cpp:108-141
-and scene/cube.cpp:136-171.  ``jitter`` is the seeded splitmix64 jitter of the benchmark
+``BoxVolume.particles``, ``FishTank.surface_sampling``, ``Cube.surface_sampling``,
+``Sphere.surface_sampling`` and ``Model.surface_sampling`` call the C-ABI samplers that restate
+fluid/simulation/boxvolume.cpp:11-40, scene/fishtank.cpp:108-141, scene/cube.cpp:136-171,
+scene/sphere.cpp:135-171 and scene/model.cpp:170-214 (the last on the GPU).  ``jitter`` is the seeded splitmix64 jitter of the benchmark
 scenes.  The BASELINE-style scenes (dam breaks, the rotated cube) are built by ``make_scene``.
 """
 import math
@@ -79,6 +80,71 @@ class Cube(RigidBody):
 
     def surface_sampling(self, spacing):
         return _sample(capi.lib().sph_scene_cube, self.side, float(spacing))
+
+
+def load_obj(path):
+    """ModelMesh(path) (sph_scene_load_obj): (vertices (n, 3) float32, indices (m,) uint32)."""
+    L = capi.lib()
+    nv, ni = capi.C.c_int(), capi.C.c_int()
+    capi.check(L.sph_scene_load_obj(str(path).encode(), None, 0, None, 0, capi.C.byref(nv), capi.C.byref(ni)))
+    v = np.zeros((nv.value, 3), np.float32)
+    ix = np.zeros(ni.value, np.uint32)
+    capi.check(L.sph_scene_load_obj(str(path).encode(), capi.ptr(v), nv.value, capi.ptr(ix), ni.value,
+                                    capi.C.byref(nv), capi.C.byref(ni)))
+    return v, ix
+
+
+def voxelize(vertices3, indices, voxel_size, precision=None):
+    """sph_scene_voxelize (GPU): the 8 corners of every voxel the mesh touches, (n, 4)."""
+    L = capi.lib()
+    v = np.ascontiguousarray(vertices3, np.float32).reshape(-1, 3)
+    ix = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+    prec = float(voxel_size) / 10.0 if precision is None else float(precision)
+    args = (capi.ptr(v), len(v), capi.ptr(ix), len(ix), float(voxel_size), prec)
+    n = L.sph_scene_voxelize(*args, None, 0)
+    if n < 0:
+        raise capi.SphError(-n, "sph_scene_voxelize")
+    out = np.zeros((n, 4), np.float32)
+    if n:
+        capi.check(min(0, L.sph_scene_voxelize(*args, capi.ptr(out), n)))
+    return out
+
+
+def icosphere(radius, level):
+    """IcoSphereMesh(radius, level): (vertices (n, 3), indices (m,))."""
+    L = capi.lib()
+    nv, ni = capi.C.c_int(), capi.C.c_int()
+    capi.check(L.sph_scene_icosphere(float(radius), int(level), None, 0, None, 0, capi.C.byref(nv),
+                                     capi.C.byref(ni)))
+    v = np.zeros((nv.value, 3), np.float32)
+    ix = np.zeros(ni.value, np.uint32)
+    capi.check(L.sph_scene_icosphere(float(radius), int(level), capi.ptr(v), nv.value, capi.ptr(ix), ni.value,
+                                     capi.C.byref(nv), capi.C.byref(ni)))
+    return v, ix
+
+
+class Sphere(RigidBody):
+    """scene/sphere.h: a sphere of radius ``radius`` (the scene files' "size"), sampled from a
+    level-3 icosphere."""
+
+    def __init__(self, radius, mass=0.0, position=(0, 0, 0)):
+        super().__init__(mass, position)
+        self.radius = float(radius)
+
+    def surface_sampling(self, spacing):
+        return _sample(capi.lib().sph_scene_sphere, self.radius, float(spacing))
+
+
+class Model(RigidBody):
+    """scene/model.h: a triangle mesh read from an OBJ file, sampled by voxelizing it on the
+    GPU (voxel size = particle spacing, precision = spacing / 10)."""
+
+    def __init__(self, obj_filename, mass=0.0, position=(0, 0, 0), rotation=None):
+        super().__init__(mass, position, rotation)
+        self.vertices, self.indices = load_obj(obj_filename)
+
+    def surface_sampling(self, spacing):
+        return voxelize(self.vertices, self.indices, float(spacing), float(spacing) / 10.0)
 
 
 def rotation_y(theta):

@@ -361,6 +361,31 @@ int sph_scene_box_volume(const float size3[3], const float center3[3], float par
 int sph_scene_fishtank(float width, float height, float depth, float spacing, float* out4, int cap);
 /* Cube::surface_sampling (scene/cube.cpp:136-171): hollow cube shell in body coordinates. */
 int sph_scene_cube(float side, float spacing, float* out4, int cap);
+/* ModelMesh(path) (mesh/modelmesh.cpp:16-88): reads an OBJ file (v / vn / f records,
+ * polygons split into triangle fans as tinyobj does) into one vertex per distinct
+ * (position, normal) reference and a triangle index list.  Indices keep only their low 16
+ * bits, as the reference's unsigned-short mesh_index does.  Writes *nvertices and
+ * *nindices always, the arrays when vcap / icap suffice.  SPH_E_INVALID when the file cannot
+ * be read or a face references a missing vertex. */
+int sph_scene_load_obj(const char* path, float* vertices3, int vcap, uint32_t* indices, int icap, int* nvertices,
+                       int* nindices);
+/* Model::surface_sampling (scene/model.cpp:170-214) on the GPU: the vendored voxelizer's
+ * vx_voxelize (external/voxelizer/voxelizer.h) of the triangle mesh with cubic voxels of
+ * voxel_size (the reference passes the particle spacing and precision = spacing / 10);
+ * writes the 8 corners of every voxel, in the voxelizer's output order, as float4 (w = 1).
+ * Returns the particle count (8 per voxel); writes nothing when out4 is NULL or cap is
+ * below the count.  Negative SPH_E_* on error (SPH_E_OVERFLOW: a triangle spans more than
+ * 2^24 voxels or the mesh more than 2^30 voxel hits).  Synchronous. */
+int sph_scene_voxelize(const float* vertices3, int nvertices, const uint32_t* indices, int nindices,
+                       float voxel_size, float precision, float* out4, int cap);
+/* IcoSphereMesh(radius, level) (mesh/icospheremesh.cpp:10-124), level 0..4. */
+int sph_scene_icosphere(float radius, int level, float* vertices3, int vcap, uint32_t* indices, int icap,
+                        int* nvertices, int* nindices);
+/* Sphere::surface_sampling (scene/sphere.cpp:135-171) of IcoSphereMesh(radius, 3): random
+ * points on each triangle (a default-seeded std::default_random_engine per triangle), then
+ * every mesh vertex; the corner reads and the area formula as written there.  Returns the
+ * count, fills out4 up to cap. */
+int sph_scene_sphere(float radius, float spacing, float* out4, int cap);
 /* Adds U(-amp, amp) to x, y, z of every particle from a splitmix64 stream seeded by seed. */
 void sph_jitter(float* pos4, int n, float amp, uint64_t seed);
 

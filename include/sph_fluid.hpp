@@ -18,6 +18,8 @@
  */
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <fstream>
@@ -165,6 +167,8 @@ class RigidBody {
      * centre kept to the container walls; used when the body has mass and can move. */
     virtual void inverse_inertia(float out[3]) const { out[0] = out[1] = out[2] = 0.f; }
     virtual float bounding_radius() const { return 0.f; }
+    /* true when surface_sampling runs on the GPU */
+    virtual bool samples_on_device() const { return false; }
     float mass = 0.f;
     float rot3x4[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
     float linear_velocity[4] = {0, 0, 0, 0};
@@ -205,6 +209,84 @@ class Cube : public RigidBody {
 
    private:
     float side_;
+};
+
+/* Sphere (scene/sphere.cpp:8-13,135-171): level-3 icosphere sampling; inertia of a solid
+ * sphere, 0.4 m r^2 (btSphereShape). */
+class Sphere : public RigidBody {
+   public:
+    explicit Sphere(float radius) : r_(radius) {}
+    void inverse_inertia(float out[3]) const override {
+        const float v = mass > 0.f ? 1.0f / (0.4f * mass * r_ * r_) : 0.f;
+        out[0] = out[1] = out[2] = v;
+    }
+    float bounding_radius() const override { return r_; }
+    std::vector<Float4> surface_sampling(float spacing) const override {
+        const int n = sph_scene_sphere(r_, spacing, nullptr, 0);
+        std::vector<Float4> out((size_t)(n > 0 ? n : 0));
+        if (n > 0) sph_scene_sphere(r_, spacing, &out[0].x, n);
+        return out;
+    }
+
+   private:
+    float r_;
+};
+
+/* Model (scene/model.cpp:11-214): an OBJ mesh read as ModelMesh does, sampled by voxelizing
+ * it on the GPU (voxel size = spacing, precision = spacing / 10).  Inertia: the box of the
+ * mesh's bounding box, I = m / 12 (ly^2 + lz^2, lx^2 + lz^2, lx^2 + ly^2) -- Bullet's
+ * approximation for convex hulls (btPolyhedralConvexShape) without its collision margin. */
+class Model : public RigidBody {
+   public:
+    explicit Model(const std::string& obj_filename) {
+        int nv = 0, ni = 0;
+        int rc = sph_scene_load_obj(obj_filename.c_str(), nullptr, 0, nullptr, 0, &nv, &ni);
+        if (rc == SPH_OK) {
+            v_.resize(3 * (size_t)nv);
+            ix_.resize((size_t)ni);
+            rc = sph_scene_load_obj(obj_filename.c_str(), v_.data(), nv, ix_.data(), ni, &nv, &ni);
+        }
+        if (rc != SPH_OK) throw Error(rc, "could not load model: " + obj_filename);
+    }
+    int vertex_count() const { return (int)(v_.size() / 3); }
+    int triangle_count() const { return (int)(ix_.size() / 3); }
+    void inverse_inertia(float out[3]) const override {
+        float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+        for (size_t i = 0; i < v_.size(); ++i) {
+            const int a = (int)(i % 3);
+            if (i < 3 || v_[i] < lo[a]) lo[a] = v_[i];
+            if (i < 3 || v_[i] > hi[a]) hi[a] = v_[i];
+        }
+        const float l2[3] = {(hi[0] - lo[0]) * (hi[0] - lo[0]), (hi[1] - lo[1]) * (hi[1] - lo[1]),
+                             (hi[2] - lo[2]) * (hi[2] - lo[2])};
+        const float I[3] = {mass / 12.f * (l2[1] + l2[2]), mass / 12.f * (l2[0] + l2[2]),
+                            mass / 12.f * (l2[0] + l2[1])};
+        for (int a = 0; a < 3; ++a) out[a] = I[a] > 0.f ? 1.0f / I[a] : 0.f;
+    }
+    float bounding_radius() const override {
+        float r2 = 0.f;
+        for (size_t i = 0; i + 2 < v_.size(); i += 3)
+            r2 = std::max(r2, v_[i] * v_[i] + v_[i + 1] * v_[i + 1] + v_[i + 2] * v_[i + 2]);
+        return std::sqrt(r2);
+    }
+    bool samples_on_device() const override { return true; }
+    std::vector<Float4> surface_sampling(float spacing) const override {
+        const float precision = spacing / 10;
+        const int n = sph_scene_voxelize(v_.data(), vertex_count(), ix_.data(), (int)ix_.size(), spacing, precision,
+                                         nullptr, 0);
+        if (n < 0) throw Error(-n, "model voxelization failed");
+        std::vector<Float4> out((size_t)n);
+        if (n > 0) {
+            const int m = sph_scene_voxelize(v_.data(), vertex_count(), ix_.data(), (int)ix_.size(), spacing,
+                                             precision, &out[0].x, n);
+            if (m != n) throw Error(m < 0 ? -m : SPH_E_CUDA, "model voxelization failed");
+        }
+        return out;
+    }
+
+   private:
+    std::vector<float> v_;
+    std::vector<uint32_t> ix_;
 };
 
 /* FluidSimulation (fluid/simulation/fluidsimulation.h:23-92): same methods. */

@@ -2,7 +2,8 @@
 # Builds oracle/_ref/libref_kernels.so: the reference's own OpenCL kernels
 # (kernels/grid.cl, wcsph.cl, normals.cl, pcisph.cl, boundary.cl, bilateral.cl,
 # curvatureflow.cl and their headers)
-# compiled for the CPU through oracle/ref_shim/clshim.hpp.  Used only to pin the oracle
+# compiled for the CPU through oracle/ref_shim/clshim.hpp, and its mesh code
+# (mesh/modelmesh.cpp, mesh/icospheremesh.cpp, external/voxelizer/voxelizer.h).  Used only to pin the oracle
 # and to generate tests/golden/ fixtures, in a container where the reference is mounted.
 #
 # The one source transformation rewrites OpenCL vector literals "(int4)(" / "(float4)("
@@ -28,6 +29,15 @@ for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary r
     "$CXX" "${flags[@]}" -c "$here/ref_shim/$u.cpp" -o "$out/obj/$u.o" &
     pids+=($!)
 done
+# the mesh code (mesh/modelmesh.cpp with the vendored tinyobj, mesh/icospheremesh.cpp and
+# the vendored voxelizer) compiles from its own sources under the reference root
+mflags=(-O1 -std=c++17 -fPIC -ffp-contract=off -w -I "$here/ref_shim" -I "$ref")
+"$CXX" "${mflags[@]}" -c "$ref/mesh/modelmesh.cpp" -o "$out/obj/ref_modelmesh.o" &
+pids+=($!)
+"$CXX" "${mflags[@]}" -c "$ref/mesh/icospheremesh.cpp" -o "$out/obj/ref_icospheremesh.o" &
+pids+=($!)
+"$CXX" "${mflags[@]}" -c "$here/ref_shim/ref_mesh.cpp" -o "$out/obj/ref_mesh.o" &
+pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 "$CXX" -shared -o "$out/libref_kernels.so" "$out"/obj/*.o
 echo "build_ref: built $out/libref_kernels.so"

@@ -214,3 +214,33 @@ def curvature_flow(depth, inv_proj_x, inv_proj_y):
     out = np.zeros_like(img)
     lib().ref_curvature_flow(P(img), P(out), i(img.shape[1]), i(img.shape[0]), f(inv_proj_x), f(inv_proj_y))
     return out
+
+
+def load_obj(path):
+    """ModelMesh(path): (vertices (n, 3) float32, indices (m,) uint32 holding its 16-bit values)."""
+    nv, ni = C.c_int(), C.c_int()
+    if lib().ref_load_obj(path.encode(), None, 0, None, 0, C.byref(nv), C.byref(ni)) != 0:
+        raise RuntimeError("ModelMesh could not load " + path)
+    v = np.zeros((nv.value, 3), np.float32)
+    ix = np.zeros(ni.value, np.uint32)
+    lib().ref_load_obj(path.encode(), P(v), nv, P(ix), ni, C.byref(nv), C.byref(ni))
+    return v, ix
+
+
+def voxelize(vertices3, indices, spacing, precision):
+    """vx_voxelize as Model::surface_sampling calls it: (n, 4) float32 output vertices."""
+    v = np.ascontiguousarray(vertices3, np.float32)
+    ix = np.ascontiguousarray(indices, np.uint32)
+    n = lib().ref_voxelize(P(v), i(len(v)), P(ix), i(len(ix)), f(spacing), f(precision), None, i(0))
+    out = np.zeros((n, 4), np.float32)
+    lib().ref_voxelize(P(v), i(len(v)), P(ix), i(len(ix)), f(spacing), f(precision), P(out), i(n))
+    return out
+
+
+def icosphere(radius, level):
+    nv, ni = C.c_int(), C.c_int()
+    lib().ref_icosphere(f(radius), C.c_uint(level), None, 0, None, 0, C.byref(nv), C.byref(ni))
+    v = np.zeros((nv.value, 3), np.float32)
+    ix = np.zeros(ni.value, np.uint32)
+    lib().ref_icosphere(f(radius), C.c_uint(level), P(v), nv, P(ix), ni, C.byref(nv), C.byref(ni))
+    return v, ix

@@ -5,6 +5,7 @@ mounted:
     python tests/golden/make_golden.py
 
     python tests/golden/make_golden.py render    # only render_small.npz
+    python tests/golden/make_golden.py mesh      # only voxel_teapot.npz
 
 Every stage output is produced by chaining reference kernels only (the key sort is the
 stable ascending sort clogs performs, numpy's stable argsort; the shuffle is a gather).  The
@@ -168,13 +169,30 @@ def render_fixture():
     print("wrote render_small.npz", os.path.getsize(path), "bytes; covered", float((depth != 0).mean()))
 
 
+def mesh_fixture():
+    """Model::surface_sampling of the reference's teapot (data/models/teapot.obj read by its
+    own ModelMesh) at particle spacing 0.03: the voxelizer's output list, in its order."""
+    from oracle.refkernels import REFERENCE_ROOT
+    v, ix = rk.load_obj(os.path.join(REFERENCE_ROOT, "data", "models", "teapot.obj"))
+    spacing = np.float32(0.03)
+    out = rk.voxelize(v, ix, spacing, np.float32(spacing / np.float32(10)))
+    path = os.path.join(HERE, "voxel_teapot.npz")
+    np.savez_compressed(path, vertices=v, indices=ix, spacing=spacing, precision=np.float32(spacing / np.float32(10)),
+                        out=out)
+    print("wrote voxel_teapot.npz", os.path.getsize(path), "bytes;", len(out), "particles")
+
+
 def main():
     if rk.build() is None:
         raise SystemExit("the reference kernels are not available here")
     if sys.argv[1:] == ["render"]:
         render_fixture()
         return
+    if sys.argv[1:] == ["mesh"]:
+        mesh_fixture()
+        return
     render_fixture()
+    mesh_fixture()
     sc = small_scene()
     out, kw, d = wcsph(sc)
     save("wcsph_compat_small.npz", sc, out, kw, d)

@@ -10,7 +10,8 @@ import pytest
 
 import fluids_gb300
 from fluids_gb300 import capi
-from fluids_gb300.scenes import BoxVolume, Cube, FishTank
+from fluids_gb300 import scenes
+from fluids_gb300.scenes import BoxVolume, Cube, FishTank, Sphere
 
 CONFIG = """# Simulation settings
 time_step=0.0002
@@ -56,9 +57,10 @@ def test_driver_parses_reference_formats(driver, tmp_path):
     assert r.returncode == 0, r.stderr
     out = json.loads(r.stdout)
     n = len(BoxVolume((0.24, 0.3, 0.2), (0.15, -0.14, 0.0)).particles(0.0075))
-    nb = len(FishTank(0.6, 0.6, 0.4).surface_sampling(0.015)) + len(Cube(0.1).surface_sampling(0.015))
+    nb = (len(FishTank(0.6, 0.6, 0.4).surface_sampling(0.015)) + len(Cube(0.1).surface_sampling(0.015)) +
+          len(Sphere(0.05).surface_sampling(0.015)))
     assert out["particles"] == n and out["boundary_particles"] == nb
-    assert out["method"] == "wcsph" and out["bodies"] == 2 and "sphere" in r.stderr
+    assert out["method"] == "wcsph" and out["bodies"] == 3 and out["device_sampled_bodies"] == 0
 
 
 def test_driver_rejects_incomplete_settings(driver, tmp_path):
@@ -90,6 +92,8 @@ def test_driver_matches_python_api(gpu_lib, driver, tmp_path):
     ctx.add_boundary(FishTank(0.6, 0.6, 0.4).surface_sampling(0.015))
     cube = Cube(0.1, position=(-0.15, -0.24, 0.0))
     ctx.add_boundary(cube.surface_sampling(0.015), rot3x4=cube.rot3x4())
+    ball = Sphere(0.05)
+    ctx.add_boundary(ball.surface_sampling(0.015), rot3x4=ball.rot3x4())
     ctx.add_volume(BoxVolume((0.24, 0.3, 0.2), (0.15, -0.14, 0.0)).particles(0.0075))
     ctx.simulate(steps)
     ctx.synchronize()
@@ -118,3 +122,67 @@ def test_driver_moves_bodies_with_mass(gpu_lib, driver, tmp_path):
     dt, g = np.float32(2e-4), 9.81
     for n, yy in zip((50, 100), y):
         assert yy == pytest.approx(0.1 - g * dt * dt * n * (n + 1) / 2, abs=1e-5)
+
+
+CUBE_OBJ = """# a closed cube of side 0.1 centred at the origin
+v -0.05 -0.05 -0.05
+v 0.05 -0.05 -0.05
+v 0.05 0.05 -0.05
+v -0.05 0.05 -0.05
+v -0.05 -0.05 0.05
+v 0.05 -0.05 0.05
+v 0.05 0.05 0.05
+v -0.05 0.05 0.05
+f 1 3 2
+f 1 4 3
+f 5 6 7
+f 5 7 8
+f 1 2 6
+f 1 6 5
+f 4 8 7
+f 4 7 3
+f 1 5 8
+f 1 8 4
+f 2 3 7
+f 2 7 6
+"""
+
+
+def model_scene(tmp_path, mass):
+    (tmp_path / "models").mkdir(exist_ok=True)
+    (tmp_path / "models" / "box.obj").write_text(CUBE_OBJ)
+    return {"container": {"width": 0.6, "height": 0.6, "depth": 0.4},
+            "fluid_volumes": [{"type": "box", "name": "f", "size": [0.12, 0.12, 0.12], "center": [0.2, -0.2, 0.0]}],
+            "rigid_bodies": [{"type": "model", "name": "box", "obj_filename": "models/box.obj", "mass": mass,
+                              "center": [-0.15, 0.1, 0.0], "rotation": [0, 1, 0, 0.5]}]}
+
+
+def test_driver_reads_model_bodies(driver, tmp_path):
+    """A "model" body is read from its OBJ file (found under --data-root); its voxel
+    sampling runs on the GPU, so a dry run reports it without sampling it."""
+    c, s = write(tmp_path, scene=model_scene(tmp_path, 0.0))
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run", "--data-root", str(tmp_path)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = json.loads(r.stdout)
+    assert out["bodies"] == 1 and out["device_sampled_bodies"] == 1 and out["boundary_particles"] == 0
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run", "--data-root", str(tmp_path / "none")],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "models/box.obj" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_runs_model_scene(gpu_lib, driver, tmp_path):
+    """The voxel-sampled model with mass falls freely as a dynamic body."""
+    c, s = write(tmp_path, scene=model_scene(tmp_path, 0.5))
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--steps", "100", "--every", "50",
+                        "--data-root", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(x) for x in r.stdout.splitlines()]
+    v, ix = scenes.load_obj(str(tmp_path / "models" / "box.obj"))
+    assert lines[-1]["boundary_particles"] == len(scenes.voxelize(v, ix, 0.015, 0.0015))
+    y = [x["bodies"]["box"][1] for x in lines[:-1]]
+    dt, g = np.float32(2e-4), 9.81
+    for n, yy in zip((50, 100), y):
+        assert yy == pytest.approx(0.1 - g * dt * dt * n * (n + 1) / 2, abs=1e-5)
+    assert lines[-1]["flags"] == 0
