@@ -19,7 +19,7 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libsph_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["sph_sort.cu", "sph_grid.cu", "sph_wcsph.cu", "sph_pcisph.cu", "sph_boundary.cu", "sph_context.cu",
-           "sph_scene.cpp", "sph_sort_noalloc.cu", "sph_adjoint.cu", "sph_render.cu", "sph_mesh.cu"]
+           "sph_scene.cpp", "sph_sort_noalloc.cu", "sph_adjoint.cu", "sph_render.cu", "sph_mesh.cu", "sph_state.cu"]
 # The screen-space surface and voxelizer kernels round every multiply and add separately (no
 # FMA contraction) so their images and voxels are reproducible operation for operation; the
 # host scene builders likewise, so Arm and x86 hosts sample the same particles.

@@ -48,7 +48,7 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_set_field_async",
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
            "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
-           "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere"]
+           "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere", "sph_save_state", "sph_load_state"]
 
 
 class SphParams(C.Structure):
@@ -184,6 +184,8 @@ def lib():
             "sph_scene_voxelize": (ip, [fp, ip, fp, ip, C.c_float, C.c_float, fp, ip]),
             "sph_scene_icosphere": (ip, [C.c_float, ip, fp, ip, fp, ip, C.POINTER(ip), C.POINTER(ip)]),
             "sph_scene_sphere": (ip, [C.c_float, C.c_float, fp, ip]),
+            "sph_save_state": (ip, [vp, C.c_char_p]),
+            "sph_load_state": (ip, [vp, C.c_char_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -369,6 +371,14 @@ class Context:
         ang = np.zeros(4, np.float32)
         self._c(self._lib.sph_get_body_state(self.h, int(body), ptr(rot), ptr(lin), ptr(ang)))
         return rot.reshape(3, 4), lin[:3], ang[:3]
+
+    def save_state(self, path):
+        """Checkpoint (sph_save_state)."""
+        self._c(self._lib.sph_save_state(self.h, str(path).encode()))
+
+    def load_state(self, path):
+        """Resume from a checkpoint into a context built from the same scene (sph_load_state)."""
+        self._c(self._lib.sph_load_state(self.h, str(path).encode()))
 
     def render_depth(self, view, d_depth):
         """sph_render_depth into the device image at address d_depth (view: SphView)."""

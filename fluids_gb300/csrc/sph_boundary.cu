@@ -11,8 +11,10 @@
  *                    the same set (r^2 < h^2) in O(n), summed in cell order.
  *   k_bnd_forces     compute_fluid_force (boundary.cl:61-118) + clsum (clreduce.h:74-86): the
  *                    pressure force of the fluid on each particle of a body with mass > 0 and
- *                    its torque about the body centre, reduced per body with warp shuffles and
- *                    one atomic per warp (no host read per body as in
+ *                    its torque about the body centre, one record per boundary particle;
+ *   k_body_sum       the per-body sums of those records (one block per body, a fixed
+ *                    strided order and a fixed tree), so a body's force -- and the motion of a
+ *                    dynamic body -- is the same on every run (no host read per body as in
  *                    boundaryhandler.cpp:338-346).
  *   k_stats          density error, kinetic/potential energy and centre of mass.
  */
@@ -81,8 +83,7 @@ __global__ void k_bnd_forces(Const c, int nb, const float4* __restrict__ bpos, c
                              const int32_t* __restrict__ body, const int32_t* __restrict__ range,
                              const float* __restrict__ xf, const float4* __restrict__ spos,
                              const float* __restrict__ dens, const float* __restrict__ pres,
-                             const int2* __restrict__ tab, float4* __restrict__ body_force,
-                             float4* __restrict__ body_torque) {
+                             const int2* __restrict__ tab, float4* __restrict__ bft) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < nb;
     int bi = -1;
@@ -126,32 +127,38 @@ __global__ void k_bnd_forces(Const c, int nb, const float4* __restrict__ bpos, c
         ty = ez * fx - ex * fz;
         tz = ex * fy - ey * fx;
     }
-    /* warp reduction when the warp's particles belong to one body, else one atomic each */
-    const unsigned active = __activemask();
-    const int b0 = __shfl_sync(active, bi, __ffs(active) - 1);
-    const bool uniform = __all_sync(active, bi == b0);
-    if (uniform) {
-        if (b0 < 0) return;
+    if (live) {
+        bft[2 * (size_t)i] = make_float4(fx, fy, fz, 0.f);
+        bft[2 * (size_t)i + 1] = make_float4(tx, ty, tz, 0.f);
+    }
+}
+
+/* One block per body: thread t sums records origin + t, origin + t + 256, ... in order, then
+ * a fixed tree over the 256 partial sums. */
+__global__ void __launch_bounds__(256) k_body_sum(const int32_t* __restrict__ range, const float4* __restrict__ bft,
+                                                  float4* __restrict__ body_force, float4* __restrict__ body_torque) {
+    __shared__ float part[6][256];
+    const int b = blockIdx.x, t = threadIdx.x;
+    const int origin = range[4 * b], count = range[4 * b + 1];
+    float a[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (range[4 * b + 3] != 0)
+        for (int k = t; k < count; k += 256) {
+            const float4 f = bft[2 * (size_t)(origin + k)], q = bft[2 * (size_t)(origin + k) + 1];
+            a[0] += f.x; a[1] += f.y; a[2] += f.z;
+            a[3] += q.x; a[4] += q.y; a[5] += q.z;
+        }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(0xffffffffu, fx, o);
-            fy += __shfl_xor_sync(0xffffffffu, fy, o);
-            fz += __shfl_xor_sync(0xffffffffu, fz, o);
-            tx += __shfl_xor_sync(0xffffffffu, tx, o);
-            ty += __shfl_xor_sync(0xffffffffu, ty, o);
-            tz += __shfl_xor_sync(0xffffffffu, tz, o);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            float* f = reinterpret_cast<float*>(&body_force[b0]);
-            float* q = reinterpret_cast<float*>(&body_torque[b0]);
-            atomicAdd(f, fx); atomicAdd(f + 1, fy); atomicAdd(f + 2, fz);
-            atomicAdd(q, tx); atomicAdd(q + 1, ty); atomicAdd(q + 2, tz);
-        }
-    } else if (bi >= 0) {
-        float* f = reinterpret_cast<float*>(&body_force[bi]);
-        float* q = reinterpret_cast<float*>(&body_torque[bi]);
-        atomicAdd(f, fx); atomicAdd(f + 1, fy); atomicAdd(f + 2, fz);
-        atomicAdd(q, tx); atomicAdd(q + 1, ty); atomicAdd(q + 2, tz);
+    for (int k = 0; k < 6; ++k) part[k][t] = a[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) part[k][t] += part[k][t + w];
+        __syncthreads();
+    }
+    if (t == 0) {
+        body_force[b] = make_float4(part[0][0], part[1][0], part[2][0], 0.f);
+        body_torque[b] = make_float4(part[3][0], part[4][0], part[5][0], 0.f);
     }
 }
 
@@ -360,10 +367,9 @@ void launch_body_integrate(cudaStream_t s, const Const& c, const Bufs& b, int nb
 
 void launch_bnd_forces(cudaStream_t s, const Const& c, const Bufs& b, int nbodies, int bs) {
     if (c.nb <= 0 || nbodies <= 0) return;
-    cudaMemsetAsync(b.body_force, 0, sizeof(float4) * nbodies, s);
-    cudaMemsetAsync(b.body_torque, 0, sizeof(float4) * nbodies, s);
     k_bnd_forces<<<nblk(c.nb, bs), bs, 0, s>>>(c, c.nb, b.bpos, b.bphi, b.bbody, b.body_range, b.body_xf, b.pos_s,
-                                               b.density, b.pressure, b.tab, b.body_force, b.body_torque);
+                                               b.density, b.pressure, b.tab, b.bft);
+    k_body_sum<<<nbodies, 256, 0, s>>>(b.body_range, b.bft, b.body_force, b.body_torque);
 }
 void launch_stats(cudaStream_t s, const Const& c, const Bufs& b) {
     cudaMemsetAsync(b.stats, 0, 8 * sizeof(double), s);

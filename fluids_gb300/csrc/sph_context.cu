@@ -259,6 +259,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.body_xf = cv.take<float>(20 * nbod);
     b.body_range = cv.take<int32_t>(4 * nbod);
     b.body_force = cv.take<float4>(nbod); b.body_torque = cv.take<float4>(nbod);
+    b.bft = cv.take<float4>(2 * nb);
     b.body_dyn = cv.take<float>(8 * nbod);
     b.flags = cv.take<unsigned>(4);
     b.pci_iters = cv.take<int32_t>(4);

@@ -43,6 +43,7 @@ struct Bufs {
     float* body_xf;                        /* 20 floats per body: rot3x4, lin4, ang4 */
     int32_t* body_range;                   /* origin, count, can_move, has_mass per body */
     float4 *body_force, *body_torque;
+    float4* bft;                           /* 2 per boundary particle: its fluid force and torque */
     float* body_dyn;                       /* 8 floats per body: dynamic, mass, inv inertia xyz, radius */
     /* batched contexts: scene table and the scene of each fluid particle (ranges never move) */
     const SceneDev* scenes;

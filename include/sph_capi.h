@@ -294,6 +294,20 @@ int sph_adj_flags(sph_adj* adj, unsigned* flags);
 /* Device bytes the adjoint holds (checkpoints, one segment's tape, scratch). */
 int sph_adj_tape_bytes(const sph_adj* adj, size_t* bytes);
 
+/* ---- checkpoint / resume -------------------------------------------------------------- */
+
+/* No counterpart in the reference (reset() rebuilds from the scene,
+ * pcisphsimluation.cpp:257-266).  Writes what the next step reads: fluid positions,
+ * velocities, half-step velocities and particle ids in the context's current order, every
+ * body's transform, velocities and dynamics, with the parameters, container and counts, and
+ * a checksum.  Synchronises.  Not for batched contexts (SPH_E_STATE). */
+int sph_save_state(sph_ctx* ctx, const char* path);
+/* Restores a sph_save_state file into a context built from the same scene (same parameters
+ * but for block_size / use_graph, container, fluid count, bodies and their particle counts;
+ * SPH_E_INVALID otherwise, and for a damaged file).  The steps that follow are bit-identical
+ * to the steps that followed the save. */
+int sph_load_state(sph_ctx* ctx, const char* path);
+
 /* ---- screen-space surface ------------------------------------------------------------ */
 
 /* The depth, blur and normals stages of SSpaceFluidRenderer (fluid/render/

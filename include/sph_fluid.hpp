@@ -433,6 +433,9 @@ class CudaFluidSimulation : public FluidSimulation {
         return f;
     }
     void synchronize() { check(sph_synchronize(ctx_), ctx_); }
+    /* checkpoint / resume (sph_save_state / sph_load_state) */
+    void save_state(const std::string& path) { check(sph_save_state(ctx_, path.c_str()), ctx_); }
+    void load_state(const std::string& path) { check(sph_load_state(ctx_, path.c_str()), ctx_); }
     sph_ctx* handle() { return ctx_; }
 
    private:
