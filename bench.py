@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["wcsph4m", "wcsph65k", "pcisph"], default="wcsph4m")
+    ap.add_argument("--workload", choices=["wcsph4m", "wcsph1m", "wcsph65k", "pcisph"], default="wcsph4m",
+                    help="wcsph1m: the 4M scene's blocks at 80^3 (profiling case)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--neighbor-mode", type=int, default=1, help="0 = cell scan in every pass, 1 = lists")
@@ -80,6 +81,8 @@ def load_workload(name, mode, seed=0):
     from fluids_gb300 import workloads
     if name == "wcsph4m":
         return workloads.double_dam_4m(mode=mode, seed=seed)
+    if name == "wcsph1m":
+        return workloads.double_dam_4m(mode=mode, seed=seed, n=80)
     if name == "wcsph65k":
         return workloads.dam_break_65k(mode=mode, seed=seed)
     return workloads.pcisph_cube(mode=mode, seed=seed)
@@ -167,6 +170,19 @@ def measured_traffic(kernel, workload):
         f = line.split()
         if len(f) >= 3 and f[0] == kernel and f[1] == workload:
             return float(f[2])
+    return None
+
+
+def measured_instructions(kernel):
+    """(warp instructions per fluid particle, source workload) of a kernel from the committed
+    ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "roofline_instructions.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        f = line.split()
+        if len(f) >= 4 and f[0] == kernel:
+            return float(f[2]) / float(f[3]), f[1]
     return None
 
 
@@ -492,6 +508,19 @@ def main():
                 "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes": bytes_launch,
                 "mean_list_lengths": {"fluid": mean_len[0], "boundary": mean_len[1]},
                 "traffic": tr, "ms_per_launch": kern[top]}
+    # the pair loops are bound by FP32 issue, not DRAM: the same kernel against the SM issue rate
+    ins = measured_instructions(top)
+    if roof is not None and ins is not None:
+        sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
+        mhz, mhz_from = (clk or {}).get("sm_mhz"), "SM clock sampled in the timed region"
+        if not mhz:
+            mhz, mhz_from = 2070.0, "maximum SM clock"
+        peak_ips = sms * 4 * mhz * 1e6
+        ach = ins[0] * n / (kern[top] / 1000.0)
+        roof["issue"] = {"bound": "fp32-issue", "achieved": ach, "peak": peak_ips, "unit": "warp-instructions/s",
+                         "frac": ach / peak_ips, "warp_instructions_per_particle": ins[0],
+                         "instructions_from": "ncu smsp__inst_executed.sum, " + ins[1],
+                         "peak_from": "%d SMs x 4 schedulers x %.0f MHz (%s)" % (sms, mhz, mhz_from)}
     passes = (d["key_bits"] + 7) // 8
     launches_per_step = sum(1 for k in kern) + (passes if "sort" in kern else 0)
     # e2e through the C ABI with pinned host buffers: state in, result out, every step
