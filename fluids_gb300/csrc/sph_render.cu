@@ -231,6 +231,11 @@ __global__ void k_depth_normals(const float* __restrict__ depth, float4* __restr
 
 inline dim3 grid2(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
 
+/* sizes the 16 x 16 pixel grids can cover */
+inline bool image_ok(int w, int h) {
+    return w > 0 && h > 0 && w <= 65536 && h <= 65536 && (long long)w * h <= (1LL << 28);
+}
+
 }  // namespace
 }  // namespace sph
 
@@ -238,8 +243,8 @@ extern "C" {
 
 int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
     if (!x || !view || !d_depth) return SPH_E_INVALID;
-    if (view->width <= 0 || view->height <= 0 || (long long)view->width * view->height > (1LL << 28))
-        return sph_ctx_fail(x, SPH_E_INVALID, "render: width and height must be > 0 (at most 2^28 pixels)");
+    if (!sph::image_ok(view->width, view->height))
+        return sph_ctx_fail(x, SPH_E_INVALID, "render: width and height must be 1..65536 (at most 2^28 pixels)");
     if (!(view->point_radius > 0.f) || !(view->point_scale > 0.f))
         return sph_ctx_fail(x, SPH_E_INVALID, "render: point_radius and point_scale must be > 0");
     if (!x->has_state || x->N <= 0) return sph_ctx_fail(x, SPH_E_STATE, "render: no particles added");
@@ -275,14 +280,15 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
 }
 
 int sph_filter_bilateral(const float* d_in, float* d_out, int width, int height, void* stream) {
-    if (!d_in || !d_out || width <= 0 || height <= 0 || d_in == d_out) return SPH_E_INVALID;
+    if (!d_in || !d_out || !sph::image_ok(width, height) || d_in == d_out) return SPH_E_INVALID;
     const dim3 b(16, 16);
     sph::k_bilateral<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(d_in, d_out, width, height);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
 }
 
 int sph_render_smooth(float* d_depth, float* d_tmp, int width, int height, int iterations, void* stream) {
-    if (!d_depth || !d_tmp || width <= 0 || height <= 0 || iterations < 0 || d_depth == d_tmp) return SPH_E_INVALID;
+    if (!d_depth || !d_tmp || !sph::image_ok(width, height) || iterations < 0 || d_depth == d_tmp)
+        return SPH_E_INVALID;
     const dim3 b(16, 16);
     const cudaStream_t s = (cudaStream_t)stream;
     for (int it = 0; it < iterations; ++it) {
@@ -294,7 +300,7 @@ int sph_render_smooth(float* d_depth, float* d_tmp, int width, int height, int i
 
 int sph_filter_curvature_flow(const float* d_in, float* d_out, int width, int height, float inv_proj_x,
                               float inv_proj_y, void* stream) {
-    if (!d_in || !d_out || width <= 0 || height <= 0 || d_in == d_out) return SPH_E_INVALID;
+    if (!d_in || !d_out || !sph::image_ok(width, height) || d_in == d_out) return SPH_E_INVALID;
     const dim3 b(16, 16);
     sph::k_curvature_flow<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(d_in, d_out, width, height,
                                                                                          inv_proj_x, inv_proj_y);
@@ -303,7 +309,7 @@ int sph_filter_curvature_flow(const float* d_in, float* d_out, int width, int he
 
 int sph_render_normals(const float* d_depth, float* d_normals4, int width, int height, const float inv_projection[16],
                        void* stream) {
-    if (!d_depth || !d_normals4 || !inv_projection || width <= 0 || height <= 0) return SPH_E_INVALID;
+    if (!d_depth || !d_normals4 || !inv_projection || !sph::image_ok(width, height)) return SPH_E_INVALID;
     sph::Inv ip;
     std::memcpy(ip.m, inv_projection, sizeof ip.m);
     const dim3 b(16, 16);

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <random>
 #include <string>
@@ -72,34 +73,36 @@ struct ObjMesh {
 };
 
 int load_obj(const char* path, ObjMesh& m) {
-    FILE* f = std::fopen(path, "rb");
-    if (!f) return -1;
+    std::ifstream in(path, std::ios::binary);
+    if (!in) return -1;
     std::vector<float> pos, nrm;
     std::map<std::pair<int, int>, int> seen;
-    char line[4096];
+    std::string line;
     std::vector<ObjRef> face;
-    int rc = 0;
-    while (std::fgets(line, sizeof line, f)) {
-        char* p = line;
+    while (std::getline(in, line)) {
+        const char* p = line.c_str();
         while (*p == ' ' || *p == '\t') ++p;
         if (p[0] == 'v' && (p[1] == ' ' || p[1] == '\t')) {
-            char* e = p + 1;
+            char* e = const_cast<char*>(p + 1);
             for (int k = 0; k < 3; ++k) pos.push_back((float)std::strtod(e, &e));
         } else if (p[0] == 'v' && p[1] == 'n' && (p[2] == ' ' || p[2] == '\t')) {
-            char* e = p + 2;
+            char* e = const_cast<char*>(p + 2);
             for (int k = 0; k < 3; ++k) nrm.push_back((float)std::strtod(e, &e));
         } else if (p[0] == 'f' && (p[1] == ' ' || p[1] == '\t')) {
             face.clear();
-            char* tok = std::strtok(p + 1, " \t\r\n");
-            for (; tok; tok = std::strtok(nullptr, " \t\r\n")) {
+            const char* q = p + 1;
+            for (;;) {   /* whitespace-separated references */
+                while (*q == ' ' || *q == '\t' || *q == '\r') ++q;
+                if (!*q) break;
                 ObjRef r;
-                if (!parse_ref(tok, (int)(pos.size() / 3), (int)(nrm.size() / 3), r)) break;
+                if (!parse_ref(q, (int)(pos.size() / 3), (int)(nrm.size() / 3), r)) break;
                 face.push_back(r);
+                while (*q && *q != ' ' && *q != '\t' && *q != '\r') ++q;
             }
             for (size_t k = 2; k < face.size(); ++k) {
                 const ObjRef tri[3] = {face[0], face[k - 1], face[k]};
                 for (const ObjRef& r : tri) {
-                    if (r.v < 0 || 3 * (size_t)r.v + 2 >= pos.size()) { rc = -2; break; }
+                    if (r.v < 0 || 3 * (size_t)r.v + 2 >= pos.size()) return -2;
                     const auto key = std::make_pair(r.v, r.n);
                     auto it = seen.find(key);
                     if (it != seen.end()) {
@@ -111,13 +114,10 @@ int load_obj(const char* path, ObjMesh& m) {
                     m.indices.push_back((uint16_t)id);
                     seen[key] = id;
                 }
-                if (rc) break;
             }
         }
-        if (rc) break;
     }
-    std::fclose(f);
-    return rc;
+    return 0;
 }
 
 /* Bullet's scalar vector arithmetic on float triples (LinearMath/btVector3.h). */

@@ -319,7 +319,7 @@ typedef struct sph_view {
     float projection[16];  /* pr_matrix (camera.projection()), column-major */
     float point_radius;    /* sprite sphere radius; the renderer uses 0.0625 (:365) */
     float point_scale;     /* viewport width * tan(fov / 2) (:366) */
-    int width, height;     /* image size in pixels (at most 2^28 pixels) */
+    int width, height;     /* image size in pixels: each 1..65536, at most 2^28 pixels */
 } sph_view;
 /* _render_depth_stage (:355-388) with shaders/sspace_fluid_rendering/depth_stage.vert and
  * .frag: every fluid particle of the context is a sphere sprite; d_depth receives at each
