@@ -19,6 +19,7 @@ _lib = None
 SPH_WCSPH, SPH_PCISPH = 0, 1
 SPH_MODE_COMPAT, SPH_MODE_PHYSICS = 0, 1
 SPH_NEIGH_SCAN, SPH_NEIGH_LIST = 0, 1
+SPH_FAULT_NONE, SPH_FAULT_BARRIER_STALL = 0, 1
 FLAGS = dict(NAN=1, ESCAPED=2, TIMEOUT=4, OVERFLOW=8, NONCONVERGED=16, NONSMOOTH=32)
 STATUS = {0: "SPH_OK", 1: "SPH_E_INVALID", 2: "SPH_E_CUDA", 3: "SPH_E_NONCONVERGED", 4: "SPH_E_ESCAPED",
           5: "SPH_E_NAN", 6: "SPH_E_TIMEOUT", 7: "SPH_E_OVERFLOW", 8: "SPH_E_STATE", 9: "SPH_E_NOMEM"}
@@ -48,7 +49,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_set_field_async",
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
            "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
-           "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere", "sph_save_state", "sph_load_state"]
+           "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere", "sph_save_state", "sph_load_state",
+           "sph_inject_fault"]
 
 
 class SphParams(C.Structure):
@@ -186,6 +188,7 @@ def lib():
             "sph_scene_sphere": (ip, [C.c_float, C.c_float, fp, ip]),
             "sph_save_state": (ip, [vp, C.c_char_p]),
             "sph_load_state": (ip, [vp, C.c_char_p]),
+            "sph_inject_fault": (ip, [vp, ip]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -371,6 +374,10 @@ class Context:
         ang = np.zeros(4, np.float32)
         self._c(self._lib.sph_get_body_state(self.h, int(body), ptr(rot), ptr(lin), ptr(ang)))
         return rot.reshape(3, 4), lin[:3], ang[:3]
+
+    def inject_fault(self, kind):
+        """sph_inject_fault (failure-detection tests)."""
+        self._c(self._lib.sph_inject_fault(self.h, int(kind)))
 
     def save_state(self, path):
         """Checkpoint (sph_save_state)."""

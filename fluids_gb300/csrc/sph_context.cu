@@ -1097,6 +1097,16 @@ int sph_simulate(sph_ctx* x, int nsteps) {
     if (check_ctx(x)) return SPH_E_INVALID;
     if (nsteps < 0) return fail(x, SPH_E_INVALID, "nsteps < 0");
     if (!x->has_state || x->N <= 0) return SPH_OK;
+    if (x->inject == SPH_FAULT_BARRIER_STALL && nsteps > 0) {
+        /* one step outside the graph with the stall in its launch parameters */
+        drop_graph(x);
+        x->inject = 0;
+        x->c.barrier_extra = 1;
+        const int rc = enqueue_step(x, x->c.pci_max_iter);
+        x->c.barrier_extra = 0;
+        if (rc != SPH_OK) return rc;
+        return sph_simulate(x, nsteps - 1);
+    }
     if (x->p.use_graph && x->graph_ok && !x->gexec) {
         int rc = build_graph(x);
         if (rc != SPH_OK) return rc;
@@ -1154,6 +1164,18 @@ int sph_profile_step(sph_ctx* x, int nsteps, float* ms_out, int max_groups, int*
         std::strncpy(names, all.c_str(), names_len - 1);
         names[names_len - 1] = 0;
     }
+    return SPH_OK;
+}
+
+int sph_inject_fault(sph_ctx* x, int kind) {
+    if (check_ctx(x)) return SPH_E_INVALID;
+    if (kind == SPH_FAULT_NONE) {
+        x->inject = 0;
+        return SPH_OK;
+    }
+    if (kind != SPH_FAULT_BARRIER_STALL) return fail(x, SPH_E_INVALID, "unknown fault kind");
+    if (x->p.method != SPH_PCISPH) return fail(x, SPH_E_STATE, "the barrier stall needs a PCISPH context");
+    x->inject = kind;
     return SPH_OK;
 }
 

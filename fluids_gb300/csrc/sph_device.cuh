@@ -31,6 +31,7 @@ struct Const {
     float dt, vmax, lim_x, lim_y, lim_z;
     float pci_eta;
     int pci_min_iter, pci_max_iter;
+    int barrier_extra;   /* 0; 1 only for an injected barrier stall (sph_inject_fault) */
     int key_bits;
     float rmin_wc;       /* largest float <= 1e-5: wcsph.cl:152 compares r > 0.00001 (a double) */
     float rmin2_wc;      /* rmin_wc^2: the same guard on r^2 */

@@ -13,9 +13,10 @@
  *                       the device after a grid barrier, so no host round trip per iteration.
  *                       Optionally the final predict_vel_n_pos (:240-284) is fused after it.
  *   k_pci_integrate     predict_vel_n_pos (pcisph.cl:240-284)
- * The grid barrier spins on a generation counter with a bounded poll count; on timeout the
- * kernel sets SPH_FLAG_TIMEOUT and every CTA returns (the launch is cooperative, so all CTAs
- * are co-resident and the wait ends in practice).
+ * The grid barrier spins on a generation counter with a bounded poll count (2^24 polls of at
+ * least 64 ns); on timeout the kernel sets SPH_FLAG_TIMEOUT and every CTA returns (the launch
+ * is cooperative, so all CTAs are co-resident and the wait ends in practice).  The test of
+ * that path injects a stall from the host (sph_inject_fault) instead of faulting anything.
  */
 #include "sph_kernels.cuh"
 
@@ -24,8 +25,10 @@ namespace sph {
 namespace {
 constexpr long long kBarrierSpinLimit = 1LL << 24;
 
-/* Grid-wide barrier: bar[0] = arrivals, bar[1] = generation.  Returns false on timeout. */
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* flags) {
+/* Grid-wide barrier: bar[0] = arrivals, bar[1] = generation.  Returns false on timeout.
+ * extra > 0 (an injected stall) waits for arrivals that never come, so every CTA's bounded
+ * wait runs out. */
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* flags, unsigned extra) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -34,7 +37,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* flags) {
         __threadfence();
         const unsigned arrived = atomicAdd(bar, 1u);
         int ok = 1;
-        if (arrived == gridDim.x - 1) {
+        if (arrived == gridDim.x - 1 + extra) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
@@ -258,12 +261,12 @@ __global__ void __launch_bounds__(256) k_pci_loop(Const c, Bufs b, int min_iter,
     int it = 1;
     for (; it <= max_iter; ++it) {
         for (int i = tid; i < n; i += stride) pci_predict_one(c, b, i);
-        if (!grid_barrier(b.barrier, b.flags)) return;
+        if (!grid_barrier(b.barrier, b.flags, (unsigned)c.barrier_extra)) return;
         float lmax = 0.f;
         for (int i = tid; i < n; i += stride) lmax = fmaxf(lmax, pci_update_one<COMPAT>(c, b, i));
         lmax = block_max(lmax);
         if (threadIdx.x == 0) atomicMax(reinterpret_cast<unsigned*>(&b.pci_maxerr[it - 1]), __float_as_uint(lmax));
-        if (!grid_barrier(b.barrier, b.flags)) return;
+        if (!grid_barrier(b.barrier, b.flags, (unsigned)c.barrier_extra)) return;
         const float mx = *reinterpret_cast<volatile float*>(&b.pci_maxerr[it - 1]);
         for (int i = tid; i < n; i += stride) pci_pressure_force_one(c, b, i);
         bool stop = false;

@@ -198,6 +198,15 @@ int sph_profile_step(sph_ctx* ctx, int nsteps, float* ms_out, int max_groups, in
                      size_t names_len);
 /* Waits for the context stream. */
 int sph_synchronize(sph_ctx* ctx);
+
+/* Host-side fault injection for failure-detection tests (no counterpart in the reference,
+ * whose only failure path is CLError, opencl/clerror.cpp:15-19).  SPH_FAULT_BARRIER_STALL
+ * (PCISPH contexts): the next step's predict-correct kernel waits at its grid barrier for one
+ * CTA more than it launched, so every CTA's bounded wait runs out (about a second), sets
+ * SPH_FLAG_TIMEOUT and returns; the step's integration is skipped, the context stays usable
+ * and the steps after it are normal.  Nothing faults or hangs.  SPH_FAULT_NONE cancels. */
+enum sph_fault { SPH_FAULT_NONE = 0, SPH_FAULT_BARRIER_STALL = 1 };
+int sph_inject_fault(sph_ctx* ctx, int kind);
 /* Reads (and with clear = 1 resets) the device status word; synchronises. */
 int sph_device_flags(sph_ctx* ctx, unsigned* flags, int clear);
 
