@@ -20,6 +20,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "sph_ctx.cuh"
 
 namespace {
@@ -385,6 +387,7 @@ int run_stage_impl(sph_ctx* x, int stage) {
 /* Profiling marks: when x->prof is set, an event is recorded after each kernel group of the
  * step so sph_profile_step can report per-kernel device time (never inside a graph). */
 void mark(sph_ctx* x, const char* name) {
+    nvtxMarkA(name);   /* a stage boundary on the timeline of an attached profiler */
     if (!x->prof) return;
     cudaEvent_t e;
     cudaEventCreate(&e);
@@ -1093,7 +1096,16 @@ int sph_get_body_state(sph_ctx* x, int body, float* rot3x4, float* lin4, float* 
 int sph_particle_count(const sph_ctx* x) { return x ? x->N : 0; }
 int sph_boundary_particle_count(const sph_ctx* x) { return x ? x->NB : 0; }
 
+namespace {
+/* NVTX range for the duration of one API call (a no-op without an attached tool) */
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+}  // namespace
+
 int sph_simulate(sph_ctx* x, int nsteps) {
+    NvtxRange range("sph_simulate");
     if (check_ctx(x)) return SPH_E_INVALID;
     if (nsteps < 0) return fail(x, SPH_E_INVALID, "nsteps < 0");
     if (!x->has_state || x->N <= 0) return SPH_OK;
@@ -1124,6 +1136,7 @@ int sph_simulate(sph_ctx* x, int nsteps) {
 
 int sph_profile_step(sph_ctx* x, int nsteps, float* ms_out, int max_groups, int* ngroups, char* names,
                      size_t names_len) {
+    NvtxRange range("sph_profile_step");
     if (check_ctx(x) || nsteps <= 0 || !ms_out || !ngroups) return SPH_E_INVALID;
     if (!x->has_state || x->N <= 0) return fail(x, SPH_E_STATE, "no particles added");
     std::vector<cudaEvent_t> ev;
@@ -1180,6 +1193,7 @@ int sph_inject_fault(sph_ctx* x, int kind) {
 }
 
 int sph_run_stage(sph_ctx* x, int stage) {
+    NvtxRange range("sph_run_stage");
     if (check_ctx(x)) return SPH_E_INVALID;
     if (!x->has_state) return fail(x, SPH_E_STATE, "no particles added");
     return run_stage_impl(x, stage);
