@@ -403,7 +403,7 @@ def bench_render(torch, ctx, stream, frames, width=1920, height=1080):
             "filter_iterations": r.filter_iterations, "frames": frames, "ms_per_frame": float(ms.sum()),
             "ms_depth": float(ms[0]), "ms_blur": float(ms[1]), "ms_normals": float(ms[2]),
             "coverage": float((r.depth != 0).float().mean().item()),
-            "kernels_per_frame": 3 + 2 * r.filter_iterations + 1}
+            "kernels_per_frame": 7 + 2 * r.filter_iterations + 1}
 
 
 def run_reference(args):

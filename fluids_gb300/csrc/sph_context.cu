@@ -948,6 +948,7 @@ int sph_destroy(sph_ctx* x) {
     if (x->stream) cudaStreamSynchronize(x->stream);
     free_arena(x);
     cudaFree(x->render_buf);
+    cudaFree(x->render_sort);
     if (x->own_stream && x->stream) cudaStreamDestroy(x->stream);
     delete x;
     return SPH_OK;

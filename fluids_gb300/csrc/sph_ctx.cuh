@@ -65,6 +65,8 @@ struct sph_ctx {
     /* depth-test scratch of sph_render_depth: 8 bytes per pixel */
     void* render_buf = nullptr;
     size_t render_pixels = 0;
+    void* render_sort = nullptr;   /* sph_render_depth: 16-bit depth keys and particle order */
+    size_t render_sort_bytes = 0;
 };
 
 /* Records msg as the context's last error (or the last creation error) and returns code. */

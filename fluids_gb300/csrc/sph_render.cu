@@ -79,21 +79,70 @@ __device__ __forceinline__ bool fragment(const View& v, const float e[4], float 
  * lowest index (the first primitive GL_LESS lets through).  Depths are >= 0, so their bit
  * patterns order like the values.  A plain read first skips fragments that already lose:
  * keys only decrease, so a stale read can only cost an unneeded atomic. */
-__global__ void k_splat_keys(View v, int n, const float4* __restrict__ pos, unsigned long long* __restrict__ key) {
+/* A lower bound of the normalised depth of every fragment of a sprite, or 0 when none is
+ * known.  With the projection's column-2 and column-3 x, y entries zero (any symmetric
+ * perspective) the fragment depth (s2 pr10 + pr11) / (s2 pr14 + pr15) depends only on the
+ * sphere point's eye z, s2 in [e_z, e_z + r]; away from the pole s2 = -pr15 / pr14 it is
+ * monotone there, so its smaller end value bounds every fragment.  A margin of 1e-5 covers the
+ * fragments' own rounding. */
+__device__ __forceinline__ float depth_floor(const View& v, const float e[4]) {
+    const float* m = v.pr;
+    if (m[8] != 0.f || m[9] != 0.f || m[12] != 0.f || m[13] != 0.f) return 0.f;
+    const float lo = e[2] - 1e-3f * v.radius, hi = e[2] + v.radius * 1.001f;
+    if (m[14] != 0.f) {
+        const float pole = -m[15] / m[14];
+        if (pole >= lo && pole <= hi) return 0.f;
+    }
+    auto lin = [&](float s2) { return ((s2 * m[10] + m[11]) / (s2 * m[14] + m[15]) + 1.0f) * 0.5f; };
+    const float b = fminf(lin(lo), lin(hi)) - 1e-5f;
+    return b > 0.f ? b : 0.f;
+}
+
+/* Front-to-back processing order: the top 16 bits of the eye distance (sign, exponent and 7
+ * mantissa bits: monotone for positive floats), particles behind the eye last.  Any order
+ * gives the same image; near sprites first let later ones skip their pixels early. */
+__global__ void k_depth_order(View v, int n, const float4* __restrict__ pos, uint32_t* __restrict__ keys,
+                              int32_t* __restrict__ vals) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const float4 p = pos[i];
+    const float d = -(v.mv[2] * p.x + v.mv[6] * p.y + v.mv[10] * p.z + v.mv[14]);
+    keys[i] = d > 0.f ? __float_as_uint(d) >> 16 : 0xffffu;
+    vals[i] = i;
+}
+
+__global__ void k_splat_keys(View v, int n, const float4* __restrict__ pos, const int32_t* __restrict__ order,
+                             unsigned long long* __restrict__ key) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = order[t];
     float e[4], wx, wy, size;
     if (!sprite(v, pos[i], e, wx, wy, size)) return;
+    /* a pixel already nearer than this sprite can get is skipped before any fragment arithmetic:
+       keys only decrease, so a stale read (even an L1 copy older than other CTAs' atomics)
+       only costs the full test */
+    const unsigned floor_bits = __float_as_uint(depth_floor(v, e));
     const int x0 = max(0, (int)floorf(wx - 0.5f * size)), x1 = min(v.w - 1, (int)ceilf(wx + 0.5f * size));
     const int y0 = max(0, (int)floorf(wy - 0.5f * size)), y1 = min(v.h - 1, (int)ceilf(wy + 0.5f * size));
-    for (int py = y0; py <= y1; ++py)
-        for (int px = x0; px <= x1; ++px) {
-            float nd, lin;
-            if (!fragment(v, e, wx, wy, size, px, py, nd, lin)) continue;
-            const unsigned long long k = ((unsigned long long)__float_as_uint(lin) << 32) | (unsigned)i;
-            unsigned long long* dst = &key[(size_t)py * v.w + px];
-            if (k < *reinterpret_cast<volatile unsigned long long*>(dst)) atomicMin(dst, k);
+    constexpr int kAhead = 8;   /* key loads in flight per thread */
+    for (int py = y0; py <= y1; ++py) {
+        unsigned long long* row = key + (size_t)py * v.w;
+        for (int px0 = x0; px0 <= x1; px0 += kAhead) {
+            unsigned long long cur[kAhead];
+#pragma unroll
+            for (int u = 0; u < kAhead; ++u)
+                cur[u] = px0 + u <= x1 ? __ldca(row + px0 + u) : 0ull;   /* L1 copy: stale is still safe */
+#pragma unroll
+            for (int u = 0; u < kAhead; ++u) {
+                const int px = px0 + u;
+                if (px > x1 || (unsigned)(cur[u] >> 32) < floor_bits) continue;
+                float nd, lin;
+                if (!fragment(v, e, wx, wy, size, px, py, nd, lin)) continue;
+                const unsigned long long k = ((unsigned long long)__float_as_uint(lin) << 32) | (unsigned)i;
+                if (k < cur[u]) atomicMin(row + px, k);
+            }
         }
+    }
 }
 
 /* Per pixel: the winning particle's fragment depth, recomputed with the same arithmetic. */
@@ -249,6 +298,18 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
         return sph_ctx_fail(x, SPH_E_INVALID, "render: point_radius and point_scale must be > 0");
     if (!x->has_state || x->N <= 0) return sph_ctx_fail(x, SPH_E_STATE, "render: no particles added");
     const size_t npix = (size_t)view->width * view->height;
+    const size_t nsort = 8 * (size_t)x->N;
+    if (x->render_sort_bytes < nsort) {
+        cudaStreamSynchronize(x->stream);
+        cudaFree(x->render_sort);
+        x->render_sort = nullptr;
+        x->render_sort_bytes = 0;
+        if (cudaMalloc(&x->render_sort, nsort) != cudaSuccess) {
+            cudaGetLastError();
+            return sph_ctx_fail(x, SPH_E_NOMEM, "render: particle order buffers");
+        }
+        x->render_sort_bytes = nsort;
+    }
     if (x->render_pixels < npix) {
         cudaStreamSynchronize(x->stream);
         cudaFree(x->render_buf);
@@ -272,7 +333,12 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
     const int bs = 256, n = x->N;
     const dim3 b2(16, 16);
     sph::k_splat_clear<<<(unsigned)((npix + bs - 1) / bs), bs, 0, s>>>(npix, key);
-    sph::k_splat_keys<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, key);
+    uint32_t* okeys = reinterpret_cast<uint32_t*>(x->render_sort);
+    int32_t* order = reinterpret_cast<int32_t*>(okeys + n);
+    sph::k_depth_order<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, okeys, order);
+    const int rc = sph_sort_pairs(okeys, order, n, 16, s);
+    if (rc != SPH_OK) return sph_ctx_fail(x, rc, "render: depth order sort");
+    sph::k_splat_keys<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, order, key);
     sph::k_splat_resolve<<<sph::grid2(v.w, v.h, b2), b2, 0, s>>>(v, x->b.pos, key, d_depth);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return sph_ctx_fail(x, SPH_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
