@@ -731,6 +731,7 @@ struct SortCache {
     unsigned* flags = nullptr;
     size_t n_cap = 0;
     int device = -1;
+    cudaEvent_t done = nullptr;   /* the last sort's end: the next one, on any stream, waits for it */
 };
 SortCache g_sort;
 
@@ -1331,6 +1332,8 @@ int sph_sort_pairs(uint32_t* d_keys, int32_t* d_vals, int n, int key_bits, void*
         if (g_sort.ws && g_sort.device == dev) {
             cudaFree(g_sort.ws); cudaFree(g_sort.kalt); cudaFree(g_sort.valt); cudaFree(g_sort.flags);
         }
+        if (g_sort.done && g_sort.device == dev) cudaEventDestroy(g_sort.done);
+        g_sort.done = nullptr;
         g_sort.ws = nullptr; g_sort.kalt = nullptr; g_sort.valt = nullptr; g_sort.flags = nullptr;
         g_sort.ws_bytes = 0; g_sort.n_cap = 0;
         g_sort.device = dev;
@@ -1342,12 +1345,22 @@ int sph_sort_pairs(uint32_t* d_keys, int32_t* d_vals, int n, int key_bits, void*
             return fail(nullptr, SPH_E_NOMEM, "sph_sort_pairs: scratch allocation failed");
         }
         cudaMemset(g_sort.flags, 0, 16);
+        if (cudaEventCreateWithFlags(&g_sort.done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            g_sort.done = nullptr;
+        }
         g_sort.ws_bytes = wsb;
         g_sort.n_cap = ncap;
     }
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaStream_t s = (cudaStream_t)stream;
+    /* calls on different streams share the scratch: each waits on the GPU for the previous
+       one (outside stream capture, where an outside event cannot be waited on) */
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cap);
+    const bool order = g_sort.done && cap == cudaStreamCaptureStatusNone;
+    if (order) cudaStreamWaitEvent(s, g_sort.done, 0);
     uint32_t* kr;
     int32_t* vr;
     sph::sort_pairs(s, d_keys, d_vals, g_sort.kalt, g_sort.valt, n, key_bits, g_sort.ws, g_sort.flags, sms, &kr, &vr);
@@ -1355,6 +1368,7 @@ int sph_sort_pairs(uint32_t* d_keys, int32_t* d_vals, int n, int key_bits, void*
         cudaMemcpyAsync(d_keys, kr, 4 * (size_t)n, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(d_vals, vr, 4 * (size_t)n, cudaMemcpyDeviceToDevice, s);
     }
+    if (order) cudaEventRecord(g_sort.done, s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "sph_sort_pairs");
     return SPH_OK;

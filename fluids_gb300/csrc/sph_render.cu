@@ -298,7 +298,8 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
         return sph_ctx_fail(x, SPH_E_INVALID, "render: point_radius and point_scale must be > 0");
     if (!x->has_state || x->N <= 0) return sph_ctx_fail(x, SPH_E_STATE, "render: no particles added");
     const size_t npix = (size_t)view->width * view->height;
-    const size_t nsort = 8 * (size_t)x->N;
+    /* keys, order, their sort ping-pong copies and the sort's workspace, all the context's own */
+    const size_t nsort = 16 * (size_t)x->N + sph::sort_workspace_bytes(x->N, 16);
     if (x->render_sort_bytes < nsort) {
         cudaStreamSynchronize(x->stream);
         cudaFree(x->render_sort);
@@ -335,10 +336,14 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
     sph::k_splat_clear<<<(unsigned)((npix + bs - 1) / bs), bs, 0, s>>>(npix, key);
     uint32_t* okeys = reinterpret_cast<uint32_t*>(x->render_sort);
     int32_t* order = reinterpret_cast<int32_t*>(okeys + n);
+    uint32_t* okeys_alt = reinterpret_cast<uint32_t*>(order + n);
+    int32_t* order_alt = reinterpret_cast<int32_t*>(okeys_alt + n);
+    void* ws = order_alt + n;
     sph::k_depth_order<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, okeys, order);
-    const int rc = sph_sort_pairs(okeys, order, n, 16, s);
-    if (rc != SPH_OK) return sph_ctx_fail(x, rc, "render: depth order sort");
-    sph::k_splat_keys<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, order, key);
+    uint32_t* ks;
+    int32_t* sorted;
+    sph::sort_pairs(s, okeys, order, okeys_alt, order_alt, n, 16, ws, x->b.flags, x->num_sms, &ks, &sorted);
+    sph::k_splat_keys<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, sorted, key);
     sph::k_splat_resolve<<<sph::grid2(v.w, v.h, b2), b2, 0, s>>>(v, x->b.pos, key, d_depth);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return sph_ctx_fail(x, SPH_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));

@@ -356,7 +356,9 @@ int sph_render_normals(const float* d_depth, float* d_normals4, int width, int h
 
 /* clsort<cl_uint, cl_int> (opencl/algorithms/clsort.h:13-35): stable ascending sort of n
  * (key, value) pairs in place in device memory, on the low key_bits bits (1..32) of the
- * key.  Scratch memory is allocated on first use and cached per device. */
+ * key.  Scratch memory is allocated on first use and cached per device; calls on different
+ * streams are ordered on the GPU one after the other (not while a stream is being captured:
+ * captured calls must not overlap another call on the GPU). */
 int sph_sort_pairs(uint32_t* d_keys, int32_t* d_vals, int n, int key_bits, void* cuda_stream);
 
 /* The same stable sort for callers that cannot allocate device memory (no counterpart in
