@@ -406,6 +406,21 @@ def bench_render(torch, ctx, stream, frames, width=1920, height=1080):
             "kernels_per_frame": 7 + 2 * r.filter_iterations + 1}
 
 
+def bench_voxelize(reps=5):
+    """GPU voxel sampler (sph_scene_voxelize, Model::surface_sampling): a level-4 icosphere
+    of radius 0.25 m (5,120 triangles) at particle spacing 0.005 m; host wall time per call
+    (it is synchronous: upload, count, emit, bucket sort, duplicate test, corners, download)."""
+    from fluids_gb300 import scenes
+    v, ix = scenes.icosphere(0.25, 4)
+    out = scenes.voxelize(v, ix, 0.005)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = scenes.voxelize(v, ix, 0.005)
+    ms = 1000.0 * (time.perf_counter() - t0) / reps
+    return {"mesh": "icosphere level 4, r = 0.25 m", "triangles": len(ix) // 3, "spacing_m": 0.005,
+            "particles": len(out), "ms_per_call": ms, "calls": reps}
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -552,9 +567,10 @@ def main():
         e2e = {"value": units_e / te, "unit": UNIT, "h2d_bytes_per_step": 48 * n,
                "d2h_bytes_per_step": 48 * n, "steps": k_e2e, "host_buffers": "pinned",
                "copies": "pos, vel, vel_half in and out on the context stream; one host wait per step"}
-    rend = None
+    rend = vox = None
     if args.render_frames > 0:
         rend = bench_render(torch, ctx, stream, args.render_frames)
+        vox = bench_voxelize()
     ctx.close()
     batched = None
     if args.batched_steps > 0 and args.workload == "wcsph4m":
@@ -581,7 +597,7 @@ def main():
                 "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk,
                 "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched, "adjoint": adjoint,
-                "pcisph": pcisph, "render": rend}
+                "pcisph": pcisph, "render": rend, "voxelize": vox}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
