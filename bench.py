@@ -373,8 +373,9 @@ def bench_pcisph(torch, steps, warmup):
 
 def bench_render(torch, ctx, stream, frames, width=1920, height=1080):
     """Screen-space surface of the context's particles (depth sprites, two blur iterations,
-    normals) at width x height with the reference's default camera and sprite radius; device
-    time per stage from CUDA events on the context stream, averaged over `frames` frames."""
+    normals, final shading over a background gradient with a random 256^2 cube map) at
+    width x height with the reference's default camera and sprite radius; device time per
+    stage from CUDA events on the context stream, averaged over `frames` frames."""
     from fluids_gb300 import capi, render
     cam = render.Camera(width, height)
     mv = render.look_at((1.0, 1.3, 3.2), (1.0, 0.25, 0.5), (0.0, 1.0, 0.0))
@@ -385,8 +386,14 @@ def bench_render(torch, ctx, stream, frames, width=1920, height=1080):
     pr = cam.projection()
     ipr = np.linalg.inv(pr.astype(np.float64)).astype(np.float32)
     view = capi.make_view(mv, pr, r.point_radius, cam.point_scale(), width, height)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    tot = np.zeros(3)
+    # a background gradient and a 256^2 cube map stand in for the scene behind and the skybox
+    dev = r.depth.device
+    yy, xx = torch.meshgrid(torch.linspace(0, 1, height, device=dev), torch.linspace(0, 1, width, device=dev),
+                            indexing="ij")
+    bkg = torch.stack([xx, yy, 0.5 * torch.ones_like(xx), torch.ones_like(xx)], -1).contiguous()
+    cube = torch.rand((6, 256, 256, 4), generator=torch.Generator(device=dev).manual_seed(0), device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    tot = np.zeros(4)
     torch.cuda.synchronize()
     for _ in range(frames):
         ev[0].record(stream)
@@ -396,14 +403,17 @@ def bench_render(torch, ctx, stream, frames, width=1920, height=1080):
         ev[2].record(stream)
         capi.render_normals(r.depth.data_ptr(), r.normals.data_ptr(), width, height, ipr, s)
         ev[3].record(stream)
+        capi.render_shade(r.depth.data_ptr(), r.normals.data_ptr(), bkg.data_ptr(), cube.data_ptr(), 256, width,
+                          height, mv, ipr, r.color.data_ptr(), s)
+        ev[4].record(stream)
         torch.cuda.synchronize()
-        tot += [ev[k].elapsed_time(ev[k + 1]) for k in range(3)]
+        tot += [ev[k].elapsed_time(ev[k + 1]) for k in range(4)]
     ms = tot / frames
     return {"image": [width, height], "particles": ctx.particle_count(), "point_radius": r.point_radius,
             "filter_iterations": r.filter_iterations, "frames": frames, "ms_per_frame": float(ms.sum()),
             "ms_depth": float(ms[0]), "ms_blur": float(ms[1]), "ms_normals": float(ms[2]),
-            "coverage": float((r.depth != 0).float().mean().item()),
-            "kernels_per_frame": 7 + 2 * r.filter_iterations + 1}
+            "ms_shade": float(ms[3]), "coverage": float((r.depth != 0).float().mean().item()),
+            "kernels_per_frame": 7 + 2 * r.filter_iterations + 2}
 
 
 def bench_voxelize(reps=5):

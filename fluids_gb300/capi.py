@@ -50,7 +50,7 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
            "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
            "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere", "sph_save_state", "sph_load_state",
-           "sph_inject_fault"]
+           "sph_inject_fault", "sph_render_shade"]
 
 
 class SphParams(C.Structure):
@@ -189,6 +189,8 @@ def lib():
             "sph_save_state": (ip, [vp, C.c_char_p]),
             "sph_load_state": (ip, [vp, C.c_char_p]),
             "sph_inject_fault": (ip, [vp, ip]),
+            "sph_render_shade": (ip, [vp, vp, vp, vp, ip, ip, ip, C.POINTER(C.c_float), C.POINTER(C.c_float), vp,
+                                      vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -563,3 +565,16 @@ def render_normals(d_depth, d_normals4, width, height, inv_projection, stream=No
     ip = np.ascontiguousarray(np.asarray(inv_projection, np.float32).reshape(4, 4).T.reshape(-1))
     check(lib().sph_render_normals(C.c_void_p(d_depth), C.c_void_p(d_normals4), int(width), int(height),
                                    ip.ctypes.data_as(C.POINTER(C.c_float)), C.c_void_p(stream or 0)))
+
+
+def render_shade(d_depth, d_normals4, d_background4, d_cube4, cube_size, width, height, modelview,
+                 inv_projection, d_rgba, stream=None):
+    """sph_render_shade; matrices in mathematical layout (passed column-major), device
+    addresses as ints (0 / None for no background or cube map)."""
+    mv = np.ascontiguousarray(np.asarray(modelview, np.float32).reshape(4, 4).T.reshape(-1))
+    ip = np.ascontiguousarray(np.asarray(inv_projection, np.float32).reshape(4, 4).T.reshape(-1))
+    fpt = C.POINTER(C.c_float)
+    check(lib().sph_render_shade(C.c_void_p(d_depth), C.c_void_p(d_normals4), C.c_void_p(d_background4 or 0),
+                                 C.c_void_p(d_cube4 or 0), int(cube_size), int(width), int(height),
+                                 mv.ctypes.data_as(fpt), ip.ctypes.data_as(fpt), C.c_void_p(d_rgba),
+                                 C.c_void_p(stream or 0)))

@@ -17,6 +17,8 @@
  *   k_depth_normals  shaders/sspace_fluid_rendering/normals_stage.frag: eye-space positions
  *                    from the inverse projection, one-sided differences with the smaller
  *                    depth jump, normal = normalize(ddx x ddy).
+ *   k_shade          shaders/sspace_fluid_rendering/final_stage.frag: the fluid's colour over
+ *                    a background image with a cube map for reflections, into an RGBA image.
  * Images are row-major, row 0 at the bottom (window coordinates), single-channel float
  * (depth) or float4 (normals); reads outside the image clamp to the edge.
  */
@@ -278,6 +280,121 @@ __global__ void k_depth_normals(const float* __restrict__ depth, float4* __restr
     nrm[(size_t)y * w + x] = make_float4(cx / l, cy / l, cz / l, 1.0f);
 }
 
+/* Bilinear read of a single-channel or float4 image at normalised coordinates (u, v) with
+ * texel centres at (i + 0.5) / w, coordinates clamped to the edge texels (GL_LINEAR). */
+__device__ __forceinline__ void bilinear_at(float u, float v, int w, int h, int& x0, int& y0, int& x1, int& y1,
+                                            float& fx, float& fy) {
+    const float px = u * (float)w - 0.5f, py = v * (float)h - 0.5f;
+    const float bx = floorf(px), by = floorf(py);
+    fx = px - bx;
+    fy = py - by;
+    x0 = (int)bx; y0 = (int)by;
+    x1 = x0 + 1; y1 = y0 + 1;
+    x0 = x0 < 0 ? 0 : (x0 >= w ? w - 1 : x0); x1 = x1 < 0 ? 0 : (x1 >= w ? w - 1 : x1);
+    y0 = y0 < 0 ? 0 : (y0 >= h ? h - 1 : y0); y1 = y1 < 0 ? 0 : (y1 >= h ? h - 1 : y1);
+}
+
+__device__ __forceinline__ float lerp1(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+__device__ float sample1(const float* img, int w, int h, float u, float v) {
+    int x0, y0, x1, y1;
+    float fx, fy;
+    bilinear_at(u, v, w, h, x0, y0, x1, y1, fx, fy);
+    const float a = lerp1(img[(size_t)y0 * w + x0], img[(size_t)y0 * w + x1], fx);
+    const float b = lerp1(img[(size_t)y1 * w + x0], img[(size_t)y1 * w + x1], fx);
+    return lerp1(a, b, fy);
+}
+
+__device__ float4 sample4(const float4* img, int w, int h, float u, float v) {
+    int x0, y0, x1, y1;
+    float fx, fy;
+    bilinear_at(u, v, w, h, x0, y0, x1, y1, fx, fy);
+    const float4 p = img[(size_t)y0 * w + x0], q = img[(size_t)y0 * w + x1];
+    const float4 r = img[(size_t)y1 * w + x0], t = img[(size_t)y1 * w + x1];
+    return make_float4(lerp1(lerp1(p.x, q.x, fx), lerp1(r.x, t.x, fx), fy),
+                       lerp1(lerp1(p.y, q.y, fx), lerp1(r.y, t.y, fx), fy),
+                       lerp1(lerp1(p.z, q.z, fx), lerp1(r.z, t.z, fx), fy),
+                       lerp1(lerp1(p.w, q.w, fx), lerp1(r.w, t.w, fx), fy));
+}
+
+/* GL cube-map lookup: the face of the major axis (+x, -x, +y, -y, +z, -z) and its (s, t) by
+ * the OpenGL face table, then a bilinear read of that face (S x S float4 texels). */
+__device__ float4 sample_cube(const float4* cube, int S, float rx, float ry, float rz) {
+    const float ax = fabsf(rx), ay = fabsf(ry), az = fabsf(rz);
+    int face;
+    float sc, tc, ma;
+    if (ax >= ay && ax >= az) {
+        face = rx >= 0.f ? 0 : 1; ma = ax; sc = rx >= 0.f ? -rz : rz; tc = -ry;
+    } else if (ay >= az) {
+        face = ry >= 0.f ? 2 : 3; ma = ay; sc = rx; tc = ry >= 0.f ? rz : -rz;
+    } else {
+        face = rz >= 0.f ? 4 : 5; ma = az; sc = rz >= 0.f ? rx : -rx; tc = -ry;
+    }
+    const float s = (sc / ma + 1.0f) * 0.5f, t = (tc / ma + 1.0f) * 0.5f;
+    return sample4(cube + (size_t)face * S * S, S, S, s, t);
+}
+
+struct Shade {
+    float mv[16], ip[16];
+};
+
+__device__ __forceinline__ void norm3(float& x, float& y, float& z) {
+    const float l = sqrtf((x * x + y * y) + z * z);
+    x /= l; y /= l; z /= l;
+}
+
+/* shaders/sspace_fluid_rendering/final_stage.frag: Blinn-Phong specular, Fresnel (Schlick,
+ * r0 = 0.1), cube-map reflection, background refraction offset by the normal, fixed
+ * attenuation colour; background where depth <= 0.  Light direction mv * (0.7, 1, 0, 0). */
+__global__ void k_shade(const float* __restrict__ depth, const float4* __restrict__ nrm,
+                        const float4* __restrict__ bkg, const float4* __restrict__ cube, int S, int w, int h,
+                        Shade sh, float4* __restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const size_t k = (size_t)y * w + x;
+    const float u = ((float)x + 0.5f) * (1.0f / (float)w), v = ((float)y + 0.5f) * (1.0f / (float)h);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float d = depth[k];
+    const float4 nn = nrm[k];
+    const float4 bg = bkg ? bkg[k] : zero;
+    if (d <= 0.0f) {
+        out[k] = make_float4(bg.x, bg.y, bg.z, 1.0f);
+        return;
+    }
+    const float* m = sh.mv;
+    float ix = m[0] * 0.7f + m[4] * 1.0f, iy = m[1] * 0.7f + m[5] * 1.0f, iz = m[2] * 0.7f + m[6] * 1.0f;
+    float p[3];
+    Inv ip;
+    for (int q = 0; q < 16; ++q) ip.m[q] = sh.ip[q];
+    uv_to_eye(ip, u, v, d, p);
+    norm3(ix, iy, iz);
+    float vx = -p[0], vy = -p[1], vz = -p[2];
+    norm3(vx, vy, vz);
+    float hx = ix + vx, hy = iy + vy, hz = iz + vz;
+    norm3(hx, hy, hz);
+    const float ndh = (hx * nn.x + hy * nn.y) + hz * nn.z;
+    const float spec = powf(fmaxf(0.0f, ndh), 50.0f);
+    const float ndv = (nn.x * vx + nn.y * vy) + nn.z * vz;
+    const float fres = 0.1f + (1.0f - 0.1f) * powf(1.0f - ndv, 5.0f);
+    /* reflect(-viewer, normal) = -v - 2 dot(n, -v) n */
+    const float ndi = (nn.x * -vx + nn.y * -vy) + nn.z * -vz;
+    float rx = -vx - (2.0f * ndi) * nn.x, ry = -vy - (2.0f * ndi) * nn.y, rz = -vz - (2.0f * ndi) * nn.z;
+    norm3(rx, ry, rz);
+    const float4 refl = cube ? sample_cube(cube, S, rx, ry, rz) : zero;
+    float au = u + nn.x * 0.010f, av = v + nn.y * 0.010f;
+    if (sample1(depth, w, h, au, av) <= 0.0f) {
+        au = u;
+        av = v;
+    }
+    const float4 refr = bkg ? sample4(bkg, w, h, au, av) : zero;
+    const float t = 1.0f - fres;
+    const float fx = 0.2f * (1.0f - 0.7f) + (t * refr.x) * 0.7f;
+    const float fy = 0.2f * (1.0f - 0.7f) + (t * refr.y) * 0.7f;
+    const float fz = 0.5f * (1.0f - 0.7f) + (t * refr.z) * 0.7f;
+    out[k] = make_float4((fx + spec * 0.5f) + refl.x * fres, (fy + spec * 0.5f) + refl.y * fres,
+                         (fz + spec * 0.5f) + refl.z * fres, 1.0f);
+}
+
 inline dim3 grid2(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
 
 /* sizes the 16 x 16 pixel grids can cover */
@@ -386,6 +503,22 @@ int sph_render_normals(const float* d_depth, float* d_normals4, int width, int h
     const dim3 b(16, 16);
     sph::k_depth_normals<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(
         d_depth, reinterpret_cast<float4*>(d_normals4), width, height, ip);
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}
+
+int sph_render_shade(const float* d_depth, const float* d_normals4, const float* d_background4,
+                     const float* d_cube4, int cube_size, int width, int height, const float modelview[16],
+                     const float inv_projection[16], float* d_rgba, void* stream) {
+    if (!d_depth || !d_normals4 || !d_rgba || !modelview || !inv_projection || !sph::image_ok(width, height))
+        return SPH_E_INVALID;
+    if (d_cube4 && (cube_size <= 0 || cube_size > 16384)) return SPH_E_INVALID;
+    sph::Shade sh;
+    std::memcpy(sh.mv, modelview, sizeof sh.mv);
+    std::memcpy(sh.ip, inv_projection, sizeof sh.ip);
+    const dim3 b(16, 16);
+    sph::k_shade<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(
+        d_depth, reinterpret_cast<const float4*>(d_normals4), reinterpret_cast<const float4*>(d_background4),
+        reinterpret_cast<const float4*>(d_cube4), cube_size, width, height, sh, reinterpret_cast<float4*>(d_rgba));
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
 }
 

@@ -1,9 +1,8 @@
 """Host side of the screen-space fluid surface: the camera of scene/camera.cpp and the stage
 sequence of SSpaceFluidRenderer (fluid/render/sspacefluidrenderer.cpp), over the C ABI of
-include/sph_capi.h (sph_render_depth, sph_render_smooth, sph_render_normals).  Images are
-device tensors (torch is only the allocator here); the final shading pass of the reference
-(final_stage.frag: background, cube map, lights) belongs to its GL window and is not part
-of this module.
+include/sph_capi.h (sph_render_depth, sph_render_smooth, sph_render_normals,
+sph_render_shade).  Images are device tensors (torch is only the allocator here); the
+background the scene would draw behind the fluid and the skybox cube map are caller images.
 """
 import math
 
@@ -58,7 +57,7 @@ class Camera:
 class SSpaceFluidRenderer:
     """Depth, blur and normals stages of SSpaceFluidRenderer::render (:35-53) for one
     context.  filter_iterations: the blur stage runs the bilateral filter twice per
-    iteration (:390-408).  point_radius: the depth stage's sprite radius (0.0625 in the
+    iteration (:388-407).  point_radius: the depth stage's sprite radius (0.0625 in the
     reference, :365)."""
 
     def __init__(self, width, height, filter_iterations=2, point_radius=0.125 * 0.5):
@@ -70,6 +69,8 @@ class SSpaceFluidRenderer:
         self.depth = torch.zeros((self.height, self.width), dtype=torch.float32, device=dev)
         self.blurred = torch.zeros_like(self.depth)
         self.normals = torch.zeros((self.height, self.width, 4), dtype=torch.float32, device=dev)
+        self.color = torch.zeros((self.height, self.width, 4), dtype=torch.float32, device=dev)
+        self._mv = None
 
     def render(self, ctx, camera, mv_matrix, stream=None):
         """Renders ctx's fluid particles; returns (depth after the blur stage, normals).
@@ -86,4 +87,19 @@ class SSpaceFluidRenderer:
                            self.filter_iterations, s)
         capi.render_normals(self.depth.data_ptr(), self.normals.data_ptr(), self.width, self.height,
                             np.linalg.inv(pr.astype(np.float64)).astype(np.float32), s)
+        self._mv = np.asarray(mv_matrix, np.float32)
         return self.depth, self.normals
+
+    def shade(self, camera, background=None, cube_map=None, stream=None):
+        """_render_final_stage (final_stage.frag) after render(): the fluid's colour as an
+        (h, w, 4) device image.  background: (h, w, 4) float32 device tensor or None;
+        cube_map: (6, S, S, 4) float32 device tensor (faces +x, -x, +y, -y, +z, -z) or None."""
+        if self._mv is None:
+            raise RuntimeError("shade() needs render() first")
+        pr = camera.projection()
+        ipr = np.linalg.inv(pr.astype(np.float64)).astype(np.float32)
+        bg = 0 if background is None else background.data_ptr()
+        cube, size = (0, 0) if cube_map is None else (cube_map.data_ptr(), int(cube_map.shape[1]))
+        capi.render_shade(self.depth.data_ptr(), self.normals.data_ptr(), bg, cube, size, self.width, self.height,
+                          self._mv, ipr, self.color.data_ptr(), int(stream or 0))
+        return self.color

@@ -319,10 +319,10 @@ int sph_load_state(sph_ctx* ctx, const char* path);
 
 /* ---- screen-space surface ------------------------------------------------------------ */
 
-/* The depth, blur and normals stages of SSpaceFluidRenderer (fluid/render/
+/* The depth, blur, normals and final shading stages of SSpaceFluidRenderer (fluid/render/
  * sspacefluidrenderer.cpp:35-53) as CUDA kernels writing plain device images instead of
  * GL textures: row-major, row 0 at the bottom, width * height floats (depth) or float4
- * (normals).  Reads outside an image clamp to its edge.  All asynchronous. */
+ * (normals, colour).  Reads outside an image clamp to its edge.  All asynchronous. */
 typedef struct sph_view {
     float modelview[16];   /* mv_matrix, column-major like a GL uniform */
     float projection[16];  /* pr_matrix (camera.projection()), column-major */
@@ -330,7 +330,7 @@ typedef struct sph_view {
     float point_scale;     /* viewport width * tan(fov / 2) (:366) */
     int width, height;     /* image size in pixels: each 1..65536, at most 2^28 pixels */
 } sph_view;
-/* _render_depth_stage (:355-388) with shaders/sspace_fluid_rendering/depth_stage.vert and
+/* _render_depth_stage (:353-386) with shaders/sspace_fluid_rendering/depth_stage.vert and
  * .frag: every fluid particle of the context is a sphere sprite; d_depth receives at each
  * pixel the NDC depth of the nearest sprite fragment (GL_LESS on the normalised depth, the
  * lower particle index winning a tie) and 0 where no sprite covers it.  No background
@@ -340,17 +340,29 @@ int sph_render_depth(sph_ctx* ctx, const sph_view* view, float* d_depth);
 /* One pass of kernels/bilateral.cl (BilateralFilter::filter, filters/bilateralfilter.cpp:
  * 28-41): d_in and d_out must differ. */
 int sph_filter_bilateral(const float* d_in, float* d_out, int width, int height, void* cuda_stream);
-/* _render_blur_stage (:390-408): iterations times bilateral d_depth -> d_tmp -> d_depth. */
+/* _render_blur_stage (:388-407): iterations times bilateral d_depth -> d_tmp -> d_depth. */
 int sph_render_smooth(float* d_depth, float* d_tmp, int width, int height, int iterations, void* cuda_stream);
 /* One explicit step of kernels/curvatureflow.cl (screen-space mean-curvature flow; the
  * reference ships the kernel without a host caller).  inv_proj_x, inv_proj_y: the inverse
  * projection's x and y scale terms. */
 int sph_filter_curvature_flow(const float* d_in, float* d_out, int width, int height, float inv_proj_x,
                               float inv_proj_y, void* cuda_stream);
-/* _render_normals_stage (:410-434) with normals_stage.frag: view-space normals (x, y, z, 1)
+/* _render_normals_stage (:409-436) with normals_stage.frag: view-space normals (x, y, z, 1)
  * of the depth image, (0, 0, 0, 0) where depth <= 0.  inv_projection: column-major. */
 int sph_render_normals(const float* d_depth, float* d_normals4, int width, int height,
                        const float inv_projection[16], void* cuda_stream);
+/* _render_final_stage (:438-480) with final_stage.frag: the fluid's colour into d_rgba (float4
+ * per pixel, alpha 1).  Inputs: the blurred depth, the normals, a background image (float4
+ * per pixel, what the scene rendered behind the fluid; NULL = black) and a cube map for
+ * reflections (6 faces of cube_size^2 float4 texels in GL order +x, -x, +y, -y, +z, -z,
+ * row 0 at t = 0; NULL = black).  Blinn-Phong specular (exponent 50) for the light direction
+ * modelview * (0.7, 1, 0, 0), Schlick Fresnel (r0 = 0.1), reflection from the cube map,
+ * refraction of the background offset by 0.01 * normal.xy, attenuation colour
+ * (0.2, 0.2, 0.5); background where depth <= 0.  Offset reads are bilinear with clamped
+ * coordinates (GL_LINEAR), the cube map read bilinear within the selected face. */
+int sph_render_shade(const float* d_depth, const float* d_normals4, const float* d_background4,
+                     const float* d_cube4, int cube_size, int width, int height, const float modelview[16],
+                     const float inv_projection[16], float* d_rgba, void* cuda_stream);
 
 /* ---- primitives ---------------------------------------------------------------------- */
 

@@ -3,12 +3,14 @@ checker of fluids_gb300/csrc/sph_render.cu; nothing in the product imports it).
 
   splat_depth      shaders/sspace_fluid_rendering/depth_stage.vert:15-24 and depth_stage.frag:52-85
                    drawn as GL_POINTS in particle order with GL_LESS against a depth buffer
-                   cleared to 1 (fluid/render/sspacefluidrenderer.cpp:355-388); no background
+                   cleared to 1 (fluid/render/sspacefluidrenderer.cpp:353-386); no background
                    depth texture (fragments at normalised depth >= 1 are dropped)
   bilateral        kernels/bilateral.cl:5-47
   curvature_flow   kernels/curvatureflow.cl:54-129
   depth_normals    shaders/sspace_fluid_rendering/normals_stage.frag:108-144, sampling texel
                    centres with the coordinates clamped to the image
+  shade            shaders/sspace_fluid_rendering/final_stage.frag:25-74, offset reads bilinear
+                   (GL_LINEAR, clamped), the cube map by the OpenGL face table
 
 Images are (height, width) float32 arrays, row 0 at the bottom (window coordinates).
 Matrices are 4x4 in mathematical (row, column) layout.  splat_depth and depth_normals do
@@ -180,3 +182,90 @@ def look_at(eye, center, up):
     m[0, :3], m[1, :3], m[2, :3] = s, u, -f
     m[:3, 3] = -m[:3, :3] @ eye
     return m.astype(F)
+
+
+def _bilinear(img, u, v):
+    """GL_LINEAR read at normalised (u, v) with coordinates clamped to the edge texels;
+    img is (h, w) or (h, w, c)."""
+    h, w = img.shape[:2]
+    px = u * F(w) - F(0.5)
+    py = v * F(h) - F(0.5)
+    bx, by = np.floor(px), np.floor(py)
+    fx, fy = px - bx, py - by
+    x0 = np.clip(bx.astype(np.int64), 0, w - 1)
+    x1 = np.clip(bx.astype(np.int64) + 1, 0, w - 1)
+    y0 = np.clip(by.astype(np.int64), 0, h - 1)
+    y1 = np.clip(by.astype(np.int64) + 1, 0, h - 1)
+    if img.ndim == 3:
+        fx, fy = fx[..., None], fy[..., None]
+
+    def lerp(a, b, t):
+        return a * (F(1) - t) + b * t
+
+    return lerp(lerp(img[y0, x0], img[y0, x1], fx), lerp(img[y1, x0], img[y1, x1], fx), fy)
+
+
+def _cube(cube, r):
+    """GL cube-map read: major-axis face (+x, -x, +y, -y, +z, -z), the face's (s, t) by the
+    OpenGL face table, bilinear within the face.  cube: (6, S, S, 4); r: (..., 3)."""
+    rx, ry, rz = r[..., 0], r[..., 1], r[..., 2]
+    ax, ay, az = np.abs(rx), np.abs(ry), np.abs(rz)
+    xm = (ax >= ay) & (ax >= az)
+    ym = ~xm & (ay >= az)
+    face = np.where(xm, np.where(rx >= 0, 0, 1), np.where(ym, np.where(ry >= 0, 2, 3), np.where(rz >= 0, 4, 5)))
+    ma = np.where(xm, ax, np.where(ym, ay, az))
+    sc = np.where(xm, np.where(rx >= 0, -rz, rz), np.where(ym, rx, np.where(rz >= 0, rx, -rx)))
+    tc = np.where(xm, -ry, np.where(ym, np.where(ry >= 0, rz, -rz), -ry))
+    s = (sc / ma + F(1)) * F(0.5)
+    t = (tc / ma + F(1)) * F(0.5)
+    out = np.zeros(r.shape[:-1] + (4,), F)
+    for f in range(6):
+        m = face == f
+        if m.any():
+            out[m] = _bilinear(cube[f], s[m], t[m])
+    return out
+
+
+def shade(depth, normals, background, cube, modelview, inv_projection):
+    """final_stage.frag over a (h, w) blurred depth and (h, w, 4) normals; background
+    (h, w, 4) or None (black), cube (6, S, S, 4) or None (black).  Returns (h, w, 4)."""
+    z = np.asarray(depth, F)
+    h, w = z.shape
+    n = np.asarray(normals, F)
+    bkg = np.zeros((h, w, 4), F) if background is None else np.asarray(background, F)
+    mv = np.asarray(modelview, F).reshape(4, 4)
+    ip = np.asarray(inv_projection, F).reshape(4, 4)
+    one = F(1)
+    u = ((np.arange(w, dtype=F) + F(0.5)) * (one / F(w)))[None, :] + np.zeros((h, 1), F)
+    v = ((np.arange(h, dtype=F) + F(0.5)) * (one / F(h)))[:, None] + np.zeros((1, w), F)
+
+    def norm3(x, y, zz):
+        ln = np.sqrt((x * x + y * y) + zz * zz)
+        return x / ln, y / ln, zz / ln
+
+    with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+        ix, iy, iz = norm3(*(np.full((h, w), mv[k, 0] * F(0.7) + mv[k, 1] * F(1.0), F) for k in range(3)))
+        e = _mv(ip, [u * F(2) - one, v * F(2) - one, z, np.ones_like(z)])
+        p = [e[0] / e[3], e[1] / e[3], e[2] / e[3]]
+        vx, vy, vz = norm3(-p[0], -p[1], -p[2])
+        hx, hy, hz = norm3(ix + vx, iy + vy, iz + vz)
+        nx, ny, nz = n[..., 0], n[..., 1], n[..., 2]
+        spec = np.power(np.maximum(F(0), (hx * nx + hy * ny) + hz * nz), F(50))
+        ndv = (nx * vx + ny * vy) + nz * vz
+        fres = F(0.1) + (one - F(0.1)) * np.power(one - ndv, F(5))
+        ndi = (nx * -vx + ny * -vy) + nz * -vz
+        rx, ry, rz = norm3(-vx - (F(2) * ndi) * nx, -vy - (F(2) * ndi) * ny, -vz - (F(2) * ndi) * nz)
+        refl = np.zeros((h, w, 4), F) if cube is None else _cube(np.asarray(cube, F), np.stack([rx, ry, rz], -1))
+        au = u + nx * F(0.010)
+        av = v + ny * F(0.010)
+        off = _bilinear(z, au, av) <= 0
+        au = np.where(off, u, au)
+        av = np.where(off, v, av)
+        refr = _bilinear(bkg, au, av)
+        t = one - fres
+        att = np.array([0.2, 0.2, 0.5], F)
+        col = [(att[c] * (one - F(0.7)) + (t * refr[..., c]) * F(0.7) + spec * F(0.5)) + refl[..., c] * fres
+               for c in range(3)]
+        out = np.stack(col + [np.ones_like(z)], -1).astype(F)
+    back = np.concatenate([bkg[..., :3], np.ones((h, w, 1), F)], -1)
+    return np.where((z > 0)[..., None], out, back).astype(F)
