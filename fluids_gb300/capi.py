@@ -50,7 +50,7 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
            "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
            "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere", "sph_save_state", "sph_load_state",
-           "sph_inject_fault", "sph_render_shade"]
+           "sph_inject_fault", "sph_render_shade", "sph_scene_wall"]
 
 
 class SphParams(C.Structure):
@@ -186,6 +186,7 @@ def lib():
             "sph_scene_voxelize": (ip, [fp, ip, fp, ip, C.c_float, C.c_float, fp, ip]),
             "sph_scene_icosphere": (ip, [C.c_float, ip, fp, ip, fp, ip, C.POINTER(ip), C.POINTER(ip)]),
             "sph_scene_sphere": (ip, [C.c_float, C.c_float, fp, ip]),
+            "sph_scene_wall": (ip, [C.c_float, C.c_float, C.c_float, fp, ip]),
             "sph_save_state": (ip, [vp, C.c_char_p]),
             "sph_load_state": (ip, [vp, C.c_char_p]),
             "sph_inject_fault": (ip, [vp, ip]),

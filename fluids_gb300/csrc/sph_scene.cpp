@@ -9,6 +9,7 @@
  *                                 parsing rules (external/tinyobj/tiny_obj_loader.h)
  *   IcoSphereMesh                 mesh/icospheremesh.cpp:10-124
  *   Sphere::surface_sampling      scene/sphere.cpp:135-171 (body coordinates)
+ *   Wall::surface_sampling        scene/wall.cpp:142-152 (body coordinates)
  * plus a seeded jitter (splitmix64, Steele/Lea/Flood 2014) used by the benchmark scenes.
  * Built without floating-point contraction, so the samplers give the same bits on every
  * host.
@@ -290,6 +291,16 @@ int sph_scene_sphere(float radius, float spacing, float* out4, int cap) {
         }
     }
     for (size_t i = 0; i + 2 < v.size(); i += 3) o.push(v[i], v[i + 1], v[i + 2]);
+    return o.n;
+}
+
+int sph_scene_wall(float width, float height, float spacing, float* out4, int cap) {
+    if (!(spacing > 0.f) || !(width >= 0.f) || !(height >= 0.f)) return -1;
+    if ((double)width / spacing > 1e6 || (double)height / spacing > 1e6) return -1;
+    Out o{out4, cap, 0};
+    /* a plane at z = 0: x outer, y inner, float-accumulated steps */
+    for (float x = -width / 2; x <= width / 2; x += spacing)
+        for (float y = -height / 2; y <= height / 2; y += spacing) o.push(x, y, 0.f);
     return o.n;
 }
 

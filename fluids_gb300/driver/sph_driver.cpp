@@ -7,12 +7,13 @@
  * the scene from the reference's JSON format -- "container" {width, height, depth} becomes the
  * rectangular limits, "fluid_volumes" of type "box" {size, center} become BoxVolumes, and
  * "rigid_bodies" of type "cube" {size, center, rotation (x, y, z, w quaternion), mass},
- * "sphere" {size (the radius), center, mass} and "model" {obj_filename, center, rotation,
- * mass} become boundary bodies (movable when mass > 0, as scene.cpp:471 passes them, and then
+ * "sphere" {size (the radius), center, mass}, "model" {obj_filename, center, rotation, mass}
+ * and "wall" become boundary bodies (movable when mass > 0, as scene.cpp:471 passes them, and then
  * moved by the solver's own rigid-body step under the fluid's force and torque and gravity;
  * bodies do not collide with each other).  A model's OBJ path is taken as written when it
  * exists, else under --data-root, else under the directory two levels above the scene file
- * (the reference's data/scenes/ layout).  "wall" bodies are reported and skipped.  Options:
+ * (the reference's data/scenes/ layout); "wall" {size [width, height], center, rotation, mass}
+ * is a sampled plane.  Options:
  *
  *   sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]
  *              [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]
@@ -202,6 +203,8 @@ Scene load_scene(const std::string& path, bool container_boundary, const std::st
         else if (type == "sphere") body = std::make_shared<Sphere>((float)r["size"].number());
         else if (type == "model")
             body = std::make_shared<Model>(resolve_model(r["obj_filename"].str, path, data_root));
+        else if (type == "wall")
+            body = std::make_shared<Wall>((float)r["size"][0].number(), (float)r["size"][1].number());
         if (!body) {
             std::fprintf(stderr, "skipping rigid body '%s' of type '%s'\n", r["name"].str.c_str(), type.c_str());
             continue;

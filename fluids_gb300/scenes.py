@@ -135,6 +135,17 @@ class Sphere(RigidBody):
         return _sample(capi.lib().sph_scene_sphere, self.radius, float(spacing))
 
 
+class Wall(RigidBody):
+    """scene/wall.h: a width x height plane (z = 0 in body coordinates)."""
+
+    def __init__(self, width, height, mass=0.0, position=(0, 0, 0), rotation=None):
+        super().__init__(mass, position, rotation)
+        self.width, self.height = float(width), float(height)
+
+    def surface_sampling(self, spacing):
+        return _sample(capi.lib().sph_scene_wall, self.width, self.height, float(spacing))
+
+
 class Model(RigidBody):
     """scene/model.h: a triangle mesh read from an OBJ file, sampled by voxelizing it on the
     GPU (voxel size = particle spacing, precision = spacing / 10)."""

@@ -423,6 +423,9 @@ int sph_scene_icosphere(float radius, int level, float* vertices3, int vcap, uin
  * every mesh vertex; the corner reads and the area formula as written there.  Returns the
  * count, fills out4 up to cap. */
 int sph_scene_sphere(float radius, float spacing, float* out4, int cap);
+/* Wall::surface_sampling (scene/wall.cpp:142-152): a width x height plane at z = 0 in body
+ * coordinates.  Returns the count (-1 for bad arguments), fills out4 up to cap. */
+int sph_scene_wall(float width, float height, float spacing, float* out4, int cap);
 /* Adds U(-amp, amp) to x, y, z of every particle from a splitmix64 stream seeded by seed. */
 void sph_jitter(float* pos4, int n, float amp, uint64_t seed);
 

@@ -232,6 +232,27 @@ class Sphere : public RigidBody {
     float r_;
 };
 
+/* Wall (scene/wall.cpp:9-152): a plane sampled at z = 0; inertia of a thin plate,
+ * m / 12 (h^2, w^2, w^2 + h^2) (Bullet's btBox2dShape without its margin). */
+class Wall : public RigidBody {
+   public:
+    Wall(float width, float height) : w_(width), h_(height) {}
+    void inverse_inertia(float out[3]) const override {
+        const float I[3] = {mass / 12.f * (h_ * h_), mass / 12.f * (w_ * w_), mass / 12.f * (w_ * w_ + h_ * h_)};
+        for (int a = 0; a < 3; ++a) out[a] = I[a] > 0.f ? 1.0f / I[a] : 0.f;
+    }
+    float bounding_radius() const override { return 0.5f * std::sqrt(w_ * w_ + h_ * h_); }
+    std::vector<Float4> surface_sampling(float spacing) const override {
+        const int n = sph_scene_wall(w_, h_, spacing, nullptr, 0);
+        std::vector<Float4> out((size_t)(n > 0 ? n : 0));
+        if (n > 0) sph_scene_wall(w_, h_, spacing, &out[0].x, n);
+        return out;
+    }
+
+   private:
+    float w_, h_;
+};
+
 /* Model (scene/model.cpp:11-214): an OBJ mesh read as ModelMesh does, sampled by voxelizing
  * it on the GPU (voxel size = spacing, precision = spacing / 10).  Inertia: the box of the
  * mesh's bounding box, I = m / 12 (ly^2 + lz^2, lx^2 + lz^2, lx^2 + ly^2) -- Bullet's

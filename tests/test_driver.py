@@ -157,6 +157,17 @@ def model_scene(tmp_path, mass):
                               "center": [-0.15, 0.1, 0.0], "rotation": [0, 1, 0, 0.5]}]}
 
 
+def test_driver_samples_wall_bodies(driver, tmp_path):
+    scene = dict(SCENE)
+    scene["rigid_bodies"] = [{"type": "wall", "name": "w", "mass": 0.0, "size": [0.3, 0.2],
+                              "center": [0.0, 0.0, 0.1], "rotation": [0, 0, 0, 1]}]
+    c, s = write(tmp_path, scene=scene)
+    r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    from fluids_gb300.scenes import Wall
+    assert json.loads(r.stdout)["boundary_particles"] == len(Wall(0.3, 0.2).surface_sampling(0.015))
+
+
 def test_driver_reads_model_bodies(driver, tmp_path):
     """A "model" body is read from its OBJ file (found under --data-root); its voxel
     sampling runs on the GPU, so a dry run reports it without sampling it."""

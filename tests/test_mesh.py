@@ -132,3 +132,19 @@ def test_gpu_voxelizer_edge_cases(gpu_lib):
     assert L.sph_scene_voxelize(capi.ptr(tri), 3, capi.ptr(ix), 2, 0.25, 0.025, None, 0) == -capi.SPH_E_INVALID
     assert L.sph_scene_voxelize(capi.ptr(tri), 3, capi.ptr(ix), 3, 0.0, 0.0, None, 0) == -capi.SPH_E_INVALID
     assert L.sph_scene_voxelize(capi.ptr(tri), 3, capi.ptr(ix), 3, 1e-4, 1e-5, None, 0) == -capi.SPH_E_OVERFLOW
+
+
+def test_wall_sampling_matches_restatement():
+    """Wall::surface_sampling (scene/wall.cpp:142-152): x outer, y inner, float steps."""
+    from fluids_gb300.scenes import Wall
+    for w, h, s in ((0.5, 0.3, 0.015), (1.0, 0.2, 0.03), (0.0, 0.1, 0.02)):
+        got = Wall(w, h).surface_sampling(s)
+        want = []
+        x = -np.float32(w) / np.float32(2)
+        while x <= np.float32(w) / np.float32(2):
+            y = -np.float32(h) / np.float32(2)
+            while y <= np.float32(h) / np.float32(2):
+                want.append((x, y, 0.0, 1.0))
+                y = np.float32(y + np.float32(s))
+            x = np.float32(x + np.float32(s))
+        assert np.array_equal(got, np.array(want, np.float32).reshape(-1, 4))
