@@ -17,7 +17,12 @@
  *
  *   sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]
  *              [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]
- *              [--data-root DIR] [--save FILE] [--resume FILE]
+ *              [--data-root DIR] [--save FILE] [--resume FILE] [--performance_output FILE]
+ *
+ * -c / -s / -o are the reference's own short forms of --config / --scene /
+ * --performance_output (main.cpp:15-19); the last writes one frames-per-second value per
+ * line, each the average of 6 steps (gui/glwidget.cpp:62-73, gui/mainwindow.cpp:99-101),
+ * a frame here being one solver step.
  *
  * Prints one JSON line per K steps with the solver statistics and a final line with the
  * wall-clock throughput.  --dump writes the final positions ordered by particle id (float32
@@ -240,14 +245,14 @@ int usage() {
     std::fprintf(stderr,
                  "usage: sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]\n"
                  "                  [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]\n"
-                 "                  [--data-root DIR] [--save FILE] [--resume FILE]\n");
+                 "                  [--data-root DIR] [--save FILE] [--resume FILE] [-o FILE]\n");
     return 2;
 }
 
 }  // namespace
 
 int main(int argc, char** argv) {
-    std::string config, scene_file, dump, mode = "physics", data_root, save, resume;
+    std::string config, scene_file, dump, mode = "physics", data_root, save, resume, fps_out;
     int steps = 100, every = 0;
     bool dry = false, container_boundary = false;
     long long jitter = -1;
@@ -258,8 +263,9 @@ int main(int argc, char** argv) {
             return argv[++a];
         };
         try {
-            if (k == "--config") config = next();
-            else if (k == "--scene") scene_file = next();
+            if (k == "--config" || k == "-c") config = next();
+            else if (k == "--scene" || k == "-s") scene_file = next();
+            else if (k == "--performance_output" || k == "-o") fps_out = next();
             else if (k == "--steps") steps = std::atoi(next().c_str());
             else if (k == "--every") every = std::atoi(next().c_str());
             else if (k == "--mode") mode = next();
@@ -309,9 +315,22 @@ int main(int argc, char** argv) {
         const char* names[8] = {"mean_compression", "mean_abs_density_error", "max_density_error", "kinetic",
                                 "potential", "com_x", "com_y", "com_z"};
         fluid->synchronize();
+        std::ofstream fps;
+        if (!fps_out.empty()) {
+            fps.open(fps_out);
+            if (!fps.good()) throw Error(SPH_E_INVALID, "cannot write " + fps_out);
+        }
         const auto t0 = std::chrono::steady_clock::now();
+        auto tf = t0;
         for (int s = 1; s <= steps; ++s) {
             fluid->simulate();
+            if (fps.is_open() && s % 6 == 0) {   /* frames per second over the last 6 steps */
+                fluid->synchronize();
+                const auto now = std::chrono::steady_clock::now();
+                const double ms = std::chrono::duration<double, std::milli>(now - tf).count();
+                tf = now;
+                fps << (ms > 0 ? 1000.0 / (ms / 6.0) : 0.0) << "\n";
+            }
             if (every > 0 && s % every == 0) {
                 const std::vector<double> st = fluid->stats();
                 std::printf("{\"step\": %d", s);

@@ -197,3 +197,15 @@ def test_driver_runs_model_scene(gpu_lib, driver, tmp_path):
     for n, yy in zip((50, 100), y):
         assert yy == pytest.approx(0.1 - g * dt * dt * n * (n + 1) / 2, abs=1e-5)
     assert lines[-1]["flags"] == 0
+
+
+@pytest.mark.gpu
+def test_driver_reference_short_options_and_fps_output(gpu_lib, driver, tmp_path):
+    """-c / -s / -o as the reference's main.cpp takes them; -o writes one FPS value per 6
+    steps."""
+    c, s = write(tmp_path)
+    out = tmp_path / "fps.txt"
+    r = subprocess.run([driver, "-c", c, "-s", s, "-o", str(out), "--steps", "18"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    vals = [float(x) for x in out.read_text().split()]
+    assert len(vals) == 3 and all(v > 0 for v in vals)
