@@ -374,11 +374,12 @@ def bench_pcisph(torch, steps, warmup):
 def bench_render(torch, ctx, stream, frames, width=1920, height=1080):
     """Screen-space surface of the context's particles (depth sprites, two blur iterations,
     normals, final shading over a background gradient with a random 256^2 cube map) at
-    width x height with the reference's default camera and sprite radius; device time per
+    width x height with the reference's default camera (view and projection) and sprite
+    radius; device time per
     stage from CUDA events on the context stream, averaged over `frames` frames."""
     from fluids_gb300 import capi, render
     cam = render.Camera(width, height)
-    mv = render.look_at((1.0, 1.3, 3.2), (1.0, 0.25, 0.5), (0.0, 1.0, 0.0))
+    mv = cam.transformation()   # the reference's default view of the container
     r = render.SSpaceFluidRenderer(width, height)
     s = stream.cuda_stream
     for _ in range(3):

@@ -50,7 +50,7 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
            "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
            "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere", "sph_save_state", "sph_load_state",
-           "sph_inject_fault", "sph_render_shade", "sph_scene_wall"]
+           "sph_inject_fault", "sph_render_shade", "sph_scene_wall", "sph_render_frame"]
 
 
 class SphParams(C.Structure):
@@ -187,6 +187,7 @@ def lib():
             "sph_scene_icosphere": (ip, [C.c_float, ip, fp, ip, fp, ip, C.POINTER(ip), C.POINTER(ip)]),
             "sph_scene_sphere": (ip, [C.c_float, C.c_float, fp, ip]),
             "sph_scene_wall": (ip, [C.c_float, C.c_float, C.c_float, fp, ip]),
+            "sph_render_frame": (ip, [vp, C.POINTER(SphView), ip, fp]),
             "sph_save_state": (ip, [vp, C.c_char_p]),
             "sph_load_state": (ip, [vp, C.c_char_p]),
             "sph_inject_fault": (ip, [vp, ip]),
@@ -381,6 +382,12 @@ class Context:
     def inject_fault(self, kind):
         """sph_inject_fault (failure-detection tests)."""
         self._c(self._lib.sph_inject_fault(self.h, int(kind)))
+
+    def render_frame(self, view, filter_iterations=2):
+        """sph_render_frame: a shaded (h, w, 4) float32 host image of the particles."""
+        out = np.zeros((view.height, view.width, 4), np.float32)
+        self._c(self._lib.sph_render_frame(self.h, C.byref(view), int(filter_iterations), ptr(out)))
+        return out
 
     def save_state(self, path):
         """Checkpoint (sph_save_state)."""

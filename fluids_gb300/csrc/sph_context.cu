@@ -950,6 +950,7 @@ int sph_destroy(sph_ctx* x) {
     free_arena(x);
     cudaFree(x->render_buf);
     cudaFree(x->render_sort);
+    cudaFree(x->frame_buf);
     if (x->own_stream && x->stream) cudaStreamDestroy(x->stream);
     delete x;
     return SPH_OK;

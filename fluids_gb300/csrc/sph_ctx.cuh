@@ -67,6 +67,8 @@ struct sph_ctx {
     size_t render_pixels = 0;
     void* render_sort = nullptr;   /* sph_render_depth: 16-bit depth keys and particle order */
     size_t render_sort_bytes = 0;
+    void* frame_buf = nullptr;     /* sph_render_frame: depth, blur scratch, normals, colour */
+    size_t frame_pixels = 0;
 };
 
 /* Records msg as the context's last error (or the last creation error) and returns code. */

@@ -22,7 +22,9 @@
  * Images are row-major, row 0 at the bottom (window coordinates), single-channel float
  * (depth) or float4 (normals); reads outside the image clamp to the edge.
  */
+#include <cmath>
 #include <cstring>
+#include <utility>
 
 #include "sph_ctx.cuh"
 
@@ -504,6 +506,72 @@ int sph_render_normals(const float* d_depth, float* d_normals4, int width, int h
     sph::k_depth_normals<<<sph::grid2(width, height, b), b, 0, (cudaStream_t)stream>>>(
         d_depth, reinterpret_cast<float4*>(d_normals4), width, height, ip);
     return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}
+
+/* 4x4 inverse (column-major in and out) by Gauss-Jordan elimination in double. */
+static bool invert4(const float* a, float* out) {
+    double m[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            m[r][c] = a[c * 4 + r];
+            m[r][c + 4] = r == c ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(m[r][c]) > std::fabs(m[p][c])) p = r;
+        if (std::fabs(m[p][c]) < 1e-300) return false;
+        if (p != c)
+            for (int k = 0; k < 8; ++k) std::swap(m[p][k], m[c][k]);
+        const double d = m[c][c];
+        for (int k = 0; k < 8; ++k) m[c][k] /= d;
+        for (int r = 0; r < 4; ++r)
+            if (r != c) {
+                const double f = m[r][c];
+                for (int k = 0; k < 8; ++k) m[r][k] -= f * m[c][k];
+            }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) out[c * 4 + r] = (float)m[r][c + 4];
+    return true;
+}
+
+int sph_render_frame(sph_ctx* x, const sph_view* view, int filter_iterations, float* rgba_host) {
+    if (!x || !view || !rgba_host || filter_iterations < 0) return SPH_E_INVALID;
+    if (!sph::image_ok(view->width, view->height))
+        return sph_ctx_fail(x, SPH_E_INVALID, "render: width and height must be 1..65536 (at most 2^28 pixels)");
+    float ip[16];
+    if (!invert4(view->projection, ip)) return sph_ctx_fail(x, SPH_E_INVALID, "render: singular projection");
+    const int w = view->width, h = view->height;
+    const size_t npix = (size_t)w * h;
+    if (x->frame_pixels < npix) {
+        cudaStreamSynchronize(x->stream);
+        cudaFree(x->frame_buf);
+        x->frame_buf = nullptr;
+        x->frame_pixels = 0;
+        if (cudaMalloc(&x->frame_buf, 40 * npix) != cudaSuccess) {
+            cudaGetLastError();
+            return sph_ctx_fail(x, SPH_E_NOMEM, "render: frame images");
+        }
+        x->frame_pixels = npix;
+    }
+    float* depth = static_cast<float*>(x->frame_buf);
+    float* tmp = depth + npix;
+    float* normals = tmp + npix;
+    float* color = normals + 4 * npix;
+    void* s = x->stream;
+    int rc = sph_render_depth(x, view, depth);
+    if (rc == SPH_OK) rc = sph_render_smooth(depth, tmp, w, h, filter_iterations, s);
+    if (rc == SPH_OK) rc = sph_render_normals(depth, normals, w, h, ip, s);
+    if (rc == SPH_OK)
+        rc = sph_render_shade(depth, normals, nullptr, nullptr, 0, w, h, view->modelview, ip, color, s);
+    if (rc != SPH_OK) return sph_ctx_fail(x, rc, "render: frame stages");
+    if (cudaMemcpyAsync(rgba_host, color, 16 * npix, cudaMemcpyDeviceToHost, x->stream) != cudaSuccess ||
+        cudaStreamSynchronize(x->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return sph_ctx_fail(x, SPH_E_CUDA, "render: frame copy");
+    }
+    return SPH_OK;
 }
 
 int sph_render_shade(const float* d_depth, const float* d_normals4, const float* d_background4,

@@ -24,6 +24,13 @@
  * line, each the average of 6 steps (gui/glwidget.cpp:62-73, gui/mainwindow.cpp:99-101),
  * a frame here being one solver step.
  *
+ * --frames DIR writes the screen-space surface (sph_render_frame: depth sprites, two blur
+ * iterations, normals, final shading over black) as DIR/frame_NNNNN.ppm every
+ * --frame-every K steps (default 10) at --frame-size WxH (default 1280x720), seen by the
+ * reference's default camera (fov 45, near 0.5, far 30; translate(0, 0, -4) . rotate 45
+ * degrees about x; scene/camera.cpp:4-21, gui/glwidget.cpp:82-88) with its sprite radius
+ * 0.0625 (fluid/render/sspacefluidrenderer.cpp:365-366).
+ *
  * Prints one JSON line per K steps with the solver statistics and a final line with the
  * wall-clock throughput.  --dump writes the final positions ordered by particle id (float32
  * x, y, z, w per particle).  --save writes a checkpoint after the last step; --resume loads
@@ -241,18 +248,67 @@ class Jittered : public FluidVolume {
     uint64_t seed_;
 };
 
+/* The reference's default camera as an sph_view (column-major matrices). */
+sph_view default_view(int w, int h) {
+    sph_view v{};
+    const double fov = 45.0, n = 0.5, f = 30.0, aspect = (double)w / (h ? h : 1);
+    const double ct = 1.0 / std::tan(fov * 3.14159265358979323846 / 360.0);
+    double pr[16] = {0};
+    pr[0] = ct / aspect;
+    pr[5] = ct;
+    pr[10] = -(f + n) / (f - n);
+    pr[11] = -1.0;
+    pr[14] = -2.0 * f * n / (f - n);
+    const double c = std::cos(3.14159265358979323846 / 4), s = std::sin(3.14159265358979323846 / 4);
+    /* translate(0, 0, -4) . rotate(45 deg about x) */
+    const double mv[16] = {1, 0, 0, 0, 0, c, s, 0, 0, -s, c, 0, 0, 0, -4, 1};
+    for (int k = 0; k < 16; ++k) {
+        v.projection[k] = (float)pr[k];
+        v.modelview[k] = (float)mv[k];
+    }
+    v.point_radius = 0.0625f;
+    v.point_scale = (float)(w * std::tan(fov * 3.14159265358979323846 / 360.0));
+    v.width = w;
+    v.height = h;
+    return v;
+}
+
+std::string pad5(int k) {
+    char b[16];
+    std::snprintf(b, sizeof b, "%05d", k);
+    return b;
+}
+
+/* 8-bit binary PPM, top row first (the image's row 0 is the bottom) */
+void write_ppm(const std::string& path, const std::vector<float>& rgba, int w, int h) {
+    std::ofstream out(path, std::ios::binary);
+    if (!out) throw Error(SPH_E_INVALID, "cannot write " + path);
+    out << "P6\n" << w << " " << h << "\n255\n";
+    std::vector<unsigned char> row(3 * (size_t)w);
+    for (int y = h - 1; y >= 0; --y) {
+        for (int x = 0; x < w; ++x)
+            for (int c = 0; c < 3; ++c) {
+                const float v = rgba[4 * ((size_t)y * w + x) + c];
+                row[3 * (size_t)x + c] = (unsigned char)(v <= 0.f ? 0 : (v >= 1.f ? 255 : (int)(v * 255.f + 0.5f)));
+            }
+        out.write(reinterpret_cast<const char*>(row.data()), (std::streamsize)row.size());
+    }
+}
+
 int usage() {
     std::fprintf(stderr,
                  "usage: sph_driver --config FILE --scene FILE [--steps N] [--every K] [--mode physics|compat]\n"
                  "                  [--container-boundary] [--jitter SEED] [--dump FILE] [--dry-run]\n"
-                 "                  [--data-root DIR] [--save FILE] [--resume FILE] [-o FILE]\n");
+                 "                  [--data-root DIR] [--save FILE] [--resume FILE] [-o FILE]\n"
+                 "                  [--frames DIR] [--frame-every K] [--frame-size WxH]\n");
     return 2;
 }
 
 }  // namespace
 
 int main(int argc, char** argv) {
-    std::string config, scene_file, dump, mode = "physics", data_root, save, resume, fps_out;
+    std::string config, scene_file, dump, mode = "physics", data_root, save, resume, fps_out, frames;
+    int frame_every = 10, frame_w = 1280, frame_h = 720;
     int steps = 100, every = 0;
     bool dry = false, container_boundary = false;
     long long jitter = -1;
@@ -275,6 +331,12 @@ int main(int argc, char** argv) {
             else if (k == "--dry-run") dry = true;
             else if (k == "--data-root") data_root = next();
             else if (k == "--save") save = next();
+            else if (k == "--frames") frames = next();
+            else if (k == "--frame-every") frame_every = std::atoi(next().c_str());
+            else if (k == "--frame-size") {
+                const std::string v = next();
+                if (std::sscanf(v.c_str(), "%dx%d", &frame_w, &frame_h) != 2) throw Error(SPH_E_INVALID, "--frame-size WxH");
+            }
             else if (k == "--resume") resume = next();
             else return usage();
         } catch (const Error& e) {
@@ -287,6 +349,7 @@ int main(int argc, char** argv) {
         PhysicsSettings phys;
         SimulationSettings sim;
         load_settings(config, phys, sim);
+        load_graphics_settings(config);   /* validates render_method as the reference does */
         Scene sc = load_scene(scene_file, container_boundary, data_root);
         if (jitter >= 0)
             for (size_t v = 0; v < sc.volumes.size(); ++v)
@@ -322,8 +385,13 @@ int main(int argc, char** argv) {
         }
         const auto t0 = std::chrono::steady_clock::now();
         auto tf = t0;
+        const sph_view view = default_view(frame_w, frame_h);
+        int frame_no = 0;
         for (int s = 1; s <= steps; ++s) {
             fluid->simulate();
+            if (!frames.empty() && frame_every > 0 && s % frame_every == 0)
+                write_ppm(frames + "/frame_" + pad5(frame_no++) + ".ppm", fluid->render_frame(view, 2), frame_w,
+                          frame_h);
             if (fps.is_open() && s % 6 == 0) {   /* frames per second over the last 6 steps */
                 fluid->synchronize();
                 const auto now = std::chrono::steady_clock::now();

@@ -38,13 +38,35 @@ def look_at(eye, center, up):
     return m.astype(np.float32)
 
 
-class Camera:
-    """The reference's default camera (gui/glwidget.cpp:82-88): fov 45 degrees, near 0.5,
-    far 30, aspect = width / height."""
+def _rotation(angle_deg, axis):
+    """QMatrix4x4::rotate's matrix for a unit axis (mathematical layout)."""
+    a = math.radians(angle_deg)
+    c, s = math.cos(a), math.sin(a)
+    x, y, z = axis
+    m = np.eye(4)
+    m[:3, :3] = [[c + x * x * (1 - c), x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
+                 [y * x * (1 - c) + z * s, c + y * y * (1 - c), y * z * (1 - c) - x * s],
+                 [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + z * z * (1 - c)]]
+    return m
 
-    def __init__(self, width, height, fov=45.0, near=0.5, far=30.0):
+
+class Camera:
+    """The reference's default camera: perspective fov 45 degrees, near 0.5, far 30, aspect =
+    width / height (gui/glwidget.cpp:82-88) and the view transformation translate(0, 0, -zoom)
+    . rotate(roll about x) . rotate(pitch about y) with zoom 4, roll 45, pitch 0
+    (scene/camera.cpp:4-21)."""
+
+    def __init__(self, width, height, fov=45.0, near=0.5, far=30.0, zoom=4.0, roll=45.0, pitch=0.0):
         self.width, self.height = int(width), int(height)
         self.fov, self.near, self.far = float(fov), float(near), float(far)
+        self.zoom, self.roll, self.pitch = float(zoom), float(roll), float(pitch)
+
+    def transformation(self):
+        """Camera::transformation(): the fluid's modelview (scene/fluid.cpp:55-60, fluid at
+        the origin)."""
+        t = np.eye(4)
+        t[2, 3] = -self.zoom
+        return (t @ _rotation(self.roll, (1, 0, 0)) @ _rotation(self.pitch, (0, 1, 0))).astype(np.float32)
 
     def projection(self):
         return perspective(self.fov, self.width / max(self.height, 1), self.near, self.far)

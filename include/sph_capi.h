@@ -363,6 +363,12 @@ int sph_render_normals(const float* d_depth, float* d_normals4, int width, int h
 int sph_render_shade(const float* d_depth, const float* d_normals4, const float* d_background4,
                      const float* d_cube4, int cube_size, int width, int height, const float modelview[16],
                      const float inv_projection[16], float* d_rgba, void* cuda_stream);
+/* A headless frame: SSpaceFluidRenderer::render (:35-53) on the context's particles — depth,
+ * filter_iterations blur iterations, normals and the final stage over a black background
+ * without a cube map — into rgba_host (width * height float4, row 0 at the bottom).  The
+ * device images are the context's (40 bytes per pixel, kept for the next frame); the inverse
+ * projection is computed from view->projection.  Synchronous. */
+int sph_render_frame(sph_ctx* ctx, const sph_view* view, int filter_iterations, float* rgba_host);
 
 /* ---- primitives ---------------------------------------------------------------------- */
 

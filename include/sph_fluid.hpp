@@ -81,6 +81,11 @@ struct DeviceOptions {
     void* cuda_stream = nullptr;          /* null: the context creates its own */
 };
 
+/* GraphicsSettings (settings/graphicssettings.h): the render method of the config file. */
+struct GraphicsSettings {
+    enum RenderMethod { PARTICLES, SCREEN_SPACE } render_method = PARTICLES;
+};
+
 /* Settings::load (settings/settings.cpp:14-59) over FileParser's key=value format
  * (settings/fileparser.cpp:7-27): '#' starts a comment, every key of the simulation and
  * physics settings is required, method is wcsph or pcisph. */
@@ -122,6 +127,30 @@ inline void load_settings(const std::string& path, PhysicsSettings& phys, Simula
     phys.gravity = (float)std::atof(opt("gravity").c_str());
     phys.gas_stiffness = (float)std::atof(opt("gas_stiffness").c_str());
     phys.surface_tension = (float)std::atof(opt("surface_tension").c_str());
+}
+
+/* The graphics part of the same file: render_method = particles | screenspace (absent:
+ * particles; the headless tools need no window to read it). */
+inline GraphicsSettings load_graphics_settings(const std::string& path) {
+    GraphicsSettings g;
+    std::ifstream in(path);
+    if (!in) throw Error(SPH_E_INVALID, "cannot open settings file '" + path + "'");
+    std::string line;
+    while (std::getline(in, line)) {
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line.resize(hash);
+        const size_t eq = line.find('=');
+        if (eq == std::string::npos) continue;
+        std::istringstream k(line.substr(0, eq)), v(line.substr(eq + 1));
+        std::string key, val;
+        k >> key;
+        v >> val;
+        if (key != "render_method") continue;
+        if (val == "particles") g.render_method = GraphicsSettings::PARTICLES;
+        else if (val == "screenspace") g.render_method = GraphicsSettings::SCREEN_SPACE;
+        else throw Error(SPH_E_INVALID, "Unknown rendering method '" + val + "'!");
+    }
+    return g;
 }
 
 /* FluidVolume (fluid/simulation/fluidvolume.h): a block of fluid sampled at a radius. */
@@ -456,6 +485,12 @@ class CudaFluidSimulation : public FluidSimulation {
     void synchronize() { check(sph_synchronize(ctx_), ctx_); }
     /* checkpoint / resume (sph_save_state / sph_load_state) */
     void save_state(const std::string& path) { check(sph_save_state(ctx_, path.c_str()), ctx_); }
+    /* a shaded screen-space frame of the particles (sph_render_frame) */
+    std::vector<float> render_frame(const sph_view& view, int filter_iterations) {
+        std::vector<float> rgba(4 * (size_t)view.width * view.height);
+        check(sph_render_frame(ctx_, &view, filter_iterations, rgba.data()), ctx_);
+        return rgba;
+    }
     void load_state(const std::string& path) { check(sph_load_state(ctx_, path.c_str()), ctx_); }
     sph_ctx* handle() { return ctx_; }
 

@@ -63,6 +63,14 @@ def test_driver_parses_reference_formats(driver, tmp_path):
     assert out["method"] == "wcsph" and out["bodies"] == 3 and out["device_sampled_bodies"] == 0
 
 
+def test_driver_checks_render_method(driver, tmp_path):
+    """render_method is particles or screenspace (settings/settings.cpp:47-57)."""
+    for val, rc in (("particles", 0), ("screenspace", 0), ("raytraced", 1)):
+        c, s = write(tmp_path, config=CONFIG + "render_method=%s\n" % val)
+        r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run"], capture_output=True, text=True)
+        assert r.returncode == rc, (val, r.stderr)
+
+
 def test_driver_rejects_incomplete_settings(driver, tmp_path):
     c, s = write(tmp_path, config=CONFIG.replace("gas_stiffness=57142.857\n", ""))
     r = subprocess.run([driver, "--config", c, "--scene", s, "--dry-run"], capture_output=True, text=True)
@@ -209,3 +217,19 @@ def test_driver_reference_short_options_and_fps_output(gpu_lib, driver, tmp_path
     assert r.returncode == 0, r.stderr
     vals = [float(x) for x in out.read_text().split()]
     assert len(vals) == 3 and all(v > 0 for v in vals)
+
+
+@pytest.mark.gpu
+def test_driver_writes_screen_space_frames(gpu_lib, driver, tmp_path):
+    c, s = write(tmp_path)
+    frames = tmp_path / "frames"
+    frames.mkdir()
+    r = subprocess.run([driver, "-c", c, "-s", s, "--steps", "20", "--frames", str(frames), "--frame-every", "10",
+                        "--frame-size", "160x90"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    files = sorted(frames.iterdir())
+    assert [f.name for f in files] == ["frame_00000.ppm", "frame_00001.ppm"]
+    raw = files[-1].read_bytes()
+    assert raw.startswith(b"P6\n160 90\n255\n") and len(raw) == len(b"P6\n160 90\n255\n") + 160 * 90 * 3
+    img = np.frombuffer(raw[len(b"P6\n160 90\n255\n"):], np.uint8)
+    assert img.max() > 0    # the fluid is in view of the default camera

@@ -269,3 +269,27 @@ def test_gpu_shade_matches_restatement(gpu_lib):
     torch.cuda.synchronize()
     want = orender.shade(g["smooth2"], g["normals"], None, None, g["modelview"], g["inv_projection"])
     assert np.abs(out.cpu().numpy().astype(np.float64) - want).max() <= 2e-5
+
+
+@pytest.mark.gpu
+def test_gpu_render_frame_equals_the_stage_sequence(gpu_lib):
+    """sph_render_frame (host image) equals depth -> 2 blur iterations -> normals -> shade
+    called one by one (no background, no cube map), up to the last bits of the inverse
+    projection (inverted in C there, by numpy here)."""
+    import torch
+    from fluids_gb300 import render
+    g = golden()
+    w, h = int(g["width"]), int(g["height"])
+    ctx = _context(g["pos"])
+    view = capi.make_view(g["modelview"], g["projection"], g["point_radius"], g["point_scale"], w, h)
+    frame = ctx.render_frame(view, 2)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    cam = render.Camera(w, h)
+    r = render.SSpaceFluidRenderer(w, h, filter_iterations=2, point_radius=float(g["point_radius"]))
+    r.render(ctx, cam, g["modelview"], stream.cuda_stream)
+    col = r.shade(cam, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    ref = col.cpu().numpy()
+    assert np.abs(frame.astype(np.float64) - ref).max() <= 1e-4
+    assert np.array_equal(frame[..., 3], ref[..., 3]) and frame[..., :3].max() > 0
