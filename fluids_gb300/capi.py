@@ -50,7 +50,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
            "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
            "sph_scene_voxelize", "sph_scene_icosphere", "sph_scene_sphere", "sph_save_state", "sph_load_state",
-           "sph_inject_fault", "sph_render_shade", "sph_scene_wall", "sph_render_frame"]
+           "sph_inject_fault", "sph_render_shade", "sph_scene_wall", "sph_render_frame",
+           "sph_render_particles"]
 
 
 class SphParams(C.Structure):
@@ -107,6 +108,24 @@ def make_view(modelview, projection, point_radius, point_scale, width, height):
     v.width = int(width)
     v.height = int(height)
     return v
+
+
+class SphLight(C.Structure):
+    _fields_ = [("direction", C.c_float * 3), ("diffuse", C.c_float * 4)]
+
+
+def make_lights(lights):
+    """[(direction (3,), diffuse rgba (4,) in 0..1)] -> ctypes array of SphLight."""
+    arr = (SphLight * max(1, len(lights)))()
+    for k, (d, c) in enumerate(lights):
+        for a in range(3):
+            arr[k].direction[a] = float(d[a])
+        for a in range(4):
+            arr[k].diffuse[a] = float(c[a])
+    return arr
+
+
+SPH_RENDER_PARTICLES, SPH_RENDER_SCREEN_SPACE = 0, 1
 
 
 class SphError(RuntimeError):
@@ -187,7 +206,8 @@ def lib():
             "sph_scene_icosphere": (ip, [C.c_float, ip, fp, ip, fp, ip, C.POINTER(ip), C.POINTER(ip)]),
             "sph_scene_sphere": (ip, [C.c_float, C.c_float, fp, ip]),
             "sph_scene_wall": (ip, [C.c_float, C.c_float, C.c_float, fp, ip]),
-            "sph_render_frame": (ip, [vp, C.POINTER(SphView), ip, fp]),
+            "sph_render_frame": (ip, [vp, C.POINTER(SphView), ip, ip, vp, ip, fp]),
+            "sph_render_particles": (ip, [vp, C.POINTER(SphView), vp, ip, vp]),
             "sph_save_state": (ip, [vp, C.c_char_p]),
             "sph_load_state": (ip, [vp, C.c_char_p]),
             "sph_inject_fault": (ip, [vp, ip]),
@@ -383,11 +403,21 @@ class Context:
         """sph_inject_fault (failure-detection tests)."""
         self._c(self._lib.sph_inject_fault(self.h, int(kind)))
 
-    def render_frame(self, view, filter_iterations=2):
-        """sph_render_frame: a shaded (h, w, 4) float32 host image of the particles."""
+    def render_frame(self, view, filter_iterations=2, method=None, lights=()):
+        """sph_render_frame: a shaded (h, w, 4) float32 host image of the particles
+        (screen-space surface by default; method SPH_RENDER_PARTICLES with lights)."""
         out = np.zeros((view.height, view.width, 4), np.float32)
-        self._c(self._lib.sph_render_frame(self.h, C.byref(view), int(filter_iterations), ptr(out)))
+        m = SPH_RENDER_SCREEN_SPACE if method is None else int(method)
+        arr = make_lights(lights)
+        self._c(self._lib.sph_render_frame(self.h, C.byref(view), m, int(filter_iterations), C.cast(arr, C.c_void_p),
+                                           len(lights), ptr(out)))
         return out
+
+    def render_particles(self, view, lights, d_rgba):
+        """sph_render_particles into the device image at d_rgba."""
+        arr = make_lights(lights)
+        self._c(self._lib.sph_render_particles(self.h, C.byref(view), C.cast(arr, C.c_void_p), len(lights),
+                                               C.c_void_p(int(d_rgba))))
 
     def save_state(self, path):
         """Checkpoint (sph_save_state)."""

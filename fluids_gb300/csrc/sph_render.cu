@@ -19,6 +19,8 @@
  *                    depth jump, normal = normalize(ddx x ddy).
  *   k_shade          shaders/sspace_fluid_rendering/final_stage.frag: the fluid's colour over
  *                    a background image with a cube map for reflections, into an RGBA image.
+ *   k_particle_*     shaders/particles.vert and .frag (the "particles" render method): the
+ *                    same sprites depth-tested at their centres and lit by directional lights.
  * Images are row-major, row 0 at the bottom (window coordinates), single-channel float
  * (depth) or float4 (normals); reads outside the image clamp to the edge.
  */
@@ -162,6 +164,79 @@ __global__ void k_splat_resolve(View v, const float4* __restrict__ pos, const un
         if (sprite(v, pos[(unsigned)kk], e, wx, wy, size) && fragment(v, e, wx, wy, size, px, py, nd, lin)) out = nd;
     }
     depth[k] = out;
+}
+
+/* shaders/particles.vert and particles.frag (ParticlesRenderer, fluid/render/
+ * particlesrenderer.cpp:40-88): the same sphere sprites, but the fragment shader writes no
+ * depth, so every fragment of a sprite is depth-tested at its centre's window depth
+ * (z_ndc + 1) / 2; the lowest index wins a tie as with the depth stage. */
+__device__ __forceinline__ bool particle_depth(const View& v, const float e[4], float& z) {
+    float c[4];
+    mat_vec(v.pr, e, c);
+    z = (c[2] / c[3] + 1.0f) * 0.5f;
+    if (z < 0.0f) z = 0.0f;
+    return z < 1.0f;
+}
+
+__global__ void k_particle_keys(View v, int n, const float4* __restrict__ pos, const int32_t* __restrict__ order,
+                                unsigned long long* __restrict__ key) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = order[t];
+    float e[4], wx, wy, size, z;
+    if (!sprite(v, pos[i], e, wx, wy, size) || !particle_depth(v, e, z)) return;
+    const unsigned zb = __float_as_uint(z);
+    const unsigned long long k = ((unsigned long long)zb << 32) | (unsigned)i;
+    const int x0 = max(0, (int)floorf(wx - 0.5f * size)), x1 = min(v.w - 1, (int)ceilf(wx + 0.5f * size));
+    const int y0 = max(0, (int)floorf(wy - 0.5f * size)), y1 = min(v.h - 1, (int)ceilf(wy + 0.5f * size));
+    for (int py = y0; py <= y1; ++py) {
+        unsigned long long* row = key + (size_t)py * v.w;
+        for (int px = x0; px <= x1; ++px) {
+            const unsigned long long cur = __ldca(row + px);
+            if (k >= cur) continue;   /* a nearer (or equal, lower-index) fragment is there */
+            const float nx = 2.0f * ((float)px + 0.5f - wx) / size;
+            const float ny = 2.0f * ((float)py + 0.5f - wy) / size;
+            if (nx * nx + ny * ny > 1.0f) continue;
+            atomicMin(row + px, k);
+        }
+    }
+}
+
+struct Lights {
+    int count;
+    float dir[8][3];
+    float diffuse[8][4];
+};
+
+/* Per pixel: the winning sprite's normal from the point coordinate, n = (2s - 1, 1 - 2t,
+ * sqrt(1 - |n.xy|^2)), lit by each directional light: diffuse * vertex colour (89, 152, 255)
+ * / 256 * max(0, n . -normalize(direction)), summed onto (0, 0, 0, 1) and clamped to [0, 1]
+ * as a fixed-point framebuffer stores it; (0, 0, 0, 1) where no sprite is. */
+__global__ void k_particle_shade(View v, const float4* __restrict__ pos, const unsigned long long* __restrict__ key,
+                                 Lights L, float4* __restrict__ out) {
+    const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= v.w || py >= v.h) return;
+    const size_t k = (size_t)py * v.w + px;
+    const unsigned long long kk = key[k];
+    float4 col = make_float4(0.f, 0.f, 0.f, 1.f);
+    float e[4], wx, wy, size;
+    if (kk != ~0ull && sprite(v, pos[(unsigned)kk], e, wx, wy, size)) {
+        const float nx = 2.0f * ((float)px + 0.5f - wx) / size;
+        const float ny = 2.0f * ((float)py + 0.5f - wy) / size;
+        const float nz = sqrtf(1.0f - (nx * nx + ny * ny));
+        const float vc[4] = {89.0f / 256.0f, 152.0f / 256.0f, 255.0f / 256.0f, 1.0f};
+        float acc[4] = {0.f, 0.f, 0.f, 1.f};
+        for (int l = 0; l < L.count; ++l) {
+            float dx = L.dir[l][0], dy = L.dir[l][1], dz = L.dir[l][2];
+            const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
+            dx = -(dx / len); dy = -(dy / len); dz = -(dz / len);
+            const float d = fmaxf(0.0f, (nx * dx + ny * dy) + nz * dz);
+            for (int c = 0; c < 4; ++c) acc[c] += (L.diffuse[l][c] * vc[c]) * d;
+        }
+        col = make_float4(fminf(fmaxf(acc[0], 0.f), 1.f), fminf(fmaxf(acc[1], 0.f), 1.f),
+                          fminf(fmaxf(acc[2], 0.f), 1.f), fminf(fmaxf(acc[3], 0.f), 1.f));
+    }
+    out[k] = col;
 }
 
 __global__ void k_splat_clear(size_t npix, unsigned long long* __restrict__ key) {
@@ -409,8 +484,10 @@ inline bool image_ok(int w, int h) {
 
 extern "C" {
 
-int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
-    if (!x || !view || !d_depth) return SPH_E_INVALID;
+/* Checks the view, allocates the depth-test keys and the particle-order buffers, clears the
+ * keys and sorts the particles front to back; the caller splats and resolves. */
+static int splat_prepare(sph_ctx* x, const sph_view* view, sph::View& v, unsigned long long*& key,
+                         const int32_t*& sorted) {
     if (!sph::image_ok(view->width, view->height))
         return sph_ctx_fail(x, SPH_E_INVALID, "render: width and height must be 1..65536 (at most 2^28 pixels)");
     if (!(view->point_radius > 0.f) || !(view->point_scale > 0.f))
@@ -441,17 +518,15 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
         }
         x->render_pixels = npix;
     }
-    sph::View v;
     std::memcpy(v.mv, view->modelview, sizeof v.mv);
     std::memcpy(v.pr, view->projection, sizeof v.pr);
     v.radius = view->point_radius;
     v.scale = view->point_scale;
     v.w = view->width;
     v.h = view->height;
-    unsigned long long* key = reinterpret_cast<unsigned long long*>(x->render_buf);
+    key = reinterpret_cast<unsigned long long*>(x->render_buf);
     const cudaStream_t s = x->stream;
     const int bs = 256, n = x->N;
-    const dim3 b2(16, 16);
     sph::k_splat_clear<<<(unsigned)((npix + bs - 1) / bs), bs, 0, s>>>(npix, key);
     uint32_t* okeys = reinterpret_cast<uint32_t*>(x->render_sort);
     int32_t* order = reinterpret_cast<int32_t*>(okeys + n);
@@ -460,10 +535,48 @@ int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
     void* ws = order_alt + n;
     sph::k_depth_order<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, okeys, order);
     uint32_t* ks;
-    int32_t* sorted;
-    sph::sort_pairs(s, okeys, order, okeys_alt, order_alt, n, 16, ws, x->b.flags, x->num_sms, &ks, &sorted);
+    int32_t* so;
+    sph::sort_pairs(s, okeys, order, okeys_alt, order_alt, n, 16, ws, x->b.flags, x->num_sms, &ks, &so);
+    sorted = so;
+    return SPH_OK;
+}
+
+int sph_render_depth(sph_ctx* x, const sph_view* view, float* d_depth) {
+    if (!x || !view || !d_depth) return SPH_E_INVALID;
+    sph::View v;
+    unsigned long long* key;
+    const int32_t* sorted;
+    const int rc = splat_prepare(x, view, v, key, sorted);
+    if (rc != SPH_OK) return rc;
+    const cudaStream_t s = x->stream;
+    const int bs = 256, n = x->N;
+    const dim3 b2(16, 16);
     sph::k_splat_keys<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, sorted, key);
     sph::k_splat_resolve<<<sph::grid2(v.w, v.h, b2), b2, 0, s>>>(v, x->b.pos, key, d_depth);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return sph_ctx_fail(x, SPH_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
+    return SPH_OK;
+}
+
+int sph_render_particles(sph_ctx* x, const sph_view* view, const sph_light* lights, int nlights, float* d_rgba) {
+    if (!x || !view || !d_rgba || nlights < 0 || nlights > 8 || (nlights > 0 && !lights)) return SPH_E_INVALID;
+    sph::Lights L{};
+    L.count = nlights;
+    for (int l = 0; l < nlights; ++l) {
+        for (int k = 0; k < 3; ++k) L.dir[l][k] = lights[l].direction[k];
+        for (int k = 0; k < 4; ++k) L.diffuse[l][k] = lights[l].diffuse[k];
+    }
+    sph::View v;
+    unsigned long long* key;
+    const int32_t* sorted;
+    const int rc = splat_prepare(x, view, v, key, sorted);
+    if (rc != SPH_OK) return rc;
+    const cudaStream_t s = x->stream;
+    const int bs = 256, n = x->N;
+    const dim3 b2(16, 16);
+    sph::k_particle_keys<<<(n + bs - 1) / bs, bs, 0, s>>>(v, n, x->b.pos, sorted, key);
+    sph::k_particle_shade<<<sph::grid2(v.w, v.h, b2), b2, 0, s>>>(v, x->b.pos, key, L,
+                                                                   reinterpret_cast<float4*>(d_rgba));
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return sph_ctx_fail(x, SPH_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
     return SPH_OK;
@@ -536,8 +649,11 @@ static bool invert4(const float* a, float* out) {
     return true;
 }
 
-int sph_render_frame(sph_ctx* x, const sph_view* view, int filter_iterations, float* rgba_host) {
-    if (!x || !view || !rgba_host || filter_iterations < 0) return SPH_E_INVALID;
+int sph_render_frame(sph_ctx* x, const sph_view* view, int method, int filter_iterations, const sph_light* lights,
+                     int nlights, float* rgba_host) {
+    if (!x || !view || !rgba_host || filter_iterations < 0 ||
+        (method != SPH_RENDER_SCREEN_SPACE && method != SPH_RENDER_PARTICLES))
+        return SPH_E_INVALID;
     if (!sph::image_ok(view->width, view->height))
         return sph_ctx_fail(x, SPH_E_INVALID, "render: width and height must be 1..65536 (at most 2^28 pixels)");
     float ip[16];
@@ -560,11 +676,16 @@ int sph_render_frame(sph_ctx* x, const sph_view* view, int filter_iterations, fl
     float* normals = tmp + npix;
     float* color = normals + 4 * npix;
     void* s = x->stream;
-    int rc = sph_render_depth(x, view, depth);
-    if (rc == SPH_OK) rc = sph_render_smooth(depth, tmp, w, h, filter_iterations, s);
-    if (rc == SPH_OK) rc = sph_render_normals(depth, normals, w, h, ip, s);
-    if (rc == SPH_OK)
-        rc = sph_render_shade(depth, normals, nullptr, nullptr, 0, w, h, view->modelview, ip, color, s);
+    int rc;
+    if (method == SPH_RENDER_PARTICLES) {
+        rc = sph_render_particles(x, view, lights, nlights, color);
+    } else {
+        rc = sph_render_depth(x, view, depth);
+        if (rc == SPH_OK) rc = sph_render_smooth(depth, tmp, w, h, filter_iterations, s);
+        if (rc == SPH_OK) rc = sph_render_normals(depth, normals, w, h, ip, s);
+        if (rc == SPH_OK)
+            rc = sph_render_shade(depth, normals, nullptr, nullptr, 0, w, h, view->modelview, ip, color, s);
+    }
     if (rc != SPH_OK) return sph_ctx_fail(x, rc, "render: frame stages");
     if (cudaMemcpyAsync(rgba_host, color, 16 * npix, cudaMemcpyDeviceToHost, x->stream) != cudaSuccess ||
         cudaStreamSynchronize(x->stream) != cudaSuccess) {

@@ -24,8 +24,10 @@
  * line, each the average of 6 steps (gui/glwidget.cpp:62-73, gui/mainwindow.cpp:99-101),
  * a frame here being one solver step.
  *
- * --frames DIR writes the screen-space surface (sph_render_frame: depth sprites, two blur
- * iterations, normals, final shading over black) as DIR/frame_NNNNN.ppm every
+ * --frames DIR writes frames of the config's render_method (sph_render_frame: "screenspace"
+ * = depth sprites, two blur iterations, normals, final shading over black; "particles", the
+ * default as in the reference = lit sphere sprites with the scene's lights) as
+ * DIR/frame_NNNNN.ppm every
  * --frame-every K steps (default 10) at --frame-size WxH (default 1280x720), seen by the
  * reference's default camera (fov 45, near 0.5, far 30; translate(0, 0, -4) . rotate 45
  * degrees about x; scene/camera.cpp:4-21, gui/glwidget.cpp:82-88) with its sprite radius
@@ -167,6 +169,7 @@ void pose(const double q[4], const double c[3], float out[12]) {
 
 struct Scene {
     float container[3] = {0, 0, 0};
+    std::vector<sph_light> lights;   /* "lights": direction, diffuse_color / 255 */
     std::vector<std::shared_ptr<FluidVolume>> volumes;
     std::vector<std::pair<std::string, std::shared_ptr<RigidBody>>> bodies;
 };
@@ -192,6 +195,14 @@ std::string resolve_model(const std::string& obj, const std::string& scene_path,
 Scene load_scene(const std::string& path, bool container_boundary, const std::string& data_root) {
     const Json j = parse_file(path);
     Scene sc;
+    for (const Json& l : j["lights"].arr) {
+        if (sc.lights.size() == 8) break;   /* MAX_DIR_LIGHTS of particles.frag */
+        sph_light li{};
+        for (int k = 0; k < 3; ++k) li.direction[k] = (float)l["direction"][k].number();
+        for (int k = 0; k < 3; ++k) li.diffuse[k] = (float)(l["diffuse_color"][k].number() / 255.0);
+        li.diffuse[3] = 1.0f;
+        sc.lights.push_back(li);
+    }
     const Json& c = j["container"];
     sc.container[0] = (float)c["width"].number();
     sc.container[1] = (float)c["height"].number();
@@ -349,7 +360,7 @@ int main(int argc, char** argv) {
         PhysicsSettings phys;
         SimulationSettings sim;
         load_settings(config, phys, sim);
-        load_graphics_settings(config);   /* validates render_method as the reference does */
+        const GraphicsSettings gfx = load_graphics_settings(config);   /* validated as the reference does */
         Scene sc = load_scene(scene_file, container_boundary, data_root);
         if (jitter >= 0)
             for (size_t v = 0; v < sc.volumes.size(); ++v)
@@ -390,7 +401,9 @@ int main(int argc, char** argv) {
         for (int s = 1; s <= steps; ++s) {
             fluid->simulate();
             if (!frames.empty() && frame_every > 0 && s % frame_every == 0)
-                write_ppm(frames + "/frame_" + pad5(frame_no++) + ".ppm", fluid->render_frame(view, 2), frame_w,
+                write_ppm(frames + "/frame_" + pad5(frame_no++) + ".ppm", fluid->render_frame(view, gfx.render_method == GraphicsSettings::PARTICLES ? SPH_RENDER_PARTICLES
+                                                                                                 : SPH_RENDER_SCREEN_SPACE,
+                                                      2, sc.lights), frame_w,
                           frame_h);
             if (fps.is_open() && s % 6 == 0) {   /* frames per second over the last 6 steps */
                 fluid->synchronize();

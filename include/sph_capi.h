@@ -363,12 +363,29 @@ int sph_render_normals(const float* d_depth, float* d_normals4, int width, int h
 int sph_render_shade(const float* d_depth, const float* d_normals4, const float* d_background4,
                      const float* d_cube4, int cube_size, int width, int height, const float modelview[16],
                      const float inv_projection[16], float* d_rgba, void* cuda_stream);
-/* A headless frame: SSpaceFluidRenderer::render (:35-53) on the context's particles — depth,
+/* A directional light of the scene file ("lights", scene/scene.cpp:340-364): direction and
+ * diffuse colour (r, g, b, a in 0..1, i.e. the file's 0..255 values / 255). */
+typedef struct sph_light {
+    float direction[3];
+    float diffuse[4];
+} sph_light;
+/* ParticlesRenderer (fluid/render/particlesrenderer.cpp:40-88, shaders/particles.vert/.frag):
+ * the context's particles as sphere sprites, each depth-tested at its centre's window depth
+ * (the fragment shader writes none; the lower index wins a tie), lit by up to 8 directional
+ * lights: (0, 0, 0, 1) + sum of diffuse * (89, 152, 255, 256) / 256 * max(0, n . -dir),
+ * n from the point coordinate; clamped to [0, 1] as a fixed-point framebuffer stores it;
+ * (0, 0, 0, 1) where no sprite is.  Into d_rgba (float4 per pixel), on the context stream. */
+int sph_render_particles(sph_ctx* ctx, const sph_view* view, const sph_light* lights, int nlights, float* d_rgba);
+/* GraphicsSettings::render_method (settings/settings.cpp:47-57). */
+enum sph_render_method { SPH_RENDER_PARTICLES = 0, SPH_RENDER_SCREEN_SPACE = 1 };
+/* A headless frame into rgba_host (width * height float4, row 0 at the bottom):
+ * SPH_RENDER_SCREEN_SPACE runs SSpaceFluidRenderer::render (:35-53) — depth,
  * filter_iterations blur iterations, normals and the final stage over a black background
- * without a cube map — into rgba_host (width * height float4, row 0 at the bottom).  The
- * device images are the context's (40 bytes per pixel, kept for the next frame); the inverse
- * projection is computed from view->projection.  Synchronous. */
-int sph_render_frame(sph_ctx* ctx, const sph_view* view, int filter_iterations, float* rgba_host);
+ * without a cube map; SPH_RENDER_PARTICLES runs sph_render_particles with the given lights.
+ * The device images are the context's (40 bytes per pixel, kept for the next frame); the
+ * inverse projection is computed from view->projection.  Synchronous. */
+int sph_render_frame(sph_ctx* ctx, const sph_view* view, int method, int filter_iterations, const sph_light* lights,
+                     int nlights, float* rgba_host);
 
 /* ---- primitives ---------------------------------------------------------------------- */
 

@@ -485,10 +485,14 @@ class CudaFluidSimulation : public FluidSimulation {
     void synchronize() { check(sph_synchronize(ctx_), ctx_); }
     /* checkpoint / resume (sph_save_state / sph_load_state) */
     void save_state(const std::string& path) { check(sph_save_state(ctx_, path.c_str()), ctx_); }
-    /* a shaded screen-space frame of the particles (sph_render_frame) */
-    std::vector<float> render_frame(const sph_view& view, int filter_iterations) {
+    /* a headless frame of the particles (sph_render_frame): screen-space surface or lit
+     * particle sprites */
+    std::vector<float> render_frame(const sph_view& view, int method, int filter_iterations,
+                                    const std::vector<sph_light>& lights) {
         std::vector<float> rgba(4 * (size_t)view.width * view.height);
-        check(sph_render_frame(ctx_, &view, filter_iterations, rgba.data()), ctx_);
+        check(sph_render_frame(ctx_, &view, method, filter_iterations, lights.empty() ? nullptr : lights.data(),
+                               (int)lights.size(), rgba.data()),
+              ctx_);
         return rgba;
     }
     void load_state(const std::string& path) { check(sph_load_state(ctx_, path.c_str()), ctx_); }

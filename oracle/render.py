@@ -269,3 +269,59 @@ def shade(depth, normals, background, cube, modelview, inv_projection):
         out = np.stack(col + [np.ones_like(z)], -1).astype(F)
     back = np.concatenate([bkg[..., :3], np.ones((h, w, 1), F)], -1)
     return np.where((z > 0)[..., None], out, back).astype(F)
+
+
+def particles_image(pos4, modelview, projection, point_radius, point_scale, width, height, lights):
+    """ParticlesRenderer (shaders/particles.vert/.frag): sphere sprites depth-tested at their
+    centre's window depth, lit by directional lights [(direction, diffuse rgba)].  Returns
+    (height, width, 4), (0, 0, 0, 1) where no sprite is, colours clamped to [0, 1]."""
+    mv = np.asarray(modelview, F).reshape(4, 4)
+    pr = np.asarray(projection, F).reshape(4, 4)
+    rad, scale = F(point_radius), F(point_scale)
+    best = np.full((height, width), np.inf, F)
+    owner = np.full((height, width), -1, np.int64)
+    sprites = {}
+    one = F(1.0)
+    for i, p in enumerate(np.asarray(pos4, F).reshape(-1, 4)):
+        e = _mv(mv, [p[0], p[1], p[2], one])
+        c = _mv(pr, e)
+        if not (c[3] > 0) or abs(c[0]) > c[3] or abs(c[1]) > c[3] or abs(c[2]) > c[3]:
+            continue
+        dist = np.sqrt((e[0] * e[0] + e[1] * e[1]) + e[2] * e[2])
+        size = max(rad * (scale / dist), one)
+        wx = ((c[0] / c[3] + one) * F(0.5)) * F(width)
+        wy = ((c[1] / c[3] + one) * F(0.5)) * F(height)
+        z = max((c[2] / c[3] + one) * F(0.5), F(0))
+        if not z < one:
+            continue
+        sprites[i] = (wx, wy, size)
+        x0, x1 = max(0, int(np.floor(wx - F(0.5) * size))), min(width - 1, int(np.ceil(wx + F(0.5) * size)))
+        y0, y1 = max(0, int(np.floor(wy - F(0.5) * size))), min(height - 1, int(np.ceil(wy + F(0.5) * size)))
+        if x0 > x1 or y0 > y1:
+            continue
+        px = np.arange(x0, x1 + 1, dtype=F)[None, :]
+        py = np.arange(y0, y1 + 1, dtype=F)[:, None]
+        nx = (F(2.0) * ((px + F(0.5)) - wx)) / size + np.zeros_like(py)
+        ny = (F(2.0) * ((py + F(0.5)) - wy)) / size + np.zeros_like(px)
+        inside = (nx * nx + ny * ny) <= one
+        b = best[y0:y1 + 1, x0:x1 + 1]
+        win = inside & (z < b)
+        b[win] = z
+        owner[y0:y1 + 1, x0:x1 + 1][win] = i
+    out = np.zeros((height, width, 4), F)
+    out[..., 3] = 1
+    vc = np.array([89.0 / 256.0, 152.0 / 256.0, 255.0 / 256.0, 1.0], F)
+    for y, x in zip(*np.nonzero(owner >= 0)):
+        wx, wy, size = sprites[int(owner[y, x])]
+        nx = (F(2.0) * ((F(x) + F(0.5)) - wx)) / size
+        ny = (F(2.0) * ((F(y) + F(0.5)) - wy)) / size
+        nz = np.sqrt(one - (nx * nx + ny * ny))
+        acc = np.array([0, 0, 0, 1], F)
+        for d, col in lights:
+            d = np.asarray(d, F)
+            ln = np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+            dx, dy, dz = -(d[0] / ln), -(d[1] / ln), -(d[2] / ln)
+            dd = max(F(0), (nx * dx + ny * dy) + nz * dz)
+            acc = (acc + (np.asarray(col, F) * vc) * dd).astype(F)
+        out[y, x] = np.clip(acc, 0, 1)
+    return out

@@ -220,8 +220,12 @@ def test_driver_reference_short_options_and_fps_output(gpu_lib, driver, tmp_path
 
 
 @pytest.mark.gpu
-def test_driver_writes_screen_space_frames(gpu_lib, driver, tmp_path):
-    c, s = write(tmp_path)
+@pytest.mark.parametrize("method", ["screenspace", "particles"])
+def test_driver_writes_frames(gpu_lib, driver, tmp_path, method):
+    scene = dict(SCENE)
+    scene["lights"] = [{"ambient_color": [100, 100, 100], "diffuse_color": [255, 255, 255],
+                        "specular_color": [255, 255, 255], "direction": [-1.0, -1.0, -1.0]}]
+    c, s = write(tmp_path, config=CONFIG + "render_method=%s\n" % method, scene=scene)
     frames = tmp_path / "frames"
     frames.mkdir()
     r = subprocess.run([driver, "-c", c, "-s", s, "--steps", "20", "--frames", str(frames), "--frame-every", "10",

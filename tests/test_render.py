@@ -293,3 +293,41 @@ def test_gpu_render_frame_equals_the_stage_sequence(gpu_lib):
     ref = col.cpu().numpy()
     assert np.abs(frame.astype(np.float64) - ref).max() <= 1e-4
     assert np.array_equal(frame[..., 3], ref[..., 3]) and frame[..., :3].max() > 0
+
+
+LIGHTS = [((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0, 1.0)), ((0.5, -1.0, 0.2), (0.4, 0.3, 0.2, 1.0))]
+
+
+def test_particles_restatement_properties():
+    w = h = 64
+    pr = orender.perspective(45.0, 1.0, 0.5, 30.0)
+    mv = np.eye(4, dtype=np.float32)
+    near = np.array([[0.0, 0.0, -3.0, 1.0]], np.float32)
+    far = np.array([[0.0, 0.0, -4.0, 1.0]], np.float32)
+    args = (mv, pr, 0.5, w * np.tan(np.radians(22.5)), w, h, LIGHTS)
+    a = orender.particles_image(np.concatenate([far, near]), *args)
+    b = orender.particles_image(np.concatenate([near, far]), *args)
+    n = orender.particles_image(near, *args)
+    assert np.array_equal(a, b) and np.array_equal(a[h // 2, w // 2], n[h // 2, w // 2])
+    assert (a >= 0).all() and (a <= 1).all() and (a[..., 3] == 1).all()
+    assert a[..., :3].max() > 0 and (a[0, 0, :3] == 0).all()
+
+
+@pytest.mark.gpu
+def test_gpu_particles_match_restatement(gpu_lib):
+    """The particle render method: depth test, winners and lighting bit for bit."""
+    import torch
+    g = golden()
+    w, h = int(g["width"]), int(g["height"])
+    ctx = _context(g["pos"])
+    pos = ctx.get("POS").reshape(-1, 4)
+    view = capi.make_view(g["modelview"], g["projection"], g["point_radius"] * 0.5, g["point_scale"], w, h)
+    img = torch.full((h, w, 4), 3.0, dtype=torch.float32, device="cuda")
+    ctx.render_particles(view, LIGHTS, img.data_ptr())
+    ctx.synchronize()
+    got = img.cpu().numpy()
+    want = orender.particles_image(pos, g["modelview"], g["projection"], g["point_radius"] * 0.5, g["point_scale"],
+                                   w, h, LIGHTS)
+    assert np.array_equal(got, want), describe_mismatch(got, want)
+    frame = ctx.render_frame(view, method=capi.SPH_RENDER_PARTICLES, lights=LIGHTS)
+    assert np.array_equal(frame, want)
