@@ -13,17 +13,24 @@
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
 ref="${1:-/root/reference}"
-if [ ! -d "$ref/kernels" ]; then
+out="$here/_ref"
+have_ref=0
+if [ -d "$ref/kernels" ]; then
+    have_ref=1
+elif [ ! -f "$out/src/grid.cl" ]; then
     echo "build_ref: no reference kernels under $ref; skipped" >&2
     exit 0
 fi
-out="$here/_ref"
 mkdir -p "$out/src" "$out/obj"
-for f in "$ref"/kernels/*.cl "$ref"/kernels/*.h; do
-    sed -E 's/\((int4|float4)\)[[:space:]]*\(/make_\1(/g' "$f" > "$out/src/$(basename "$f")"
-done
+if [ "$have_ref" = 1 ]; then
+    for f in "$ref"/kernels/*.cl "$ref"/kernels/*.h; do
+        sed -E 's/\((int4|float4)\)[[:space:]]*\(/make_\1(/g' "$f" > "$out/src/$(basename "$f")"
+    done
+fi
+# (without the reference mounted, e.g. on the GPU machine, the kernel copies made here
+# under oracle/_ref/src, which travel with the working tree, are compiled again)
 CXX="${CXX:-g++}"
-flags=(-O1 -std=c++17 -fPIC -ffp-contract=off -Wall -Wno-sign-compare -Wno-unused -Wno-narrowing -I "$here/ref_shim" -I "$out/src")
+flags=(-O2 -std=c++17 -fPIC -ffp-contract=off -pthread -Wall -Wno-sign-compare -Wno-unused -Wno-narrowing -I "$here/ref_shim" -I "$out/src")
 pids=()
 for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary ref_render; do
     "$CXX" "${flags[@]}" -c "$here/ref_shim/$u.cpp" -o "$out/obj/$u.o" &
@@ -31,13 +38,16 @@ for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary r
 done
 # the mesh code (mesh/modelmesh.cpp with the vendored tinyobj, mesh/icospheremesh.cpp and
 # the vendored voxelizer) compiles from its own sources under the reference root
-mflags=(-O1 -std=c++17 -fPIC -ffp-contract=off -w -I "$here/ref_shim" -I "$ref")
-"$CXX" "${mflags[@]}" -c "$ref/mesh/modelmesh.cpp" -o "$out/obj/ref_modelmesh.o" &
-pids+=($!)
-"$CXX" "${mflags[@]}" -c "$ref/mesh/icospheremesh.cpp" -o "$out/obj/ref_icospheremesh.o" &
-pids+=($!)
-"$CXX" "${mflags[@]}" -c "$here/ref_shim/ref_mesh.cpp" -o "$out/obj/ref_mesh.o" &
-pids+=($!)
+rm -f "$out"/obj/ref_modelmesh.o "$out"/obj/ref_icospheremesh.o "$out"/obj/ref_mesh.o
+if [ "$have_ref" = 1 ]; then
+    mflags=(-O2 -std=c++17 -fPIC -ffp-contract=off -pthread -w -I "$here/ref_shim" -I "$ref")
+    "$CXX" "${mflags[@]}" -c "$ref/mesh/modelmesh.cpp" -o "$out/obj/ref_modelmesh.o" &
+    pids+=($!)
+    "$CXX" "${mflags[@]}" -c "$ref/mesh/icospheremesh.cpp" -o "$out/obj/ref_icospheremesh.o" &
+    pids+=($!)
+    "$CXX" "${mflags[@]}" -c "$here/ref_shim/ref_mesh.cpp" -o "$out/obj/ref_mesh.o" &
+    pids+=($!)
+fi
 for p in "${pids[@]}"; do wait "$p"; done
-"$CXX" -shared -o "$out/libref_kernels.so" "$out"/obj/*.o
+"$CXX" -shared -pthread -o "$out/libref_kernels.so" "$out"/obj/*.o
 echo "build_ref: built $out/libref_kernels.so"

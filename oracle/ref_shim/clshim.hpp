@@ -51,6 +51,8 @@ void barrier_impl();
  * multiple of local, as the reference's launches are). With fibers=false, a barrier()
  * aborts: use it only for kernels that have none. */
 void run_ndrange(size_t global, size_t local, bool fibers, const std::function<void()>& body);
+/* __local memory of the work-group running on this thread (slot 0..7, at least bytes). */
+void* group_local(int slot, size_t bytes);
 /* A 2-D NDRange of independent work-items (no barrier), dimension 0 fastest. */
 void run_ndrange_2d(size_t gx, size_t gy, const std::function<void()>& body);
 }  // namespace clshim

@@ -5,6 +5,9 @@
  */
 #include "clshim.hpp"
 
+#include <algorithm>
+#include <cstring>
+
 #include "clshim_kernel_begin.hpp"
 namespace ref_grid {
 #include "grid.cl"
@@ -32,16 +35,26 @@ void ref_compute_hashes(const float* pos4, int n, float size, float cell_size, i
     });
 }
 
+/* CLAllocator::fill_buffer of the cell table with zeros (grid.cpp:41) on the host's threads:
+ * n ints in chunks of 65,536 as independent work-groups. */
+void ref_fill_zero(int32_t* p, long long n) {
+    const size_t chunk = 65536;
+    const size_t groups = (size_t)((n + (long long)chunk - 1) / (long long)chunk);
+    run_ndrange(groups, 1, false, [&] {
+        const size_t g = get_global_id(0);
+        const size_t a = g * chunk, b = std::min((size_t)n, a + chunk);
+        std::memset(p + a, 0, 4 * (b - a));
+    });
+}
+
 /* intervals: 2 * cps^3 ints, zero-filled by the caller (grid.cpp:41). */
 void ref_compute_cell_intervals(const float* spos4, const uint32_t* hashes, int n, float size,
                                 float cell_size, int cps, int32_t* intervals) {
     ref_grid::GridInfo gi = make_info(size, cell_size, cps);
     const size_t local = 32;
-    std::vector<float4> lpos(local);
-    std::vector<uint> lhash(local);
     run_ndrange((size_t)n, local, true, [&] {
         ref_grid::compute_cell_intervals(reinterpret_cast<const float4*>(spos4), hashes, intervals,
-                                         lpos.data(), lhash.data(), gi, n);
+                                         static_cast<float4*>(group_local(0, sizeof(float4) * local)), static_cast<uint*>(group_local(1, sizeof(uint) * local)), gi, n);
     });
 }
 

@@ -23,12 +23,10 @@ void ref_compute_normals(const float* pos4, const float* dens, float* nrm4, int 
     g_particle_mass = mass_define;
     g_support_radius = support_define;
     const size_t local = local_size > 0 ? (size_t)local_size : 64;
-    std::vector<float4> pc(local);
-    std::vector<float> dc(local);
     image1d_buffer_t ip{pos4, 4}, id{dens, 1};
     run_ndrange((size_t)n, local, true, [&] {
-        ref_normals::compute_normals(ip, id, reinterpret_cast<float4*>(nrm4), len, list, w_grad, pc.data(),
-                                     dc.data());
+        ref_normals::compute_normals(ip, id, reinterpret_cast<float4*>(nrm4), len, list, w_grad, static_cast<float4*>(group_local(0, sizeof(float4) * local)),
+                                     static_cast<float*>(group_local(1, sizeof(float) * local)));
     });
 }
 

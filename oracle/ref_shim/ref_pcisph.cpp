@@ -31,10 +31,9 @@ void ref_pci_initial_density(const float* pos4, float* dens, int n, const int32_
                              int local_size) {
     set_defines(n, support_define, mass_define, rho0_define);
     const size_t local = local_size > 0 ? (size_t)local_size : 64;
-    std::vector<float4> pc(local);
     image1d_buffer_t ip{pos4, 4}, ib{bpos4, 4}, iphi{bphi, 1};
     run_ndrange((size_t)n, local, true, [&] {
-        ref_pcisph::compute_initial_density(ip, dens, flen, flist, blist, blen, ib, iphi, w_eval, pc.data());
+        ref_pcisph::compute_initial_density(ip, dens, flen, flist, blist, blen, ib, iphi, w_eval, static_cast<float4*>(group_local(0, sizeof(float4) * local)));
     });
 }
 
@@ -44,13 +43,11 @@ void ref_pci_initial_forces(const float* pos4, const float* vel4, const float* d
                             float mass_define, float rho0_define, int local_size) {
     set_defines(n, support_define, mass_define, rho0_define);
     const size_t local = local_size > 0 ? (size_t)local_size : 64;
-    std::vector<float4> pc(local), vc(local), nc(local);
-    std::vector<float> dc(local);
     image1d_buffer_t ip{pos4, 4}, iv{vel4, 4}, id{dens, 1}, in{nrm4, 4};
     run_ndrange((size_t)n, local, true, [&] {
         ref_pcisph::compute_initial_forces(ip, iv, id, in, reinterpret_cast<float4*>(fo4), mu, sigma, flen, flist,
-                                           visc_lapl, st_main, st_term, pc.data(), vc.data(), dc.data(),
-                                           nc.data());
+                                           visc_lapl, st_main, st_term, static_cast<float4*>(group_local(0, sizeof(float4) * local)), static_cast<float4*>(group_local(1, sizeof(float4) * local)), static_cast<float*>(group_local(3, sizeof(float) * local)),
+                                           static_cast<float4*>(group_local(2, sizeof(float4) * local)));
     });
 }
 
@@ -73,11 +70,10 @@ void ref_pci_update_pressure(const float* pred4, float* dens_var, float* pres, i
                              float support_define, float mass_define, float rho0_define, int local_size) {
     set_defines(n, support_define, mass_define, rho0_define);
     const size_t local = local_size > 0 ? (size_t)local_size : 64;
-    std::vector<float4> pc(local);
     image1d_buffer_t ip{pred4, 4}, ib{bpos4, 4}, iphi{bphi, 1};
     run_ndrange((size_t)n, local, true, [&] {
         ref_pcisph::update_pressure(ip, dens_var, pres, delta, flen, flist, blist, blen, ib, iphi, w_eval,
-                                    pc.data());
+                                    static_cast<float4*>(group_local(0, sizeof(float4) * local)));
     });
 }
 
@@ -88,14 +84,12 @@ void ref_pci_pressure_force(const float* pos4, const float* dens, const float* p
                             int local_size) {
     set_defines(n, support_define, mass_define, rho0_define);
     const size_t local = local_size > 0 ? (size_t)local_size : 64;
-    std::vector<float4> pc(local);
-    std::vector<float> dc(local), prc(local);
     ref_pcisph::GridInfo gi;
     gi.size = size; gi.cell_size = cell_size; gi.cells_per_side = cps; gi.cells_count = cps * cps * cps;
     image1d_buffer_t ip{pos4, 4}, id{dens, 1}, ipr{pres, 1}, ib{bpos4, 4}, iphi{bphi, 1};
     run_ndrange((size_t)n, local, true, [&] {
         ref_pcisph::compute_pressure_force(ip, id, ipr, reinterpret_cast<float4*>(fp4), gi, flen, flist, blist,
-                                           blen, ib, iphi, w_grad, pc.data(), dc.data(), prc.data());
+                                           blen, ib, iphi, w_grad, static_cast<float4*>(group_local(0, sizeof(float4) * local)), static_cast<float*>(group_local(3, sizeof(float) * local)), static_cast<float*>(group_local(4, sizeof(float) * local)));
     });
 }
 

@@ -13,14 +13,27 @@ REFERENCE_ROOT = "/root/reference"
 _lib = None
 
 
+SRC_COPIES = os.path.join(HERE, "_ref", "src", "grid.cl")
+
+
 def available():
-    return os.path.exists(LIB) or os.path.isdir(os.path.join(REFERENCE_ROOT, "kernels"))
+    return (os.path.exists(LIB) or os.path.isdir(os.path.join(REFERENCE_ROOT, "kernels"))
+            or os.path.exists(SRC_COPIES))
+
+
+def has_mesh_code():
+    """The mesh entry points need the reference's own mesh sources at build time."""
+    try:
+        lib().ref_load_obj
+        return True
+    except (AttributeError, RuntimeError):
+        return False
 
 
 def build(force=False):
     if os.path.exists(LIB) and not force:
         return LIB
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "kernels")):
+    if not (os.path.isdir(os.path.join(REFERENCE_ROOT, "kernels")) or os.path.exists(SRC_COPIES)):
         return None
     subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
     return LIB if os.path.exists(LIB) else None
@@ -59,8 +72,13 @@ def compute_hashes(pos4, size, h, cps):
     return hs, mk
 
 
-def compute_cell_intervals(spos4, hashes, size, h, cps):
-    iv = np.zeros(2 * cps ** 3, np.int32)
+def compute_cell_intervals(spos4, hashes, size, h, cps, out=None):
+    """out: a reused 2 * cps^3 int32 table, zero-filled here as grid.cpp:41 fills it."""
+    if out is None:
+        iv = np.zeros(2 * cps ** 3, np.int32)
+    else:
+        iv = out
+        lib().ref_fill_zero(P(iv), C.c_longlong(iv.size))
     lib().ref_compute_cell_intervals(P(spos4), P(hashes), i(len(spos4)), f(size), f(h), i(cps), P(iv))
     return iv
 
