@@ -606,10 +606,26 @@ def main():
                 capi.check(L.sph_get_field_async(ctx.h, capi.FIELDS[f], a.ctypes.data, a.nbytes), ctx.h)
             capi.check(L.sph_synchronize(ctx.h), ctx.h)
         te = time.perf_counter() - t0
+        # the same copies without the step: the host link's share of the e2e time
+        t1 = time.perf_counter()
+        for _ in range(k_e2e):
+            for f, a in state:
+                capi.check(L.sph_set_field_async(ctx.h, capi.FIELDS[f], a.ctypes.data, a.nbytes), ctx.h)
+            capi.check(L.sph_synchronize(ctx.h), ctx.h)
+        th = (time.perf_counter() - t1) / k_e2e
+        t1 = time.perf_counter()
+        for _ in range(k_e2e):
+            for f, a in state:
+                capi.check(L.sph_get_field_async(ctx.h, capi.FIELDS[f], a.ctypes.data, a.nbytes), ctx.h)
+            capi.check(L.sph_synchronize(ctx.h), ctx.h)
+        td = (time.perf_counter() - t1) / k_e2e
+        ms_e2e = te * 1e3 / k_e2e
         te, units_e = replicas.aggregate(te, n * k_e2e, device="cuda")
         e2e = {"value": units_e / te, "unit": UNIT, "h2d_bytes_per_step": 48 * n,
                "d2h_bytes_per_step": 48 * n, "steps": k_e2e, "host_buffers": "pinned",
-               "copies": "pos, vel, vel_half in and out on the context stream; one host wait per step"}
+               "copies": "pos, vel, vel_half in and out on the context stream; one host wait per step",
+               "ms_per_step": ms_e2e, "copy_ms_per_step": (th + td) * 1e3,
+               "h2d_gbs": 48 * n / th / 1e9, "d2h_gbs": 48 * n / td / 1e9}
     rend = vox = None
     if args.render_frames > 0:
         rend = bench_render(torch, ctx, stream, args.render_frames)

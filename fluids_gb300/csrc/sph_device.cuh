@@ -279,27 +279,59 @@ __device__ __forceinline__ int build_scan(const Const& c, float px, float py, fl
 /* Visits the materialised list of particle i (column-major list[k * n + i], grid.cl:174).
  * The pass is bound by the latency of the dependent loads (list entry, then the
  * neighbour's data), so U entries and their positions are loaded before the U visits
- * run; the visits still run in list order, so every sum keeps the list's order. */
+ * run.  PIPE also loads the next U entries (the rows live in HBM: 200 bytes per particle)
+ * before the current U visits, so their latency overlaps the visits: measured on GB300 it
+ * speeds up the normal pass (0.310 -> 0.291 ms at 4M) and slows the force pass, whose
+ * registers it pushes into spills (0.699 -> 0.761 ms).  The visits run in list order
+ * either way, so every sum keeps the list's order. */
 #ifndef SPH_LIST_UNROLL
 #define SPH_LIST_UNROLL 4
 #endif
-template <int U = SPH_LIST_UNROLL, class F>
+template <int U = SPH_LIST_UNROLL, bool PIPE = false, class F>
 __device__ __forceinline__ void list_neighbors(int i, int n, const int* __restrict__ list, int len,
                                                const float4* __restrict__ npos, float px, float py, float pz,
                                                F&& f) {
     const size_t sn = (size_t)n;
     const int* __restrict__ p = list + i;
     int k = 0;
+    if (!PIPE) {
 #pragma unroll 1
-    for (; k + U <= len; k += U, p += U * sn) {
-        int j[U];
-        float4 q[U];
+        for (; k + U <= len; k += U, p += U * sn) {
+            int j[U];
+            float4 q[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) j[u] = __ldg(p + u * sn);
+            for (int u = 0; u < U; ++u) j[u] = __ldg(p + u * sn);
 #pragma unroll
-        for (int u = 0; u < U; ++u) q[u] = __ldg(&npos[j[u]]);
+            for (int u = 0; u < U; ++u) q[u] = __ldg(&npos[j[u]]);
 #pragma unroll
-        for (int u = 0; u < U; ++u) f(j[u], q[u], __fsub_rn(px, q[u].x), __fsub_rn(py, q[u].y), __fsub_rn(pz, q[u].z));
+            for (int u = 0; u < U; ++u)
+                f(j[u], q[u], __fsub_rn(px, q[u].x), __fsub_rn(py, q[u].y), __fsub_rn(pz, q[u].z));
+        }
+    } else if (len >= U) {
+        int jn[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) jn[u] = __ldg(p + u * sn);
+        p += U * sn;
+#pragma unroll 1
+        for (;;) {
+            int j[U];
+            float4 q[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) j[u] = jn[u];
+#pragma unroll
+            for (int u = 0; u < U; ++u) q[u] = __ldg(&npos[j[u]]);
+            k += U;
+            const bool more = k + U <= len;
+            if (more) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) jn[u] = __ldg(p + u * sn);
+                p += U * sn;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                f(j[u], q[u], __fsub_rn(px, q[u].x), __fsub_rn(py, q[u].y), __fsub_rn(pz, q[u].z));
+            if (!more) break;
+        }
     }
 #pragma unroll 1
     for (; k < len; ++k, p += sn) {
@@ -316,9 +348,9 @@ struct Neigh {
     const int* list;
     const int* len;
     const float4* npos;
-    template <class F>
+    template <bool PIPE = false, class F>
     __device__ __forceinline__ void visit(const Const& c, int i, float px, float py, float pz, F&& f) const {
-        if (LIST) list_neighbors(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
+        if (LIST) list_neighbors<SPH_LIST_UNROLL, PIPE>(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
         else scan_neighbors<EXACT>(c, px, py, pz, tab, npos, f);
     }
 };

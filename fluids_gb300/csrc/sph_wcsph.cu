@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
     const float4 pi = __ldg(&fl.npos[i]);
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
-    fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
+    fl.template visit<true>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
         /* 1/rho_j from the dense density array (8 particles per 32-byte sector instead of 2
          * for aux; the pass is bound by L1 throughput); __frcp_rn is the correctly rounded
          * reciprocal, the value aux holds */
