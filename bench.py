@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--batched-steps", type=int, default=500, help="0 skips the batched comparison")
     ap.add_argument("--adjoint-steps", type=int, default=200, help="0 skips the adjoint comparison")
     ap.add_argument("--pcisph-steps", type=int, default=100, help="0 skips the PCISPH line")
+    ap.add_argument("--pcisph4m-steps", type=int, default=20, help="0 skips the PCISPH 4M line")
     ap.add_argument("--render-frames", type=int, default=20, help="0 skips the screen-space surface line")
     return ap.parse_args()
 
@@ -343,11 +344,12 @@ def bench_adjoint(torch, steps=200, every=20):
     return out
 
 
-def bench_pcisph(torch, steps, warmup):
-    """PCISPH double block + rotated cube (358,400 fluid particles), PHYSICS mode: device time
-    of `steps` graph-replayed steps (the predict-correct loop is one persistent kernel)."""
+def bench_pcisph(torch, steps, warmup, large=False):
+    """PCISPH double block + rotated cube (358,400 fluid particles), or with `large` the
+    4,194,304-particle double dam break, PHYSICS mode: device time of `steps` graph-replayed
+    steps (the predict-correct loop is one persistent kernel)."""
     from fluids_gb300 import capi, workloads
-    w = workloads.pcisph_cube(capi.SPH_MODE_PHYSICS)
+    w = (workloads.pcisph_double_dam_4m if large else workloads.pcisph_cube)(capi.SPH_MODE_PHYSICS)
     stream = torch.cuda.Stream()
     ctx = workloads.build_context(w)
     ctx.set_stream(stream.cuda_stream)
@@ -366,7 +368,8 @@ def bench_pcisph(torch, steps, warmup):
     t = e0.elapsed_time(e1) / 1000.0
     out = {"workload": w["name"], "particles": n, "boundary_particles": nb, "steps": steps,
            "updates_per_s": n * steps / t, "ms_per_step": 1000 * t / steps,
-           "pci_iterations_sampled": iters, "device_flags": ctx.device_flags()}
+           "pci_iterations_sampled": iters, "device_flags": ctx.device_flags(),
+           "kernel_ms_per_step": ctx.profile_step(3)}
     ctx.close()
     return out
 
@@ -634,11 +637,13 @@ def main():
     batched = None
     if args.batched_steps > 0 and args.workload == "wcsph4m":
         batched = bench_batched(args.batched_steps, max(args.warmup, 3), torch, rank=rank, world=world)
-    adjoint = pcisph = None
+    adjoint = pcisph = pcisph4m = None
     if args.adjoint_steps > 0 and args.workload == "wcsph4m":
         adjoint = bench_adjoint(torch, args.adjoint_steps)
     if args.pcisph_steps > 0 and args.workload == "wcsph4m":
         pcisph = bench_pcisph(torch, args.pcisph_steps, max(args.warmup, 3))
+    if args.pcisph4m_steps > 0 and args.workload == "wcsph4m":
+        pcisph4m = bench_pcisph(torch, args.pcisph4m_steps, 3, large=True)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         z = w["fluid"][:, 2]
@@ -656,7 +661,7 @@ def main():
                 "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk,
                 "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched, "adjoint": adjoint,
-                "pcisph": pcisph, "render": rend, "voxelize": vox}
+                "pcisph": pcisph, "pcisph_4m": pcisph4m, "render": rend, "voxelize": vox}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

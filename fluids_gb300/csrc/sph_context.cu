@@ -238,6 +238,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.normal = cv.take<float4>(n); b.accel = cv.take<float4>(n); b.pos_pred = cv.take<float4>(n);
     b.f_other = cv.take<float4>(n); b.f_press = cv.take<float4>(n);
     b.density = cv.take<float>(n); b.pressure = cv.take<float>(n); b.dens_var = cv.take<float>(n);
+    b.pci_c = cv.take<float>(n);
     b.aux = cv.take<float4>(n);
     b.nrec = cv.take<float4>(2 * n);
     b.keys = cv.take<uint32_t>(n); b.keys_alt = cv.take<uint32_t>(n);

@@ -16,6 +16,7 @@ struct Bufs {
     float4 *pos_s, *vel_s, *vhalf_s;       /* this step's sorted copies */
     float4 *normal, *accel, *pos_pred, *f_other, *f_press;
     float *density, *pressure, *dens_var;
+    float* pci_c;                          /* PCISPH loop: p / rho^2 of each particle this iteration */
     float4* aux;                           /* per particle (p/rho^2, 1/rho, rho, p) */
     float4* nrec;                          /* 2 per particle: (v, p/rho^2), (normal, 1/rho) for the force pass */
     uint32_t *keys, *keys_alt;

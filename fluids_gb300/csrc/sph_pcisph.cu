@@ -121,7 +121,12 @@ __device__ __forceinline__ void pci_integrate_one(const Const& c, const Bufs& b,
     if (bad) atomicOr(b.flags, kFlagNan);
 }
 
-/* update_pressure for one particle: predicted density from the fixed lists at x*. */
+/* update_pressure for one particle: predicted density from the fixed lists at x*.  The
+ * list entries and the neighbours' x* are loaded four at a time before the four visits
+ * (the sum keeps list order).  x* is written by this kernel, so it is read with plain loads.
+ * The updated pressure's p / rho^2 (the initial density, as compute_pressure_force uses it)
+ * goes to pci_c for the force phase: the same IEEE quotient the force phase would form per
+ * pair, formed once per particle. */
 template <bool COMPAT>
 __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, int i) {
     const float4 pi = b.pos_pred[i];
@@ -129,9 +134,25 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
     const size_t n = (size_t)c.n;
     float pd = 0.f, pdb = 0.f;
     const int len = __ldg(&b.nlen[i]);
-    for (int k = 0; k < len; ++k) {
-        const int j = __ldg(&b.nlist[k * n + i]);
-        const float4 pj = b.pos_pred[j];
+    const int* __restrict__ e = b.nlist + i;
+    int k = 0;
+#pragma unroll 1
+    for (; k + 4 <= len; k += 4, e += 4 * n) {
+        int j[4];
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) j[u] = __ldg(e + u * n);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = b.pos_pred[j[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float dx = pi.x - q[u].x, dy = pi.y - q[u].y, dz = pi.z - q[u].z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (COMPAT || r2 < HH) { const float t = HH - r2; pd += (t * t) * t; }
+        }
+    }
+    for (; k < len; ++k, e += n) {
+        const float4 pj = b.pos_pred[__ldg(e)];
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (COMPAT || r2 < HH) { const float t = HH - r2; pd += (t * t) * t; }
@@ -146,35 +167,58 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
         if (COMPAT || r2 < HH) { const float t = HH - r2; pdb += ((t * t) * t) * __ldg(&b.bphi_s[j]); }
     }
     pdb *= c.default_eval;
-    const float e = pd + pdb - c.rho0_def;
-    const float dv = (0.f < e) ? e : 0.f;
+    const float e0 = pd + pdb - c.rho0_def;
+    const float dv = (0.f < e0) ? e0 : 0.f;
     b.dens_var[i] = dv;
-    b.pressure[i] += dv * c.delta;
+    const float p = b.pressure[i] + dv * c.delta;
+    b.pressure[i] = p;
+    const float di = __ldg(&b.density[i]);
+    b.pci_c[i] = p / (di * di);
     return dv;
 }
 
-/* compute_pressure_force for one particle (initial density, updated pressure). */
+/* compute_pressure_force for one particle (initial density, updated pressure):
+ * (p_i / rho_i^2 + p_j / rho_j^2) per pair with both quotients from pci_c (written by this
+ * kernel's update phase, so plain loads); entries and positions four at a time. */
 __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Bufs& b, int i) {
     const float4 pi = __ldg(&b.pos_s[i]);
     const float H = c.h_def;
     const size_t n = (size_t)c.n;
-    const float di = __ldg(&b.density[i]), p_i = b.pressure[i];
-    const float C = p_i / (di * di);
+    const float C = b.pci_c[i];
     float fx = 0.f, fy = 0.f, fz = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
     const int len = __ldg(&b.nlen[i]);
-    for (int k = 0; k < len; ++k) {
-        const int j = __ldg(&b.nlist[k * n + i]);
-        const float4 pj = __ldg(&b.pos_s[j]);
+    const int* __restrict__ e = b.nlist + i;
+    auto visit = [&](float4 pj, float cj) {
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-        const float l = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float il = rsqrtf(r2), l = r2 * il;
         if (l >= 1e-5f) {
-            const float dj = __ldg(&b.density[j]);
-            const float q = C + b.pressure[j] / (dj * dj);
-            const float il = 1.0f / l, t = (H - l) * (H - l);
+            const float q = C + cj;
+            const float t = (H - l) * (H - l);
             fx += q * ((dx * il) * t);
             fy += q * ((dy * il) * t);
             fz += q * ((dz * il) * t);
         }
+    };
+    int k = 0;
+#pragma unroll 1
+    for (; k + 4 <= len; k += 4, e += 4 * n) {
+        int j[4];
+        float4 q[4];
+        float cj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) j[u] = __ldg(e + u * n);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            q[u] = __ldg(&b.pos_s[j[u]]);
+            cj[u] = b.pci_c[j[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) visit(q[u], cj[u]);
+    }
+    for (; k < len; ++k, e += n) {
+        const int j = __ldg(e);
+        visit(__ldg(&b.pos_s[j]), b.pci_c[j]);
     }
     const float sf = (-(c.mass_def * c.mass_def)) * c.spiky_grad;
     fx *= sf; fy *= sf; fz *= sf;
@@ -253,8 +297,13 @@ __global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {
                                vz * vsc + tsc * (uz + oz * csc), 0.f);
 }
 
+/* 5 blocks/SM (at most 51 registers, a few bytes of spill): 6.7 ms per 4M-particle step vs
+ * 7.2 ms at the unbounded 60 registers (4 blocks/SM), measured on GB300. */
+#ifndef SPH_PCI_LOOP_MIN_BLOCKS
+#define SPH_PCI_LOOP_MIN_BLOCKS 5
+#endif
 template <bool COMPAT, bool FUSE_INTEGRATE>
-__global__ void __launch_bounds__(256) k_pci_loop(Const c, Bufs b, int min_iter, int max_iter) {
+__global__ void __launch_bounds__(256, SPH_PCI_LOOP_MIN_BLOCKS) k_pci_loop(Const c, Bufs b, int min_iter, int max_iter) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
     const int n = c.n;

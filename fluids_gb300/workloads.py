@@ -85,6 +85,22 @@ def pcisph_cube(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=500, dx=0.0125, **kw):
                 bodies=bodies, container=container, steps=steps, dx=dx)
 
 
+def pcisph_double_dam_4m(mode=capi.SPH_MODE_PHYSICS, seed=0, steps=200, n=128, dt=2e-4, **kw):
+    """The 4,194,304-particle double dam break of double_dam_4m stepped by PCISPH with the
+    parameters of pcisph_cube (tolerance 1 %, 3..8 iterations); dt = 2e-4 s is that
+    configuration's 5e-4 s scaled by the spacing ratio 0.005 / 0.0125."""
+    w = double_dam_4m(mode, seed, steps, n)
+    dx = w["dx"]
+    p = capi.make_params(capi.SPH_PCISPH, mode=mode, time_step=dt, max_vel=20.0, particle_radius=dx / 2.0,
+                         support_radius=2.0 * dx, pcisph_min_iterations=3, pcisph_max_iterations=8,
+                         pcisph_error_ratio=0.01, rest_density=REST_DENSITY, k_viscosity=1.7, gravity=9.81,
+                         surface_tension=1.0, relax_on_add=0)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    w.update(name="pcisph_double_dam_break_%d" % len(w["fluid"]), params=p)
+    return w
+
+
 def batched_scenes(nscenes=256, seed=0, dx=0.015, nmin=2048, nmax=65536):
     """Independent dam breaks of uneven size: N log-uniform in [nmin, nmax], container
     (a, 1, 1) with a ~ U[1, 3], viscosity log-uniform in [1e-3, 1e-1], c0 ~ U[10, 40] m/s.
