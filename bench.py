@@ -347,7 +347,9 @@ def bench_adjoint(torch, steps=200, every=20):
 def bench_pcisph(torch, steps, warmup, large=False):
     """PCISPH double block + rotated cube (358,400 fluid particles), or with `large` the
     4,194,304-particle double dam break, PHYSICS mode: device time of `steps` graph-replayed
-    steps (the predict-correct loop is one persistent kernel)."""
+    steps, each between its own CUDA events so that its predict-correct iteration count (the
+    loop is one persistent kernel) can be read after it; the kernel split comes from one
+    profiled step, whose iteration count is given beside it."""
     from fluids_gb300 import capi, workloads
     w = (workloads.pcisph_double_dam_4m if large else workloads.pcisph_cube)(capi.SPH_MODE_PHYSICS)
     stream = torch.cuda.Stream()
@@ -355,21 +357,25 @@ def bench_pcisph(torch, steps, warmup, large=False):
     ctx.set_stream(stream.cuda_stream)
     n, nb = ctx.particle_count(), ctx.boundary_particle_count()
     ctx.simulate(warmup)
+    # each timed step between its own pair of events on the context stream, its iteration
+    # count read after it (outside the events)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     iters = []
-    for _ in range(5):
+    torch.cuda.synchronize()
+    for a, b in ev:
+        a.record(stream)
         ctx.simulate(1)
+        b.record(stream)
         iters.append(int(ctx.get("PCI_ITERS")[0]))
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    ctx.simulate(steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1000.0
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
+    flags = ctx.device_flags()
+    prof = ctx.profile_step(1)
+    prof_iters = int(ctx.get("PCI_ITERS")[0])
     out = {"workload": w["name"], "particles": n, "boundary_particles": nb, "steps": steps,
            "updates_per_s": n * steps / t, "ms_per_step": 1000 * t / steps,
-           "pci_iterations_sampled": iters, "device_flags": ctx.device_flags(),
-           "kernel_ms_per_step": ctx.profile_step(3)}
+           "pci_iterations_mean": float(np.mean(iters)), "pci_iterations": iters, "device_flags": flags,
+           "kernel_ms_per_step": prof, "kernel_ms_iterations": prof_iters}
     ctx.close()
     return out
 

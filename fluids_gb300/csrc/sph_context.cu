@@ -439,11 +439,14 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
         mark(x, "k_neigh_lists");
         sph::launch_pci_init_density(s, c, b, bs);
         mark(x, "k_pci_init_density");
-        if (c.sigma != 0.f) {
-            sph::launch_normals(s, c, b, true, bs);
+        /* with surface tension the normal pass also writes the packed per-neighbour records
+         * (velocity, normal, 1/rho) that the force pass reads */
+        const bool pack = c.sigma != 0.f;
+        if (pack) {
+            sph::launch_normals(s, c, b, true, bs, true);
             mark(x, "k_normals");
         }
-        sph::launch_pci_init_forces(s, c, b, bs);
+        sph::launch_pci_init_forces(s, c, b, bs, pack);
         mark(x, "k_pci_init_forces");
         cudaMemsetAsync(b.pci_maxerr, 0, sizeof(float) * x->max_iter_slots, s);
         cudaMemsetAsync(b.barrier, 0, 4 * sizeof(unsigned), s);

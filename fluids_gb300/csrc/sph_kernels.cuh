@@ -95,7 +95,7 @@ void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, c
 
 /* sph_pcisph.cu */
 void launch_pci_init_density(cudaStream_t s, const Const& c, const Bufs& b, int bs);
-void launch_pci_init_forces(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+void launch_pci_init_forces(cudaStream_t s, const Const& c, const Bufs& b, int bs, bool pack = false);
 int pci_loop_blocks(int num_sms, int bs);
 cudaError_t launch_pci_loop(cudaStream_t s, const Const& c, const Bufs& b, int min_iter, int max_iter, int blocks,
                             int bs, bool fuse_integrate);

@@ -262,6 +262,13 @@ __global__ void __launch_bounds__(256) k_pci_init_density(Const c, Bufs b) {
     b.aux[i] = make_float4(0.f, 1.0f / d, d, 0.f);
 }
 
+/* PACK (surface tension on, the normal pass wrote nrec): each neighbour's velocity, normal
+ * and 1/rho come from nrec as two adjacent float4 (one 32-byte sector) instead of three
+ * loads, and the pair terms use the forms of the WCSPH force pass: 1/r from rsqrtf,
+ * (h - r) / rho_j as (h - r) * (1/rho_j), and 2 rho0 / (rho_i + rho_j) as
+ * 2 rho0 R_j / (rho_i R_j + 1) with a fast division (FP32 results within a few ulp of the
+ * IEEE forms).  Without PACK the pair terms are the kernel text's IEEE divisions. */
+template <bool PACK>
 __global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
@@ -269,22 +276,37 @@ __global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {
     const float4 pi = __ldg(&b.pos_s[i]), vi = __ldg(&b.vel_s[i]), ni = __ldg(&b.normal[i]);
     const float di = __ldg(&b.density[i]);
     const float H = c.h_def;
+    const float two_rho0 = 2.0f * c.rho0_def;
     float vx = 0.f, vy = 0.f, vz = 0.f, ux = 0.f, uy = 0.f, uz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f;
     list_neighbors(i, c.n, b.nlist, __ldg(&b.nlen[i]), b.pos_s, pi.x, pi.y, pi.z,
                    [&](int j, float4, float dx, float dy, float dz) {
-                       const float4 vj = __ldg(&b.vel_s[j]), nj = __ldg(&b.normal[j]);
-                       const float dj = __ldg(&b.density[j]);
-                       const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
-                       const float w = (H - rn) / dj;
+                       float4 vj, nj;
+                       float rn, inv, w, K;
+                       const float r2 = dx * dx + dy * dy + dz * dz;
+                       if constexpr (PACK) {
+                           vj = __ldg(&b.nrec[2 * (size_t)j]);
+                           nj = __ldg(&b.nrec[2 * (size_t)j + 1]);
+                           const float Rj = nj.w;
+                           inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+                           rn = r2 * inv;
+                           w = (H - rn) * Rj;
+                           K = __fdividef(two_rho0 * Rj, di * Rj + 1.0f);
+                       } else {
+                           vj = __ldg(&b.vel_s[j]);
+                           nj = __ldg(&b.normal[j]);
+                           const float dj = __ldg(&b.density[j]);
+                           rn = sqrtf(r2);
+                           w = (H - rn) / dj;
+                           K = st_corr(c.rho0_def, di, dj);
+                           inv = rn > 0.f ? 1.0f / rn : 0.f;
+                       }
                        vx += (vj.x - vi.x) * w;
                        vy += (vj.y - vi.y) * w;
                        vz += (vj.z - vi.z) * w;
-                       const float K = st_corr(c.rho0_def, di, dj);
                        ux += (ni.x - nj.x) * K;
                        uy += (ni.y - nj.y) * K;
                        uz += (ni.z - nj.z) * K;
                        const float sk = st_kernel(rn, H, c.st_term);
-                       const float inv = rn > 0.f ? 1.0f / rn : 0.f;
                        ox += ((dx * inv) * sk) * K;
                        oy += ((dy * inv) * sk) * K;
                        oz += ((dz * inv) * sk) * K;
@@ -347,9 +369,10 @@ void launch_pci_init_density(cudaStream_t s, const Const& c, const Bufs& b, int 
     if (c.compat) k_pci_init_density<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
     else k_pci_init_density<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
 }
-void launch_pci_init_forces(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+void launch_pci_init_forces(cudaStream_t s, const Const& c, const Bufs& b, int bs, bool pack) {
     if (c.n <= 0) return;
-    k_pci_init_forces<<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+    if (pack) k_pci_init_forces<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+    else k_pci_init_forces<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
 }
 
 static void* loop_fn(bool compat, bool fuse) {
