@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["wcsph4m", "wcsph1m", "wcsph65k", "pcisph"], default="wcsph4m",
+    ap.add_argument("--workload", choices=["wcsph4m", "wcsph1m", "wcsph65k", "pcisph", "pcisph4m"], default="wcsph4m",
                     help="wcsph1m: the 4M scene's blocks at 80^3 (profiling case)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -86,6 +86,8 @@ def load_workload(name, mode, seed=0):
         return workloads.double_dam_4m(mode=mode, seed=seed, n=80)
     if name == "wcsph65k":
         return workloads.dam_break_65k(mode=mode, seed=seed)
+    if name == "pcisph4m":
+        return workloads.pcisph_double_dam_4m(mode=mode, seed=seed)
     return workloads.pcisph_cube(mode=mode, seed=seed)
 
 
