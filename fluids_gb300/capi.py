@@ -19,7 +19,7 @@ _lib = None
 SPH_WCSPH, SPH_PCISPH = 0, 1
 SPH_MODE_COMPAT, SPH_MODE_PHYSICS = 0, 1
 SPH_NEIGH_SCAN, SPH_NEIGH_LIST = 0, 1
-SPH_FAULT_NONE, SPH_FAULT_BARRIER_STALL = 0, 1
+SPH_FAULT_NONE, SPH_FAULT_BARRIER_STALL, SPH_FAULT_ALLOC_FAIL = 0, 1, 2
 FLAGS = dict(NAN=1, ESCAPED=2, TIMEOUT=4, OVERFLOW=8, NONCONVERGED=16, NONSMOOTH=32)
 STATUS = {0: "SPH_OK", 1: "SPH_E_INVALID", 2: "SPH_E_CUDA", 3: "SPH_E_NONCONVERGED", 4: "SPH_E_ESCAPED",
           5: "SPH_E_NAN", 6: "SPH_E_TIMEOUT", 7: "SPH_E_OVERFLOW", 8: "SPH_E_STATE", 9: "SPH_E_NOMEM"}

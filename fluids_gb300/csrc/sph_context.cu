@@ -527,25 +527,52 @@ int rebuild(sph_ctx* x, bool keep) {
             SPH_CUDA(x, cudaMemcpy(x->bodies[k].xf, x->b.body_xf + 20 * k, sizeof x->bodies[k].xf,
                                    cudaMemcpyDeviceToHost));
     }
-    free_arena(x);
+    /* The new arena is allocated before the old one is freed, so a refused allocation (or a
+     * refused derivation) leaves the context as it was: sizes, constants, buffers and the
+     * device state.  Growth therefore needs the old and the new arena at once. */
+    const int old_n = x->N, old_nb = x->NB, old_slots = x->max_iter_slots;
+    const Const old_c = x->c;
+    const Bufs old_b = x->b;
+    sph::SceneDev* const old_scenes = x->d_scenes;
+    int32_t* const old_scene_of = x->d_scene_of;
+    double* const old_scene_stats = x->d_scene_stats;
+    auto restore = [&]() {
+        x->N = old_n; x->NB = old_nb; x->max_iter_slots = old_slots;
+        x->c = old_c;
+        x->b = old_b;
+        x->d_scenes = old_scenes; x->d_scene_of = old_scene_of; x->d_scene_stats = old_scene_stats;
+    };
     x->N = (int)(x->vol_pos.size() / 4);
     x->NB = (int)(x->braw_host.size() / 4);
     int rc = derive(x);
-    if (rc != SPH_OK) return rc;
+    if (rc != SPH_OK) {
+        restore();
+        return rc;
+    }
     {
         const int relax_iter = x->p.pcisph_relax_max_iterations > 0 ? x->p.pcisph_relax_max_iterations : 10000;
         x->max_iter_slots = std::max(std::max(x->p.pcisph_max_iterations, relax_iter), 1);
     }
     Carver dry;
     carve(x, dry);
-    x->arena_bytes = dry.off + 256;
-    cudaError_t e = cudaMalloc(&x->arena, x->arena_bytes);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        x->arena = nullptr;
-        return fail(x, SPH_E_NOMEM, "device arena of " + std::to_string(x->arena_bytes) + " bytes: " +
-                                        cudaGetErrorString(e));
+    const size_t bytes = dry.off + 256;
+    void* fresh = nullptr;
+    cudaError_t e;
+    if (x->inject_alloc) {
+        /* injected allocator failure: the allocation is refused as cudaMalloc refuses one */
+        x->inject_alloc = false;
+        e = cudaErrorMemoryAllocation;
+    } else {
+        e = cudaMalloc(&fresh, bytes);
+        if (e != cudaSuccess) cudaGetLastError();
     }
+    if (e != cudaSuccess) {
+        restore();
+        return fail(x, SPH_E_NOMEM, "device arena of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+    }
+    free_arena(x);
+    x->arena = static_cast<char*>(fresh);
+    x->arena_bytes = bytes;
     Carver real;
     real.base = x->arena;
     carve(x, real);
@@ -991,10 +1018,15 @@ int sph_reset(sph_ctx* x, const sph_params* params) {
     if (check_ctx(x) || !params) return SPH_E_INVALID;
     if (params->block_size % 32 != 0 || params->block_size > 256 || params->block_size < 0)
         return fail(x, SPH_E_INVALID, "block_size must be a multiple of 32 up to 256");
+    const sph_params old_p = x->p;
+    const int old_bs = x->bs;
     x->p = *params;
     x->bs = x->p.block_size > 0 ? x->p.block_size : 256;
     int rc = rebuild(x, false);
-    if (rc != SPH_OK) return rc;
+    if (rc != SPH_OK) {
+        if (rc == SPH_E_NOMEM) { x->p = old_p; x->bs = old_bs; }   /* the context is unchanged */
+        return rc;
+    }
     return relax(x);
 }
 
@@ -1002,9 +1034,12 @@ int sph_set_rect_limits(sph_ctx* x, float w, float h, float d) {
     if (check_ctx(x)) return SPH_E_INVALID;
     if (!x->scene_in.empty()) return fail(x, SPH_E_STATE, "a batched context sets containers per scene");
     if (!(w > 0.f && h > 0.f && d > 0.f)) return fail(x, SPH_E_INVALID, "container extents must be > 0");
+    const float old_lim[3] = {x->lim[0], x->lim[1], x->lim[2]};
     x->lim[0] = w; x->lim[1] = h; x->lim[2] = d;
     if (!x->has_state) return derive(x);
-    return rebuild(x, true);
+    const int rc = rebuild(x, true);
+    if (rc == SPH_E_NOMEM) std::memcpy(x->lim, old_lim, sizeof old_lim);   /* the context is unchanged */
+    return rc;
 }
 
 int sph_add_volume(sph_ctx* x, const float* pos4, const float* vel4, int n) {
@@ -1012,12 +1047,18 @@ int sph_add_volume(sph_ctx* x, const float* pos4, const float* vel4, int n) {
     if (!x->scene_in.empty()) return fail(x, SPH_E_STATE, "a batched context takes its particles at creation");
     if (n < 0 || (n > 0 && !pos4)) return fail(x, SPH_E_INVALID, "bad particle array");
     const size_t old = x->vol_pos.size();
+    if (old / 4 + (size_t)n > (size_t)0x3fffffff) return fail(x, SPH_E_OVERFLOW, "more than 2^30 particles");
     x->vol_pos.insert(x->vol_pos.end(), pos4, pos4 + 4 * (size_t)n);
     x->vol_vel.resize(old + 4 * (size_t)n, 0.f);
     if (vel4) std::memcpy(&x->vol_vel[old], vel4, 16 * (size_t)n);
-    if (x->vol_pos.size() / 4 > (size_t)0x3fffffff) return fail(x, SPH_E_OVERFLOW, "more than 2^30 particles");
     int rc = rebuild(x, false);
-    if (rc != SPH_OK) return rc;
+    if (rc != SPH_OK) {
+        if (rc == SPH_E_NOMEM) {   /* the context is unchanged: the volume is not added */
+            x->vol_pos.resize(old);
+            x->vol_vel.resize(old);
+        }
+        return rc;
+    }
     return relax(x);
 }
 
@@ -1037,9 +1078,16 @@ int sph_add_boundary(sph_ctx* x, const float* pos4, int n, int can_move, const f
         bd.xf[12 + k] = lin4 ? lin4[k] : 0.f;
         bd.xf[16 + k] = ang4 ? ang4[k] : 0.f;
     }
+    const size_t old = x->braw_host.size();
+    if (old / 4 + (size_t)n > (size_t)0x3fffffff) return fail(x, SPH_E_OVERFLOW, "more than 2^30 particles");
     x->bodies.push_back(bd);
     x->braw_host.insert(x->braw_host.end(), pos4, pos4 + 4 * (size_t)n);
-    return rebuild(x, true);
+    const int rc = rebuild(x, true);
+    if (rc == SPH_E_NOMEM) {   /* the context is unchanged: the body is not added */
+        x->bodies.pop_back();
+        x->braw_host.resize(old);
+    }
+    return rc;
 }
 
 int sph_set_body_transform(sph_ctx* x, int body, const float* rot3x4, const float* lin4, const float* ang4) {
@@ -1191,6 +1239,11 @@ int sph_inject_fault(sph_ctx* x, int kind) {
     if (check_ctx(x)) return SPH_E_INVALID;
     if (kind == SPH_FAULT_NONE) {
         x->inject = 0;
+        x->inject_alloc = false;
+        return SPH_OK;
+    }
+    if (kind == SPH_FAULT_ALLOC_FAIL) {
+        x->inject_alloc = true;
         return SPH_OK;
     }
     if (kind != SPH_FAULT_BARRIER_STALL) return fail(x, SPH_E_INVALID, "unknown fault kind");

@@ -62,6 +62,7 @@ struct sph_ctx {
     int32_t* d_scene_of = nullptr;
     double* d_scene_stats = nullptr;
     int inject = 0;   /* one-shot fault for the next step (sph_inject_fault) */
+    bool inject_alloc = false;   /* the next arena allocation fails (sph_inject_fault) */
     /* depth-test scratch of sph_render_depth: 8 bytes per pixel */
     void* render_buf = nullptr;
     size_t render_pixels = 0;

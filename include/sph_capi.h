@@ -204,8 +204,12 @@ int sph_synchronize(sph_ctx* ctx);
  * (PCISPH contexts): the next step's predict-correct kernel waits at its grid barrier for one
  * CTA more than it launched, so every CTA's bounded wait runs out (about a second), sets
  * SPH_FLAG_TIMEOUT and returns; the step's integration is skipped, the context stays usable
- * and the steps after it are normal.  Nothing faults or hangs.  SPH_FAULT_NONE cancels. */
-enum sph_fault { SPH_FAULT_NONE = 0, SPH_FAULT_BARRIER_STALL = 1 };
+ * and the steps after it are normal.  Nothing faults or hangs.  SPH_FAULT_ALLOC_FAIL (any
+ * context): the next device-arena allocation (sph_add_volume, sph_add_boundary,
+ * sph_set_rect_limits, sph_reset) is refused as cudaMalloc refuses one; the call returns
+ * SPH_E_NOMEM and leaves the context as it was (the arena is grown by allocating the new one
+ * before freeing the old).  SPH_FAULT_NONE cancels both. */
+enum sph_fault { SPH_FAULT_NONE = 0, SPH_FAULT_BARRIER_STALL = 1, SPH_FAULT_ALLOC_FAIL = 2 };
 int sph_inject_fault(sph_ctx* ctx, int kind);
 /* Reads (and with clear = 1 resets) the device status word; synchronises. */
 int sph_device_flags(sph_ctx* ctx, unsigned* flags, int clear);

@@ -83,3 +83,38 @@ def test_injected_barrier_stall_times_out_and_the_context_recovers(gpu_lib):
     assert not np.array_equal(ctx.get("POS"), before)
     with pytest.raises(capi.SphError):
         wcsph_ctx().inject_fault(capi.SPH_FAULT_BARRIER_STALL)   # WCSPH has no grid barrier
+
+
+def test_injected_allocation_failure_leaves_the_context_unchanged(gpu_lib):
+    """An allocator failure made on the host (the next arena allocation is refused as
+    cudaMalloc refuses one): each scene call that must grow the arena returns SPH_E_NOMEM, and
+    the context keeps its particles, bodies, container and evolved state, steps on, and grows
+    once the allocation is allowed."""
+    from scenes_np import jittered_block
+    ctx = wcsph_ctx()
+    ctx.simulate(3)
+    n, nb = ctx.particle_count(), ctx.boundary_particle_count()
+    state = {f: ctx.get(f).copy() for f in ("POS", "VEL", "VEL_HALF", "ID")}
+    extra = jittered_block(4, 4, 4, 0.015, (0.3, -0.2, 0.0), seed=9)
+    wall = np.array([[x, 0.2, z, 1.0] for x in np.arange(-0.1, 0.1, 0.015) for z in np.arange(-0.1, 0.1, 0.015)],
+                    np.float32)
+    for call in (lambda: ctx.add_volume(extra), lambda: ctx.add_boundary(wall),
+                 lambda: ctx.set_rect_limits(2.2, 1.0, 1.0)):
+        ctx.inject_fault(capi.SPH_FAULT_ALLOC_FAIL)
+        with pytest.raises(capi.SphError) as e:
+            call()
+        assert e.value.code == capi.SPH_E_NOMEM
+        assert ctx.particle_count() == n and ctx.boundary_particle_count() == nb
+        for f, a in state.items():
+            assert np.array_equal(ctx.get(f), a), f
+    ctx.simulate(2)                      # the context steps on
+    assert ctx.device_flags(clear=True) & (F["NAN"] | F["TIMEOUT"]) == 0
+    assert not np.array_equal(ctx.get("POS"), state["POS"])
+    ctx.add_boundary(wall)               # and grows once the allocation is allowed
+    assert ctx.boundary_particle_count() == nb + len(wall)
+    ctx.inject_fault(capi.SPH_FAULT_ALLOC_FAIL)
+    ctx.inject_fault(capi.SPH_FAULT_NONE)   # cancelled: the next growth succeeds
+    ctx.add_volume(extra)
+    assert ctx.particle_count() == n + len(extra)
+    ctx.simulate(2)
+    assert np.isfinite(ctx.get("POS")).all()
