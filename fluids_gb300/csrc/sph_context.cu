@@ -405,13 +405,18 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
     const int bs = x->bs;
     int rc;
     mark(x, "start");
-    const int pre[] = {SPH_S_BOUNDARY_SYNC, SPH_S_HASHES, SPH_S_SORT, SPH_S_SHUFFLE, SPH_S_CELL_INTERVALS};
-    const char* pre_names[] = {"boundary_sync", "k_hashes", "sort", "k_gather", "k_cell_ranges"};
-    for (int k = 0; k < 5; ++k) {
+    const int pre[] = {SPH_S_BOUNDARY_SYNC, SPH_S_HASHES, SPH_S_SORT};
+    const char* pre_names[] = {"boundary_sync", "k_hashes", "sort"};
+    for (int k = 0; k < 3; ++k) {
         if (pre[k] == SPH_S_BOUNDARY_SYNC && !(x->NB > 0 && x->any_movable)) continue;
         if ((rc = run_stage_impl(x, pre[k])) != SPH_OK) return rc;
         mark(x, pre_names[k]);
     }
+    /* the SHUFFLE and CELL_INTERVALS stages in one pass */
+    sph::launch_gather_ranges(s, c, x->N, b.mask_sorted, b.pos, b.pos_s, b.vel, b.vel_s,
+                              x->p.method == SPH_WCSPH ? b.vhalf : nullptr, b.vhalf_s, b.ids, b.ids_s, b.keys_sorted,
+                              b.tab, b.cell_prev, b.flags, bs, b.scenes, b.scene_of);
+    mark(x, "k_gather_ranges");
     if (x->p.method == SPH_WCSPH) {
         const bool lists = x->p.neighbor_mode == SPH_NEIGH_LIST;
         if (lists) {

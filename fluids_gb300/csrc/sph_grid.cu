@@ -106,6 +106,42 @@ __global__ void k_cell_ranges(Const c, const float4* __restrict__ spos, const ui
     }
 }
 
+/* k_gather and k_cell_ranges in one pass for the fused step: the thread of sorted particle i
+ * already holds its position, and the position of particle i + 1 is fetched only where a
+ * cell ends (h0 < h1).  Same results as the two kernels. */
+__global__ void k_gather_ranges(Const c, int n, const int32_t* __restrict__ perm, const float4* __restrict__ a,
+                                float4* __restrict__ as, const float4* __restrict__ b, float4* __restrict__ bs,
+                                const float4* __restrict__ c3, float4* __restrict__ cs,
+                                const int32_t* __restrict__ ids, int32_t* __restrict__ ids_s,
+                                const uint32_t* __restrict__ keys, int2* __restrict__ tab,
+                                int32_t* __restrict__ cell_out, unsigned* __restrict__ flags,
+                                const SceneDev* __restrict__ scenes, const int32_t* __restrict__ scene_of) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int src = __ldg(&perm[i]);
+    const float4 p = __ldg(&a[src]);
+    as[i] = p;
+    bs[i] = __ldg(&b[src]);
+    if (c3) cs[i] = __ldg(&c3[src]);
+    if (ids) ids_s[i] = __ldg(&ids[src]);
+    int* t = reinterpret_cast<int*>(tab);
+    const long long id0 = global_cell(c, p, scenes, scene_of, i);
+    const bool ok0 = id0 >= 0;
+    if (!ok0) atomicOr(flags, kFlagEscaped);
+    cell_out[i] = ok0 ? (int)id0 : -1;
+    if (i == n - 1) {
+        if (ok0) t[2 * id0 + 1] = i + 1;
+    } else {
+        const uint32_t h0 = __ldg(&keys[i]), h1 = __ldg(&keys[i + 1]);
+        if (h0 < h1) {
+            const float4 p1 = __ldg(&a[__ldg(&perm[i + 1])]);
+            const long long id1 = global_cell(c, p1, scenes, scene_of, i + 1);
+            if (ok0) t[2 * id0 + 1] = i + 1;
+            if (id1 >= 0) t[2 * id1] = i + 1;
+        }
+    }
+}
+
 __global__ void k_neigh_lists(Const c0, const float4* __restrict__ spos, const int2* __restrict__ tab0,
                               const float4* __restrict__ bpos_s, const int2* __restrict__ btab0,
                               int* __restrict__ nlist, int* __restrict__ nlen, int* __restrict__ sblist,
@@ -156,6 +192,14 @@ void launch_gather_boundary(cudaStream_t s, int n, const int32_t* perm, const fl
                             const int32_t* body, int32_t* body_s, const float* phi, float* phi_s, int bs) {
     if (n <= 0) return;
     k_gather_boundary<<<blocks_for(n, bs), bs, 0, s>>>(n, perm, pos, pos_s, body, body_s, phi, phi_s);
+}
+void launch_gather_ranges(cudaStream_t s, const Const& c, int n, const int32_t* perm, const float4* a, float4* as,
+                          const float4* b, float4* bs_, const float4* c3, float4* cs, const int32_t* ids,
+                          int32_t* ids_s, const uint32_t* keys, int2* tab, int32_t* cell_out, unsigned* flags, int bs,
+                          const SceneDev* scenes, const int32_t* scene_of) {
+    if (n <= 0) return;
+    k_gather_ranges<<<blocks_for(n, bs), bs, 0, s>>>(c, n, perm, a, as, b, bs_, c3, cs, ids, ids_s, keys, tab,
+                                                     cell_out, flags, scenes, scene_of);
 }
 void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, const uint32_t* keys, int n,
                         int2* tab, int32_t* cell_out, unsigned* flags, int bs, const SceneDev* scenes,

@@ -69,6 +69,10 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
 void launch_hashes(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int32_t* mask,
                    int2* tab, const int32_t* cell_prev, unsigned* flags, int bs, const SceneDev* scenes,
                    const int32_t* scene_of);
+void launch_gather_ranges(cudaStream_t s, const Const& c, int n, const int32_t* perm, const float4* a, float4* as,
+                          const float4* b, float4* bs_, const float4* c3, float4* cs, const int32_t* ids,
+                          int32_t* ids_s, const uint32_t* keys, int2* tab, int32_t* cell_out, unsigned* flags, int bs,
+                          const SceneDev* scenes, const int32_t* scene_of);
 void launch_gather(cudaStream_t s, int n, const int32_t* perm, const float4* a, float4* as, const float4* b,
                    float4* bs_, const float4* c3, float4* cs, const int32_t* ids, int32_t* ids_s, int bs);
 void launch_gather_boundary(cudaStream_t s, int n, const int32_t* perm, const float4* pos, float4* pos_s,
