@@ -246,6 +246,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.ids = cv.take<int32_t>(n); b.ids_s = cv.take<int32_t>(n);
     b.tab = cv.take<int2>((size_t)x->c.ncells);
     b.cell_prev = cv.take<int32_t>(n);
+    b.noff = cv.take<int32_t>(32);
     b.nlist = cv.take<int32_t>(cap * n); b.nlen = cv.take<int32_t>(n);
     b.sblist = cv.take<int32_t>(cap * n); b.sblen = cv.take<int32_t>(n);
     b.sort_ws = cv.take<char>(sph::sort_workspace_bytes((int)n, x->c.key_bits));
@@ -340,7 +341,7 @@ int run_stage_impl(sph_ctx* x, int stage) {
     case SPH_S_NEIGH_LIST:
     case SPH_S_SB_NEIGH_LIST:
         sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
-                                b.scenes, b.scene_of, b.bnear);
+                                b.scenes, b.scene_of, b.bnear, b.noff);
         break;
     case SPH_S_WC_DENSITY:
         sph::launch_wc_density(s, c, b, x->p.neighbor_mode == SPH_NEIGH_LIST, bs);
@@ -440,7 +441,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
         mark(x, "k_wc_forces");
     } else {
         sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
-                                b.scenes, b.scene_of, b.bnear);
+                                b.scenes, b.scene_of, b.bnear, b.noff);
         mark(x, "k_neigh_lists");
         sph::launch_pci_init_density(s, c, b, bs);
         mark(x, "k_pci_init_density");
@@ -586,6 +587,12 @@ int rebuild(sph_ctx* x, bool keep) {
     SPH_CUDA(x, cudaMemsetAsync(x->arena, 0, x->arena_bytes, s));
     SPH_CUDA(x, cudaMemsetAsync(b.cell_prev, 0xff, sizeof(int32_t) * (x->N > 0 ? x->N : 1), s));
     SPH_CUDA(x, cudaMemsetAsync(b.bcell_prev, 0xff, sizeof(int32_t) * (x->NB > 0 ? x->NB : 1), s));
+    {
+        int32_t off[32] = {0};
+        sph::neigh_linear_offsets(x->c.nx, x->c.ny, off);
+        SPH_CUDA(x, cudaMemcpyAsync(b.noff, off, sizeof off, cudaMemcpyHostToDevice, s));
+        SPH_CUDA(x, cudaStreamSynchronize(s));   /* off is a stack array */
+    }
     if (x->scene_in.empty()) {
         /* the one scene of a single-scene context: its grid and parameters */
         sph::SceneDev sd{};

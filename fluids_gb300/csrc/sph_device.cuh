@@ -228,12 +228,23 @@ __device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py
 #endif
 constexpr int kBuildUnroll = SPH_BUILD_UNROLL;
 /* CELL_NEIGH_OFFSET order as (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4, one byte per offset. */
-static __constant__ uint8_t kNeighCode[27] = {
-    0x15, 0x00, 0x10, 0x20, 0x04, 0x14, 0x24, 0x08, 0x18, 0x28, 0x01, 0x11, 0x21,
-    0x05, 0x25, 0x09, 0x19, 0x29, 0x02, 0x12, 0x22, 0x06, 0x16, 0x26, 0x0a, 0x1a, 0x2a};
+#define SPH_NEIGH_CODES                                                                                  \
+    0x15, 0x00, 0x10, 0x20, 0x04, 0x14, 0x24, 0x08, 0x18, 0x28, 0x01, 0x11, 0x21, 0x05, 0x25, 0x09, 0x19, \
+        0x29, 0x02, 0x12, 0x22, 0x06, 0x16, 0x26, 0x0a, 0x1a, 0x2a
+static __constant__ uint8_t kNeighCode[27] = {SPH_NEIGH_CODES};
+/* Linear cell-id offsets of the 27 neighbour cells, in the order above, on an nx x ny x nz
+ * grid (host side; the list builder reads them for cells away from the grid's faces). */
+inline void neigh_linear_offsets(int nx, int ny, int32_t* out27) {
+    static const uint8_t codes[27] = {SPH_NEIGH_CODES};
+    for (int o = 0; o < 27; ++o) {
+        const int ox = (codes[o] & 3) - 1, oy = ((codes[o] >> 2) & 3) - 1, oz = ((codes[o] >> 4) & 3) - 1;
+        out27[o] = ox + nx * oy + nx * ny * oz;
+    }
+}
 template <class F>
 __device__ __forceinline__ int build_scan(const Const& c, float px, float py, float pz, int cx, int cy, int cz,
-                                          const int2* __restrict__ tab, const float4* __restrict__ npos, F&& f) {
+                                          const int2* __restrict__ tab, const float4* __restrict__ npos,
+                                          const int32_t* __restrict__ noff, F&& f) {
     const float h2 = c.h2_list;
     int cnt = 0;
     /* PHYSICS grid: 32-bit cell ids (the grid has < 2^31 cells) and no bounds test for a cell
@@ -244,13 +255,17 @@ __device__ __forceinline__ int build_scan(const Const& c, float px, float py, fl
     const int base = cx + sy * cy + sz * cz;
 #pragma unroll 1
     for (int o = 0; o < 27 && cnt < c.cap; ++o) {
-        const int code = kNeighCode[o];
-        const int ox = (code & 3) - 1, oy = ((code >> 2) & 3) - 1, oz = ((code >> 4) & 3) - 1;
         long long id;
-        if (interior) {
-            id = base + ox + sy * oy + sz * oz;
-        } else if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) {
-            continue;
+        if (interior && noff != nullptr) {
+            id = base + __ldg(&noff[o]);   /* one load, the same address in every lane */
+        } else {
+            const int code = kNeighCode[o];
+            const int ox = (code & 3) - 1, oy = ((code >> 2) & 3) - 1, oz = ((code >> 4) & 3) - 1;
+            if (interior) {
+                id = base + ox + sy * oy + sz * oz;
+            } else if (!neigh_cell(c, cx + ox, cy + oy, cz + oz, id)) {
+                continue;
+            }
         }
         const int2 r = __ldg(&tab[id]);
         if (cnt + (r.y - r.x) <= c.cap) {

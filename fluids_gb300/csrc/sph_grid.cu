@@ -146,7 +146,8 @@ __global__ void k_neigh_lists(Const c0, const float4* __restrict__ spos, const i
                               const float4* __restrict__ bpos_s, const int2* __restrict__ btab0,
                               int* __restrict__ nlist, int* __restrict__ nlen, int* __restrict__ sblist,
                               int* __restrict__ sblen, const SceneDev* __restrict__ scenes,
-                              const int32_t* __restrict__ scene_of, const uint8_t* __restrict__ bnear) {
+                              const int32_t* __restrict__ scene_of, const uint8_t* __restrict__ bnear,
+                              const int32_t* __restrict__ noff) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
@@ -158,7 +159,8 @@ __global__ void k_neigh_lists(Const c0, const float4* __restrict__ spos, const i
     int cx, cy, cz;
     cell_of(c, pi.x, pi.y, pi.z, cx, cy, cz);
     int* out = nlist + i;
-    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, [&](bool hit, int j, float) {
+    const int* nof = c.batched ? nullptr : noff;
+    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, nof, [&](bool hit, int j, float) {
         if (hit) *out = j;
         out += hit ? n : 0;
     });
@@ -167,7 +169,7 @@ __global__ void k_neigh_lists(Const c0, const float4* __restrict__ spos, const i
     /* boundary cells only where bnear marks one within a cell (PHYSICS grid) */
     if (c.nb > 0 && (c.wrap || bnear == nullptr || bnear[base + cell_lin(c, cx, cy, cz)] != 0)) {
         int* bout = sblist + i;
-        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, [&](bool hit, int j, float) {
+        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, nof, [&](bool hit, int j, float) {
             if (hit) *bout = j;
             bout += hit ? n : 0;
         });
@@ -209,10 +211,11 @@ void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, cons
 }
 void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, const int2* tab, const float4* bpos_s,
                         const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs,
-                        const SceneDev* scenes, const int32_t* scene_of, const uint8_t* bnear) {
+                        const SceneDev* scenes, const int32_t* scene_of, const uint8_t* bnear,
+                        const int32_t* noff) {
     if (c.n <= 0) return;
     k_neigh_lists<<<blocks_for(c.n, bs), bs, 0, s>>>(c, spos, tab, bpos_s, btab, nlist, nlen, sblist, sblen, scenes,
-                                                     scene_of, bnear);
+                                                     scene_of, bnear, noff);
 }
 
 }  // namespace sph

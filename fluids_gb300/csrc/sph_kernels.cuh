@@ -26,6 +26,7 @@ struct Bufs {
     int32_t *ids, *ids_s;
     int2* tab;                             /* fluid cell table */
     int32_t* cell_prev;                    /* cell id of each sorted particle (sparse clear) */
+    int32_t* noff;                         /* 27 linear neighbour-cell offsets (single-scene grid) */
     int32_t *nlist, *nlen, *sblist, *sblen;
     void* sort_ws;
     /* boundary */
@@ -82,7 +83,8 @@ void launch_cell_ranges(cudaStream_t s, const Const& c, const float4* spos, cons
                         const int32_t* scene_of);
 void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, const int2* tab, const float4* bpos_s,
                         const int2* btab, int* nlist, int* nlen, int* sblist, int* sblen, int bs,
-                        const SceneDev* scenes, const int32_t* scene_of, const uint8_t* bnear);
+                        const SceneDev* scenes, const int32_t* scene_of, const uint8_t* bnear,
+                        const int32_t* noff = nullptr);
 
 /* sph_wcsph.cu */
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);

@@ -66,8 +66,10 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
 /* compute_neigh_list (kernels/grid.cl:145-182, fluid and boundary) fused with
  * compute_density_pressure: the density sums run over exactly the pairs written to the
  * lists, in list order, so the step needs no separate density pass. */
+/* 8 blocks/SM holds the builder at 32 registers (full occupancy); unbounded it takes 34 and
+ * runs slower (1.147 vs 1.108 ms at 4M, measured on GB300). */
 #ifndef SPH_LISTS_MIN_BLOCKS
-#define SPH_LISTS_MIN_BLOCKS 1
+#define SPH_LISTS_MIN_BLOCKS 8
 #endif
 /* REMAP (the adjoint's tape, which keeps particles in id order): the list of sorted particle
  * i is written as row remap[i] with entries remap[j], and its density, pressure and aux go to
@@ -85,7 +87,8 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
                                                        const int32_t* __restrict__ scene_of,
                                                        const int32_t* __restrict__ remap = nullptr,
                                                        unsigned* __restrict__ flags = nullptr,
-                                                       const uint8_t* __restrict__ bnear = nullptr) {
+                                                       const uint8_t* __restrict__ bnear = nullptr,
+                                                       const int32_t* __restrict__ noff = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c0.n) return;
     Const c = c0;
@@ -100,7 +103,8 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     cell_of(c, pi.x, pi.y, pi.z, cx, cy, cz);
     float di = 0.f;
     int* out = nlist + row;
-    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, [&](bool hit, int j, float r2) {
+    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, BATCH ? nullptr : noff,
+                             [&](bool hit, int j, float r2) {
         if (hit) *out = REMAP ? __ldg(&remap[j]) : j;
         out += hit ? n : 0;
         const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
@@ -116,7 +120,8 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     const bool scan_b = c.wrap || bnear == nullptr || bnear[base + cell_lin(c, cx, cy, cz)] != 0;
     if (c.nb > 0 && !REMAP && scan_b) {
         int* bout = sblist + i;
-        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, [&](bool hit, int j, float r2) {
+        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, BATCH ? nullptr : noff,
+                        [&](bool hit, int j, float r2) {
             if (hit) *bout = j;
             bout += hit ? n : 0;
             const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
@@ -371,7 +376,7 @@ static void lists_density_launch(cudaStream_t s, const Const& c, const Bufs& b, 
     k_lists_density<COMPAT, BATCH><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s,
                                                                 b.nlist, b.nlen, b.sblist, b.sblen, b.density,
                                                                 b.pressure, b.aux, b.scenes, b.scene_of, nullptr,
-                                                                nullptr, b.bnear);
+                                                                nullptr, b.bnear, b.noff);
 }
 
 void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, const int32_t* remap, int bs) {
