@@ -67,24 +67,35 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_
 }
 }  // namespace
 
-/* Histogram of all digit passes: hist[pass][256]. */
+/* Histogram of all digit passes: hist[pass][256].  Each thread loads kHistItems keys
+ * (coalesced across the warp) before it ranks any, so that their loads are in flight
+ * together; per key and pass, the lanes holding the same digit add their count once. */
+constexpr int kHistItems = 8;
 __global__ void __launch_bounds__(kThreads) k_sort_hist(const uint32_t* __restrict__ keys, int n, int passes,
                                                         uint32_t* __restrict__ hist) {
     __shared__ uint32_t s_hist[4][256];
     for (int t = threadIdx.x; t < 4 * 256; t += kThreads) (&s_hist[0][0])[t] = 0u;
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int stride = gridDim.x * kThreads;
-    for (int base = blockIdx.x * kThreads; base < n; base += stride) {
-        const int i = base + threadIdx.x;
-        const bool valid = i < n;
-        const uint32_t k = valid ? keys[i] : 0u;
-        const unsigned active = __ballot_sync(0xffffffffu, valid);
-        if (valid) {
-            for (int p = 0; p < passes; ++p) {
-                const uint32_t d = (k >> (8 * p)) & 255u;
-                const unsigned peers = __match_any_sync(active, d);
-                if (lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+    const long long step = (long long)gridDim.x * kThreads * kHistItems;
+    for (long long base = (long long)blockIdx.x * kThreads * kHistItems; base < n; base += step) {
+        uint32_t k[kHistItems];
+#pragma unroll
+        for (int u = 0; u < kHistItems; ++u) {
+            const long long i = base + (long long)u * kThreads + threadIdx.x;
+            k[u] = i < n ? __ldg(&keys[i]) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kHistItems; ++u) {
+            const long long i = base + (long long)u * kThreads + threadIdx.x;
+            const bool valid = i < n;
+            const unsigned active = __ballot_sync(0xffffffffu, valid);
+            if (valid) {
+                for (int p = 0; p < passes; ++p) {
+                    const uint32_t d = (k[u] >> (8 * p)) & 255u;
+                    const unsigned peers = __match_any_sync(active, d);
+                    if (lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+                }
             }
         }
     }
@@ -219,7 +230,7 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
     uint32_t* counters = hist + 4 * 256;
     uint32_t* status = counters + 64;
     cudaMemsetAsync(ws, 0, sort_workspace_bytes(n, key_bits), s);
-    int hblocks = min(tiles * kItems, 2 * num_sms);
+    int hblocks = min((n + kThreads * kHistItems - 1) / (kThreads * kHistItems), 4 * num_sms);
     if (hblocks < 1) hblocks = 1;
     k_sort_hist<<<hblocks, kThreads, 0, s>>>(k0, n, passes, hist);
     uint32_t *ki = k0, *ko = k1;
