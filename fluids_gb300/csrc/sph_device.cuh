@@ -217,8 +217,9 @@ __device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py
 }
 
 /* The scan of scan_neighbors<true> (same cells, order, cap and exact r^2), written for the
- * list builder: every candidate runs the same instructions and f(hit, j, r2) applies the
- * hit with predicated stores and selects instead of a branch, so the lanes of a warp that
+ * list builder: every candidate runs the same instructions and f(hit, j, r2, k) applies the
+ * hit (k = the entries kept so far, the slot of a hit) with predicated stores and selects
+ * instead of a branch, so the lanes of a warp that
  * walk the same cell stay converged whichever of them hit.  The particle's cell (cx, cy, cz)
  * comes from the caller.  No cell is skipped by distance: in a warp the lanes that share a
  * cell would skip different cells, so the warp walks their union anyway, and measured on
@@ -274,7 +275,7 @@ __device__ __forceinline__ int build_scan(const Const& c, float px, float py, fl
                 const float4 pj = __ldg(&npos[j]);
                 const float r2 = r2_exact(__fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
                 const bool hit = r2 < h2;
-                f(hit, j, r2);
+                f(hit, j, r2, cnt);
                 cnt += hit ? 1 : 0;
             }
         } else {
@@ -283,12 +284,18 @@ __device__ __forceinline__ int build_scan(const Const& c, float px, float py, fl
                 const float4 pj = __ldg(&npos[j]);
                 const float r2 = r2_exact(__fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
                 const bool hit = r2 < h2;
-                f(hit, j, r2);
+                f(hit, j, r2, cnt);
                 cnt += hit ? 1 : 0;
             }
         }
     }
     return cnt;
+}
+
+/* Entry k of a column-major list row (row + k * n): one widening multiply-add on the entry
+ * count instead of a 64-bit pointer advanced per candidate; n4 = 4 n bytes (n < 2^30). */
+__device__ __forceinline__ int* list_slot(char* row, int k, unsigned n4) {
+    return reinterpret_cast<int*>(row + (unsigned long long)(unsigned)k * n4);
 }
 
 /* Visits the materialised list of particle i (column-major list[k * n + i], grid.cl:174).

@@ -155,23 +155,21 @@ __global__ void k_neigh_lists(Const c0, const float4* __restrict__ spos, const i
     const int2* tab = tab0 + base;
     const int2* btab = btab0 + base;
     const float4 pi = spos[i];
-    const size_t n = (size_t)c.n;
     int cx, cy, cz;
     cell_of(c, pi.x, pi.y, pi.z, cx, cy, cz);
-    int* out = nlist + i;
     const int* nof = c.batched ? nullptr : noff;
-    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, nof, [&](bool hit, int j, float) {
-        if (hit) *out = j;
-        out += hit ? n : 0;
+    char* const lrow = reinterpret_cast<char*>(nlist + i);
+    const unsigned n4 = 4u * (unsigned)c.n;
+    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, nof, [&](bool hit, int j, float, int slot) {
+        if (hit) *list_slot(lrow, slot, n4) = j;
     });
     nlen[i] = k;
     int kb = 0;
     /* boundary cells only where bnear marks one within a cell (PHYSICS grid) */
     if (c.nb > 0 && (c.wrap || bnear == nullptr || bnear[base + cell_lin(c, cx, cy, cz)] != 0)) {
-        int* bout = sblist + i;
-        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, nof, [&](bool hit, int j, float) {
-            if (hit) *bout = j;
-            bout += hit ? n : 0;
+        char* const brow = reinterpret_cast<char*>(sblist + i);
+        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, nof, [&](bool hit, int j, float, int slot) {
+            if (hit) *list_slot(brow, slot, n4) = j;
         });
     }
     sblen[i] = kb;

@@ -96,17 +96,16 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     tab += base;
     btab += base;
     const float4 pi = spos[i];
-    const size_t n = (size_t)c.n;
     const float hh = c.h * c.h;
     const int row = REMAP ? __ldg(&remap[i]) : i;
     int cx, cy, cz;
     cell_of(c, pi.x, pi.y, pi.z, cx, cy, cz);
     float di = 0.f;
-    int* out = nlist + row;
+    char* const lrow = reinterpret_cast<char*>(nlist + row);
+    const unsigned n4 = 4u * (unsigned)c.n;
     const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, BATCH ? nullptr : noff,
-                             [&](bool hit, int j, float r2) {
-        if (hit) *out = REMAP ? __ldg(&remap[j]) : j;
-        out += hit ? n : 0;
+                             [&](bool hit, int j, float r2, int slot) {
+        if (hit) *list_slot(lrow, slot, n4) = REMAP ? __ldg(&remap[j]) : j;
         const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
         di += (t * t) * t;
     });
@@ -119,11 +118,10 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
      * (bnear, PHYSICS grid); every other particle's boundary list is empty */
     const bool scan_b = c.wrap || bnear == nullptr || bnear[base + cell_lin(c, cx, cy, cz)] != 0;
     if (c.nb > 0 && !REMAP && scan_b) {
-        int* bout = sblist + i;
+        char* const brow = reinterpret_cast<char*>(sblist + i);
         kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, BATCH ? nullptr : noff,
-                        [&](bool hit, int j, float r2) {
-            if (hit) *bout = j;
-            bout += hit ? n : 0;
+                        [&](bool hit, int j, float r2, int slot) {
+            if (hit) *list_slot(brow, slot, n4) = j;
             const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
             float w = 0.f;
             if (hit) w = __ldg(&bphi_s[j]);
