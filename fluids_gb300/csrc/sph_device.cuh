@@ -270,9 +270,10 @@ __device__ __forceinline__ int build_scan(const Const& c, float px, float py, fl
         }
         const int2 r = __ldg(&tab[id]);
         if (cnt + (r.y - r.x) <= c.cap) {
+            const float4* __restrict__ q = npos + r.x;
 #pragma unroll kBuildUnroll
-            for (int j = r.x; j < r.y; ++j) {
-                const float4 pj = __ldg(&npos[j]);
+            for (int j = r.x; j < r.y; ++j, ++q) {
+                const float4 pj = __ldg(q);
                 const float r2 = r2_exact(__fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
                 const bool hit = r2 < h2;
                 f(hit, j, r2, cnt);
