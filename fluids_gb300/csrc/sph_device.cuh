@@ -304,8 +304,9 @@ __device__ __forceinline__ int* list_slot(char* row, int k, unsigned n4) {
  * neighbour's data), so U entries and their positions are loaded before the U visits
  * run.  PIPE also loads the next U entries (the rows live in HBM: 200 bytes per particle)
  * before the current U visits, so their latency overlaps the visits: measured on GB300 it
- * speeds up the normal pass (0.310 -> 0.291 ms at 4M) and slows the force pass, whose
- * registers it pushes into spills (0.699 -> 0.761 ms).  The visits run in list order
+ * speeds up both walks that use it two entries deep: the normal pass 0.310 -> 0.291 ms at
+ * 4M four deep and 0.272 ms two deep (eight deep 0.471 ms at 66 registers), the force pass
+ * 0.699 -> 0.667 ms two deep (four deep its registers spill).  The visits run in list order
  * either way, so every sum keeps the list's order. */
 #ifndef SPH_LIST_UNROLL
 #define SPH_LIST_UNROLL 4
@@ -371,9 +372,9 @@ struct Neigh {
     const int* list;
     const int* len;
     const float4* npos;
-    template <bool PIPE = false, class F>
+    template <bool PIPE = false, int U = SPH_LIST_UNROLL, class F>
     __device__ __forceinline__ void visit(const Const& c, int i, float px, float py, float pz, F&& f) const {
-        if (LIST) list_neighbors<SPH_LIST_UNROLL, PIPE>(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
+        if (LIST) list_neighbors<U, PIPE>(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
         else scan_neighbors<EXACT>(c, px, py, pz, tab, npos, f);
     }
 };

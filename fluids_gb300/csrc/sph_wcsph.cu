@@ -159,7 +159,8 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
     const float4 pi = __ldg(&fl.npos[i]);
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
-    fl.template visit<true>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
+    /* two entries deep with the next two loaded during the visits (0.272 ms vs 0.291 four deep) */
+    fl.template visit<true, 2>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
         /* 1/rho_j from the dense density array (8 particles per 32-byte sector instead of 2
          * for aux; the pass is bound by L1 throughput); __frcp_rn is the correctly rounded
          * reciprocal, the value aux holds */
@@ -252,7 +253,9 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
     float pax = 0.f, pay = 0.f, paz = 0.f, vax = 0.f, vay = 0.f, vaz = 0.f;
     float cux = 0.f, cuy = 0.f, cuz = 0.f, cox = 0.f, coy = 0.f, coz = 0.f;
     const float rmin2 = c.rmin2_wc, two_rho0 = 2.0f * c.rho0;
-    fl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
+    /* list walk two entries deep with the next two entries loaded during the visits: 0.667 ms
+     * vs 0.699 ms for four deep without that prefetch (and vs spills at four deep with it) */
+    fl.template visit<true, 2>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
         const float r2 = dx * dx + dy * dy + dz * dz;
         /* loaded ahead of the guard so that the list loop can issue them early */
         float4 aj, vj, nj = make_float4(0.f, 0.f, 0.f, 0.f);
