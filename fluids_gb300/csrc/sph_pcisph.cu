@@ -122,8 +122,8 @@ __device__ __forceinline__ void pci_integrate_one(const Const& c, const Bufs& b,
 }
 
 /* update_pressure for one particle: predicted density from the fixed lists at x*.  The
- * list entries and the neighbours' x* are loaded four at a time before the four visits
- * (the sum keeps list order).  x* is written by this kernel, so it is read with plain loads.
+ * list is walked two entries deep with the next two entries loaded during the current two
+ * visits (the sum keeps list order).  x* is written by this kernel, so it is read with plain loads.
  * The updated pressure's p / rho^2 (the initial density, as compute_pressure_force uses it)
  * goes to pci_c for the force phase: the same IEEE quotient the force phase would form per
  * pair, formed once per particle. */
@@ -135,28 +135,32 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
     float pd = 0.f, pdb = 0.f;
     const int len = __ldg(&b.nlen[i]);
     const int* __restrict__ e = b.nlist + i;
-    int k = 0;
-#pragma unroll 1
-    for (; k + 4 <= len; k += 4, e += 4 * n) {
-        int j[4];
-        float4 q[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) j[u] = __ldg(e + u * n);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) q[u] = b.pos_pred[j[u]];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const float dx = pi.x - q[u].x, dy = pi.y - q[u].y, dz = pi.z - q[u].z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (COMPAT || r2 < HH) { const float t = HH - r2; pd += (t * t) * t; }
-        }
-    }
-    for (; k < len; ++k, e += n) {
-        const float4 pj = b.pos_pred[__ldg(e)];
+    auto visit = [&](float4 pj) {
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (COMPAT || r2 < HH) { const float t = HH - r2; pd += (t * t) * t; }
+    };
+    int k = 0;
+    if (len >= 2) {
+        /* two entries deep, the next two loaded during the current two visits */
+        int jn0 = __ldg(e), jn1 = __ldg(e + n);
+        e += 2 * n;
+#pragma unroll 1
+        for (;;) {
+            const float4 q0 = b.pos_pred[jn0], q1 = b.pos_pred[jn1];
+            k += 2;
+            const bool more = k + 2 <= len;
+            if (more) {
+                jn0 = __ldg(e);
+                jn1 = __ldg(e + n);
+                e += 2 * n;
+            }
+            visit(q0);
+            visit(q1);
+            if (!more) break;
+        }
     }
+    for (; k < len; ++k, e += n) visit(b.pos_pred[__ldg(e)]);
     pd *= c.default_eval * c.mass_def;
     const int blen = __ldg(&b.sblen[i]);
     for (int k = 0; k < blen; ++k) {
@@ -179,7 +183,7 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
 
 /* compute_pressure_force for one particle (initial density, updated pressure):
  * (p_i / rho_i^2 + p_j / rho_j^2) per pair with both quotients from pci_c (written by this
- * kernel's update phase, so plain loads); entries and positions four at a time. */
+ * kernel's update phase, so plain loads); walked two entries deep like the update phase. */
 __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Bufs& b, int i) {
     const float4 pi = __ldg(&b.pos_s[i]);
     const float H = c.h_def;
@@ -201,20 +205,25 @@ __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Buf
         }
     };
     int k = 0;
+    if (len >= 2) {
+        /* two entries deep, the next two loaded during the current two visits */
+        int jn0 = __ldg(e), jn1 = __ldg(e + n);
+        e += 2 * n;
 #pragma unroll 1
-    for (; k + 4 <= len; k += 4, e += 4 * n) {
-        int j[4];
-        float4 q[4];
-        float cj[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) j[u] = __ldg(e + u * n);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            q[u] = __ldg(&b.pos_s[j[u]]);
-            cj[u] = b.pci_c[j[u]];
+        for (;;) {
+            const float4 q0 = __ldg(&b.pos_s[jn0]), q1 = __ldg(&b.pos_s[jn1]);
+            const float c0 = b.pci_c[jn0], c1 = b.pci_c[jn1];
+            k += 2;
+            const bool more = k + 2 <= len;
+            if (more) {
+                jn0 = __ldg(e);
+                jn1 = __ldg(e + n);
+                e += 2 * n;
+            }
+            visit(q0, c0);
+            visit(q1, c1);
+            if (!more) break;
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) visit(q[u], cj[u]);
     }
     for (; k < len; ++k, e += n) {
         const int j = __ldg(e);
@@ -247,7 +256,7 @@ __global__ void __launch_bounds__(256) k_pci_init_density(Const c, Bufs b) {
     const float4 pi = __ldg(&b.pos_s[i]);
     const float H = c.h_def, HH = H * H;
     float di = 0.f, bdi = 0.f;
-    list_neighbors(i, c.n, b.nlist, __ldg(&b.nlen[i]), b.pos_s, pi.x, pi.y, pi.z,
+    list_neighbors<2, true>(i, c.n, b.nlist, __ldg(&b.nlen[i]), b.pos_s, pi.x, pi.y, pi.z,
                    [&](int, float4, float dx, float dy, float dz) {
                        const float t = HH - (dx * dx + dy * dy + dz * dz);
                        di += (t * t) * t;
