@@ -400,6 +400,13 @@ __device__ __forceinline__ float st_kernel(float r, float h, float c) {
     }
     return 0.0f;
 }
+/* st_kernel with selects instead of branches (same arithmetic, same values). */
+__device__ __forceinline__ float st_kernel_sel(float r, float h, float c) {
+    const float t1 = h - r;
+    const float t2 = (t1 * t1 * t1) * (r * r * r);
+    const float inner = 2.0f * t2 - c;
+    return r <= 0.5f * h ? inner : (r <= h ? t2 : 0.0f);
+}
 /* OpenCL clamp = fmin(fmax(x, lo), hi) and sign(). */
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 __device__ __forceinline__ float signf(float x) {

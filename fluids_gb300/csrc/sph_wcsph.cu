@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
                 cux += (ni.x - nj.x) * K;
                 cuy += (ni.y - nj.y) * K;
                 cuz += (ni.z - nj.z) * K;
-                const float ck = st_kernel(rn, h, c.st_term) * K * irn;
+                const float ck = st_kernel_sel(rn, h, c.st_term) * K * irn;
                 cox += dx * ck;
                 coy += dy * ck;
                 coz += dz * ck;
