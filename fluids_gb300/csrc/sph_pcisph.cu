@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {
                        ux += (ni.x - nj.x) * K;
                        uy += (ni.y - nj.y) * K;
                        uz += (ni.z - nj.z) * K;
-                       const float sk = st_kernel(rn, H, c.st_term);
+                       const float sk = st_kernel_sel(rn, H, c.st_term);
                        ox += ((dx * inv) * sk) * K;
                        oy += ((dy * inv) * sk) * K;
                        oz += ((dz * inv) * sk) * K;
