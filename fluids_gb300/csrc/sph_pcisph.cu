@@ -138,7 +138,9 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
     auto visit = [&](float4 pj) {
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (COMPAT || r2 < HH) { const float t = HH - r2; pd += (t * t) * t; }
+        /* the range test as a select: a rejected pair adds +0 */
+        const float t = (COMPAT || r2 < HH) ? HH - r2 : 0.f;
+        pd += (t * t) * t;
     };
     int k = 0;
     if (len >= 2) {
@@ -195,14 +197,15 @@ __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Buf
     auto visit = [&](float4 pj, float cj) {
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const float il = rsqrtf(r2), l = r2 * il;
-        if (l >= 1e-5f) {
-            const float q = C + cj;
-            const float t = (H - l) * (H - l);
-            fx += q * ((dx * il) * t);
-            fy += q * ((dy * il) * t);
-            fz += q * ((dz * il) * t);
-        }
+        const float il0 = rsqrtf(r2), l0 = r2 * il0;
+        /* the distance guard as selects: a rejected pair (the particle itself) adds zeros */
+        const bool ok = l0 >= 1e-5f;
+        const float il = ok ? il0 : 0.f, l = ok ? l0 : H;
+        const float q = C + cj;
+        const float t = (H - l) * (H - l);
+        fx += q * ((dx * il) * t);
+        fy += q * ((dy * il) * t);
+        fz += q * ((dz * il) * t);
     };
     int k = 0;
     if (len >= 2) {
