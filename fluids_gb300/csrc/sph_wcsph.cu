@@ -235,19 +235,6 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
     const float4 ai = __ldg(&b.aux[i]);
     const float C = ai.x, di = ai.z;
     const float h = c.h, sg = c.spiky_grad;
-    float bax = 0.f, bay = 0.f, baz = 0.f;
-    if (c.nb > 0) {
-        const float c2 = 2.0f * C * sg;
-        bl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const float irn = rsqrtf(r2);
-            const float w = h - r2 * irn;
-            const float k = -__ldg(&b.bphi_s[j]) * (irn * (w * w)) * c2;
-            bax += dx * k;
-            bay += dy * k;
-            baz += dz * k;
-        });
-    }
     float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ST) ni = __ldg(&b.normal[i]);
     float pax = 0.f, pay = 0.f, paz = 0.f, vax = 0.f, vay = 0.f, vaz = 0.f;
@@ -293,6 +280,21 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
             }
         }
     });
+    /* the boundary pairs after the fluid pairs, so that their sums are not live during the
+     * fluid walk (each term keeps its own accumulator, so the result is the same) */
+    float bax = 0.f, bay = 0.f, baz = 0.f;
+    if (c.nb > 0) {
+        const float c2 = 2.0f * C * sg;
+        bl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float irn = rsqrtf(r2);
+            const float w = h - r2 * irn;
+            const float k = -__ldg(&b.bphi_s[j]) * (irn * (w * w)) * c2;
+            bax += dx * k;
+            bay += dy * k;
+            baz += dz * k;
+        });
+    }
     const float m = c.mass;
     pax *= -m; pay *= -m; paz *= -m;
     const float vs = COMPAT ? (c.visc_lapl * c.mu) : (c.visc_lapl * c.mu) * (m * ai.y);
