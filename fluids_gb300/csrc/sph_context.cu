@@ -440,11 +440,17 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
         sph::launch_wc_forces(s, c, b, lists, true, false, bs, pack);
         mark(x, "k_wc_forces");
     } else {
-        sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
-                                b.scenes, b.scene_of, b.bnear, b.noff);
-        mark(x, "k_neigh_lists");
-        sph::launch_pci_init_density(s, c, b, bs);
-        mark(x, "k_pci_init_density");
+        if (!c.compat && !c.batched) {
+            /* the lists and the initial density in one pass */
+            sph::launch_lists_density_pci(s, c, b, bs);
+            mark(x, "k_lists_density");
+        } else {
+            sph::launch_neigh_lists(s, c, b.pos_s, b.tab, b.bpos_s, b.btab, b.nlist, b.nlen, b.sblist, b.sblen, bs,
+                                    b.scenes, b.scene_of, b.bnear, b.noff);
+            mark(x, "k_neigh_lists");
+            sph::launch_pci_init_density(s, c, b, bs);
+            mark(x, "k_pci_init_density");
+        }
         /* with surface tension the normal pass also writes the packed per-neighbour records
          * (velocity, normal, 1/rho) that the force pass reads */
         const bool pack = c.sigma != 0.f;

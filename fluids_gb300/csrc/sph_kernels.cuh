@@ -95,6 +95,8 @@ void launch_wc_forces(cudaStream_t s, const Const& c, const Bufs& b, bool lists,
                       bool write_acc, int bs, bool pack = false);
 void launch_wc_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs);
 void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+/* PHYSICS PCISPH: the neighbour lists and compute_initial_density in one pass */
+void launch_lists_density_pci(cudaStream_t s, const Const& c, const Bufs& b, int bs);
 void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs);
 /* the list builder writing rows, entries and densities in id order (remap = sorted -> id) */
 void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, const int32_t* remap, int bs);

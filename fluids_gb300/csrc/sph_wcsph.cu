@@ -74,7 +74,11 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
 /* REMAP (the adjoint's tape, which keeps particles in id order): the list of sorted particle
  * i is written as row remap[i] with entries remap[j], and its density, pressure and aux go to
  * remap[i]; the visits, their order and the arithmetic are those of the plain builder. */
-template <bool COMPAT, bool BATCH, bool REMAP = false>
+/* PCI (PHYSICS PCISPH): the fused density is compute_initial_density (pcisph.cl:33-102) over
+ * the same pairs instead -- rho = w (m_def sum W + sum Psi W) with h_def and the PCISPH
+ * normaliser, pressure 0 (pcisphsimluation.cpp:118), aux = (0, 1/rho, rho, 0) -- so the
+ * PCISPH step needs no separate initial-density pass. */
+template <bool COMPAT, bool BATCH, bool REMAP = false, bool PCI = false>
 __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Const c0, const float4* __restrict__ spos,
                                                        const int2* __restrict__ tab,
                                                        const float4* __restrict__ bpos_s,
@@ -96,7 +100,7 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     tab += base;
     btab += base;
     const float4 pi = spos[i];
-    const float hh = c.h * c.h;
+    const float hh = PCI ? c.h_def * c.h_def : c.h * c.h;
     const int row = REMAP ? __ldg(&remap[i]) : i;
     int cx, cy, cz;
     cell_of(c, pi.x, pi.y, pi.z, cx, cy, cz);
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     });
     nlen[row] = k;
     if (k >= c.cap && REMAP) atomicOr(flags, kFlagOverflow);
-    di *= c.poly6_eval * c.mass;
+    if (!PCI) di *= c.poly6_eval * c.mass;
     int kb = 0;
     float bdi = 0.f;
     /* the boundary scan only where a boundary particle is binned in one of the 27 cells
@@ -129,6 +133,13 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
         });
     }
     if (!REMAP) sblen[i] = kb;
+    if (PCI) {
+        const float d = c.default_eval * ((di * c.mass_def) + bdi);
+        dens[row] = d;
+        pres[row] = 0.f;
+        aux[row] = make_float4(0.f, 1.0f / d, d, 0.f);
+        return;
+    }
     di += c.poly6_eval * bdi;
     dens[row] = di;
     const float pv = c.kgas * (pown7(di / c.rho0) - 1.0f);
@@ -382,6 +393,12 @@ static void lists_density_launch(cudaStream_t s, const Const& c, const Bufs& b, 
                                                                 nullptr, b.bnear, b.noff);
 }
 
+void launch_lists_density_pci(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    k_lists_density<false, false, false, true><<<nblk(c.n, bs), bs, 0, s>>>(
+        c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist, b.nlen, b.sblist, b.sblen, b.density, b.pressure,
+        b.aux, b.scenes, b.scene_of, nullptr, nullptr, b.bnear, b.noff);
+}
 void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, const int32_t* remap, int bs) {
     if (c.n <= 0) return;
     k_lists_density<false, false, true><<<nblk(c.n, bs), bs, 0, s>>>(
