@@ -246,6 +246,21 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
     const float4 ai = __ldg(&b.aux[i]);
     const float C = ai.x, di = ai.z;
     const float h = c.h, sg = c.spiky_grad;
+    float bax = 0.f, bay = 0.f, baz = 0.f;
+    auto boundary_pairs = [&]() {
+        if (c.nb <= 0) return;
+        const float c2 = 2.0f * C * sg;
+        bl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float irn = rsqrtf(r2);
+            const float w = h - r2 * irn;
+            const float k = -__ldg(&b.bphi_s[j]) * (irn * (w * w)) * c2;
+            bax += dx * k;
+            bay += dy * k;
+            baz += dz * k;
+        });
+    };
+    if (BATCH) boundary_pairs();
     float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ST) ni = __ldg(&b.normal[i]);
     float pax = 0.f, pay = 0.f, paz = 0.f, vax = 0.f, vay = 0.f, vaz = 0.f;
@@ -284,28 +299,18 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
                 cux += (ni.x - nj.x) * K;
                 cuy += (ni.y - nj.y) * K;
                 cuz += (ni.z - nj.z) * K;
-                const float ck = st_kernel_sel(rn, h, c.st_term) * K * irn;
+                /* selects in the single-scene kernel (0.666 -> 0.636 ms), branches in the batched one */
+                const float ck = (BATCH ? st_kernel(rn, h, c.st_term) : st_kernel_sel(rn, h, c.st_term)) * K * irn;
                 cox += dx * ck;
                 coy += dy * ck;
                 coz += dz * ck;
             }
         }
     });
-    /* the boundary pairs after the fluid pairs, so that their sums are not live during the
-     * fluid walk (each term keeps its own accumulator, so the result is the same) */
-    float bax = 0.f, bay = 0.f, baz = 0.f;
-    if (c.nb > 0) {
-        const float c2 = 2.0f * C * sg;
-        bl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const float irn = rsqrtf(r2);
-            const float w = h - r2 * irn;
-            const float k = -__ldg(&b.bphi_s[j]) * (irn * (w * w)) * c2;
-            bax += dx * k;
-            bay += dy * k;
-            baz += dz * k;
-        });
-    }
+    /* single scene: the boundary pairs after the fluid pairs, so that their sums are not live
+     * during the fluid walk (each term keeps its own accumulator, so the result is the same);
+     * the batched kernel measured faster with them first (2.46 vs 2.59 ms per batched step) */
+    if (!BATCH) boundary_pairs();
     const float m = c.mass;
     pax *= -m; pay *= -m; paz *= -m;
     const float vs = COMPAT ? (c.visc_lapl * c.mu) : (c.visc_lapl * c.mu) * (m * ai.y);
