@@ -140,6 +140,21 @@ def test_workload_sizes():
     assert workloads.tait_stiffness(20.0) == pytest.approx(57142.857, rel=1e-6)
 
 
+def test_pcisph_4m_workload_is_the_wcsph_scene_stepped_by_pcisph():
+    """The 4M PCISPH line steps the WCSPH double dam break's particles and walls with the
+    PCISPH settings of the 358k configuration, dt scaled by the spacing ratio."""
+    pw = workloads.pcisph_double_dam_4m(n=16)
+    ww = workloads.double_dam_4m(n=16)
+    assert np.array_equal(pw["fluid"], ww["fluid"]) and len(pw["fluid"]) == 2 * 16 ** 3
+    assert np.array_equal(pw["bodies"][0][0], ww["bodies"][0][0])
+    p, q = pw["params"], workloads.pcisph_cube()["params"]
+    assert p.method == capi.SPH_PCISPH and p.time_step == pytest.approx(5e-4 * 0.005 / 0.0125)
+    assert p.particle_radius == pytest.approx(0.0025) and p.support_radius == pytest.approx(0.01)
+    for f in ("pcisph_min_iterations", "pcisph_max_iterations", "pcisph_error_ratio", "k_viscosity",
+              "surface_tension", "rest_density", "max_vel"):
+        assert getattr(p, f) == pytest.approx(getattr(q, f)), f
+
+
 def test_create_without_gpu_fails_cleanly():
     if capi.cuda_available():
         pytest.skip("a GPU is visible")
