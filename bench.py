@@ -37,7 +37,7 @@ FALLBACK_HBM_GBS = 6800.0
 # Algorithmic HBM bytes per fluid particle of each kernel (compulsory traffic; neighbour data
 # is assumed to come from L1/L2).  The list-based kernels also move their neighbour lists:
 # LIST_BYTES[k] = (bytes per fluid-list entry, bytes per boundary-list entry, fixed bytes),
-# multiplied by the step's mean list lengths.  The derivation is tabulated in the design doc.
+# multiplied by the step's mean list lengths.
 ALG_BYTES = {
     "k_hashes": 16 + 4 + 4 + 4 + 8,          # pos in; key, mask out; cell_prev in; clear 8 B/cell (upper bound)
     "k_gather": 4 + 3 * 16 * 2 + 4 * 2,      # perm; pos/vel/vhalf gathered and written; ids

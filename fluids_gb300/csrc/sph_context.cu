@@ -6,7 +6,7 @@
  *     429-469 (PCISPH delta), mullerconstants.cpp:4-38, boundaryhandler.cpp:144,306-309,
  *     grid.cpp:61-68, and the 6-decimal -D rounding of opencl/clcompiler.cpp:50-54;
  *   - memory: one device arena per context holding every SoA array (replaces CLAllocator,
- *     opencl/clallocator.h); sizes in the design doc;
+ *     opencl/clallocator.h), carved by carve() below;
  *   - the step: WCSPHSimulation::simulate (wcsphsimluation.cpp:40-106) and
  *     PCISPHSimulation::_simulate_pcisph_step (pcisphsimluation.cpp:72-165) as one sequence
  *     of launches on the context stream, captured once into a CUDA graph and replayed;

@@ -11,7 +11,7 @@
  *                 staging or barrier needed on this hardware).
  *   k_neigh_lists compute_neigh_list (kernels/grid.cl:145-182) for the fluid and the boundary
  *                 tables in one launch, column-major list[k * n + i].
- * All are HBM-streaming kernels (bytes per particle listed in the design doc).
+ * All are HBM-streaming kernels.
  */
 #include "sph_kernels.cuh"
 

@@ -16,8 +16,10 @@
  *      so that consecutive threads write consecutive addresses of a digit bucket.
  * Traffic per pass: 8 B read + 8 B written per pair.
  * Every look-back wait is bounded: after kSpinLimit polls the CTA sets SPH_FLAG_TIMEOUT in
- * the status word, treats the missing count as 0 and finishes (the result is then wrong
- * and the host reports SPH_E_TIMEOUT); with in-order tile ids the wait always ends.
+ * the flag word, treats the missing count as 0 and finishes (the result is then wrong);
+ * with in-order tile ids the wait always ends.  A context's step sorts into the context's
+ * flag word, which sph_device_flags reads (SPH_FLAG_TIMEOUT); the standalone entry points
+ * sph_sort_pairs and sph_sort_pairs_noalloc do not read their flag word back.
  */
 #include "sph_kernels.cuh"
 

@@ -24,7 +24,15 @@
  *     the parts that must start at zero are cleared at the start of each call, but two
  *     calls whose work overlaps on the GPU (different streams, or different host threads)
  *     race on it: serialise them;
- *   - asynchronous on the given stream; no cudaMalloc, cudaFree or allocating library call.
+ *   - asynchronous on the given stream; no cudaMalloc, cudaFree or allocating library call;
+ *   - the array's address is looked up once per device and kept; it does not survive
+ *     cudaDeviceReset (which unloads the module), so a host that resets a device must not
+ *     call this entry point on it again; a failed launch forgets the address, and the next
+ *     call looks it up again;
+ *   - the error check after the launches (cudaGetLastError) also returns, and clears, an
+ *     error that earlier asynchronous work on the calling thread left behind;
+ *   - a look-back wait that gives up (it cannot on a correct launch: tiles are taken in
+ *     order) leaves a wrong result and is not reported by the return code.
  * The kernels are the ones of sph_sort.cu (block size 256); the passes ping-pong between
  * the caller's output and the array's copy so that the input is only read.
  */
@@ -85,6 +93,15 @@ int scratch_for_current_device(unsigned char** base, int* sms) {
     return SPH_OK;
 }
 
+/* After a failed launch the context may have been lost and the module reloaded: look the
+ * address up again on the next call. */
+void forget_scratch_for_current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_base[dev] = nullptr;
+}
+
 bool overlaps(const void* a, size_t na, const void* b, size_t nb) {
     const char* x = static_cast<const char*>(a);
     const char* y = static_cast<const char*>(b);
@@ -99,7 +116,10 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* d_keys_in, const int32_t* 
     if (n == 0) return SPH_OK;
     if (!d_keys_in || !d_vals_in || !d_keys_out || !d_vals_out) return SPH_E_INVALID;
     const size_t bytes = (size_t)4 * n;
+    /* an output may overlap neither input (with an odd pass count the first pass writes the
+     * outputs while it still reads the inputs) nor the other output */
     if (overlaps(d_keys_in, bytes, d_keys_out, bytes) || overlaps(d_vals_in, bytes, d_vals_out, bytes) ||
+        overlaps(d_keys_in, bytes, d_vals_out, bytes) || overlaps(d_vals_in, bytes, d_keys_out, bytes) ||
         overlaps(d_keys_out, bytes, d_vals_out, bytes))
         return SPH_E_INVALID;
     unsigned char* base = nullptr;
@@ -144,6 +164,9 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* d_keys_in, const int32_t* 
         ki = ko;
         vi = vo;
     }
-    if (cudaGetLastError() != cudaSuccess) return SPH_E_CUDA;
+    if (cudaGetLastError() != cudaSuccess) {
+        forget_scratch_for_current_device();
+        return SPH_E_CUDA;
+    }
     return SPH_OK;
 }

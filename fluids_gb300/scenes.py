@@ -4,7 +4,7 @@
 ``Sphere.surface_sampling`` and ``Model.surface_sampling`` call the C-ABI samplers that restate
 fluid/simulation/boxvolume.cpp:11-40, scene/fishtank.cpp:108-141, scene/cube.cpp:136-171,
 scene/sphere.cpp:135-171 and scene/model.cpp:170-214 (the last on the GPU).  ``jitter`` is the seeded splitmix64 jitter of the benchmark
-scenes.  The BASELINE-style scenes (dam breaks, the rotated cube) are built by ``make_scene``.
+scenes.  The benchmark scenes (dam breaks, the rotated cube) are built by ``make_scene``.
 """
 import math
 

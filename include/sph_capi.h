@@ -408,8 +408,11 @@ int sph_sort_pairs(uint32_t* d_keys, int32_t* d_vals, int n, int key_bits, void*
  * device array of 9,441,792 bytes per GPU, held until the process exits.  At most
  * SPH_NOALLOC_SORT_MAX_PAIRS pairs (SPH_E_OVERFLOW above that, nothing launched).  The
  * first call on a device looks up the array's address, so make it before any stream
- * capture.  All calls on a device share the array: calls that overlap on the GPU race, so
- * serialise them.  Asynchronous on cuda_stream. */
+ * capture; the address is kept and does not survive cudaDeviceReset (do not call this
+ * again on a device that was reset).  All calls on a device share the array: calls that
+ * overlap on the GPU race, so serialise them.  No output may overlap an input or the other
+ * output (SPH_E_INVALID).  Asynchronous on cuda_stream; its closing cudaGetLastError also
+ * returns and clears an error left by earlier work on the calling thread. */
 #define SPH_NOALLOC_SORT_MAX_PAIRS 1048576
 int sph_sort_pairs_noalloc(const uint32_t* d_keys_in, const int32_t* d_vals_in, uint32_t* d_keys_out,
                            int32_t* d_vals_out, int n, int key_bits, void* cuda_stream);

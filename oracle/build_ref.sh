@@ -9,10 +9,16 @@
 # The one source transformation rewrites OpenCL vector literals "(int4)(" / "(float4)("
 # into function calls, on copies written under oracle/_ref/src (never committed).
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#        oracle/build_ref.sh --root      (prints the reference root it would use)
+# The root is the argument, else $FLUIDS_REFERENCE_ROOT, else the container's mount point.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+if [ "${1:-}" = "--root" ]; then
+    echo "${FLUIDS_REFERENCE_ROOT:-/root/reference}"
+    exit 0
+fi
+ref="${1:-${FLUIDS_REFERENCE_ROOT:-/root/reference}}"
 out="$here/_ref"
 have_ref=0
 if [ -d "$ref/kernels" ]; then

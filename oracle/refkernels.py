@@ -9,8 +9,17 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_ref", "libref_kernels.so")
-REFERENCE_ROOT = "/root/reference"
 _lib = None
+
+
+def reference_root():
+    """Where the reference sources are mounted: the root build_ref.sh resolves (its argument
+    default, or $FLUIDS_REFERENCE_ROOT)."""
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "--root"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+REFERENCE_ROOT = reference_root()
 
 
 SRC_COPIES = os.path.join(HERE, "_ref", "src", "grid.cl")

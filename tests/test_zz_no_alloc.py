@@ -65,7 +65,11 @@ def test_noalloc_sort_rejects_what_it_cannot_do(gpu_lib):
     assert L.sph_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), ko.data_ptr(), vo.data_ptr(), MAX_PAIRS + 1, 32,
                                     None) == 7
     assert L.sph_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), ko.data_ptr(), vo.data_ptr(), 8, 0, None) == 1
-    # output aliasing the input
+    # an output aliasing an input, its own or the other one (with 8-bit keys the single pass
+    # would write the outputs while still reading the inputs), or the other output
     assert L.sph_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), k.data_ptr(), vo.data_ptr(), 8, 32, None) == 1
+    assert L.sph_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), ko.data_ptr(), k.data_ptr(), 8, 8, None) == 1
+    assert L.sph_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), v.data_ptr(), vo.data_ptr(), 8, 8, None) == 1
+    assert L.sph_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), ko.data_ptr(), ko.data_ptr(), 8, 8, None) == 1
     assert L.sph_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), ko.data_ptr(), vo.data_ptr(), 0, 32, None) == 0
     torch.cuda.synchronize()
