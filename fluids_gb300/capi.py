@@ -27,7 +27,8 @@ STATUS = {0: "SPH_OK", 1: "SPH_E_INVALID", 2: "SPH_E_CUDA", 3: "SPH_E_NONCONVERG
  SPH_E_STATE, SPH_E_NOMEM) = range(10)
 STAGES = dict(BOUNDARY_SYNC=0, HASHES=1, SORT=2, SHUFFLE=3, CELL_INTERVALS=4, NEIGH_LIST=5, SB_NEIGH_LIST=6,
               WC_DENSITY=7, NORMALS=8, WC_ACCEL=9, WC_INTEGRATE=10, PCI_INIT_DENSITY=11, PCI_INIT_FORCES=12,
-              PCI_LOOP=13, PCI_INTEGRATE=14, BOUNDARY_FORCES=15)
+              PCI_LOOP=13, PCI_INTEGRATE=14, BOUNDARY_FORCES=15, PCI_PREDICT=16, PCI_UPDATE_PRESSURE=17,
+              PCI_PRESSURE_FORCE=18)
 FIELDS = dict(POS=0, VEL=1, VEL_HALF=2, POS_SORTED=3, VEL_SORTED=4, VEL_HALF_SORTED=5, HASHES=6, MASK=7,
               CELL_INTERVALS=8, NEIGH_LIST=9, NEIGH_LEN=10, SB_NEIGH_LIST=11, SB_NEIGH_LEN=12, DENSITY=13,
               PRESSURE=14, NORMAL=15, ACCEL=16, POS_PRED=17, FORCE_OTHER=18, FORCE_PRESSURE=19, DENS_VAR=20,

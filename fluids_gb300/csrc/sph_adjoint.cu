@@ -171,10 +171,11 @@ __global__ void __launch_bounds__(256) k_adj_forces_bwd(Const c, int n, const fl
     if (rho > 0.f) {
         const float q = rho / c.rho0;
         const float q6 = ((((q * q) * q) * q) * q) * q;
-        const float pv = c.kgas * (q6 * q - 1.0f);
+        const float q7m1 = pown7(q) - 1.0f;   /* the forward pass's EOS, same rounding */
+        const float pv = c.kgas * q7m1;
         const bool act = pv > 0.f;
         const float dp = act ? 7.0f * c.kgas * q6 / c.rho0 : 0.f;
-        const float dpk = act ? (q6 * q - 1.0f) : 0.f;
+        const float dpk = act ? q7m1 : 0.f;
         const float ir2 = 1.0f / (rho * rho);
         lr = lC * (dp * ir2 - 2.0f * p * ir2 / rho) - lR * ir2;
         gki = lC * dpk * ir2;

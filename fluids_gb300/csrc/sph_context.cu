@@ -377,6 +377,14 @@ int run_stage_impl(sph_ctx* x, int stage) {
         if (x->any_massive) sph::launch_bnd_forces(s, c, b, (int)x->bodies.size(), bs);
         if (x->any_dynamic) sph::launch_body_integrate(s, c, b, (int)x->bodies.size());
         break;
+    case SPH_S_PCI_PREDICT:
+    case SPH_S_PCI_UPDATE_PRESSURE:
+    case SPH_S_PCI_PRESSURE_FORCE:
+        if (x->p.method != SPH_PCISPH) return fail(x, SPH_E_INVALID, "PCISPH stage on a non-PCISPH context");
+        if (stage == SPH_S_PCI_PREDICT) sph::launch_pci_predict(s, c, b, bs);
+        else if (stage == SPH_S_PCI_UPDATE_PRESSURE) sph::launch_pci_update_pressure(s, c, b, bs);
+        else sph::launch_pci_pressure_force(s, c, b, bs);
+        break;
     default:
         return fail(x, SPH_E_INVALID, "unknown stage id");
     }

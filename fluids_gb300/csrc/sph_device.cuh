@@ -382,9 +382,12 @@ struct Neigh {
 /* pown(x, n) restated as left-to-right repeated multiplication. */
 __device__ __forceinline__ float pown2(float x) { return x * x; }
 __device__ __forceinline__ float pown3(float x) { return (x * x) * x; }
+/* Rounded products (__fmul_rn): the equation of state subtracts 1 from the power, and a
+ * contracted last multiply (one FMA with the -1) would round once where the kernel text
+ * rounds twice, so the pressure would not be the EOS of the density bit for bit. */
 __device__ __forceinline__ float pown7(float x) {
-    float r = x * x;
-    r = r * x; r = r * x; r = r * x; r = r * x; r = r * x;
+    float r = __fmul_rn(x, x);
+    r = __fmul_rn(r, x); r = __fmul_rn(r, x); r = __fmul_rn(r, x); r = __fmul_rn(r, x); r = __fmul_rn(r, x);
     return r;
 }
 /* kernels/surface_tension.h:23-50 */

@@ -108,6 +108,9 @@ int pci_loop_blocks(int num_sms, int bs);
 cudaError_t launch_pci_loop(cudaStream_t s, const Const& c, const Bufs& b, int min_iter, int max_iter, int blocks,
                             int bs, bool fuse_integrate);
 void launch_pci_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+void launch_pci_predict(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+void launch_pci_update_pressure(cudaStream_t s, const Const& c, const Bufs& b, int bs);
+void launch_pci_pressure_force(cudaStream_t s, const Const& c, const Bufs& b, int bs);
 
 /* sph_boundary.cu */
 void launch_bnd_transform(cudaStream_t s, const Bufs& b, int nbodies, int nb, bool compat, bool only_movable,

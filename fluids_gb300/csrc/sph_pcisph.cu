@@ -374,7 +374,49 @@ __global__ void __launch_bounds__(256) k_pci_integrate(Const c, Bufs b) {
     pci_integrate_one(c, b, i);
 }
 
+/* The loop's three passes as separate launches, for stage-by-stage parity on fields set
+ * from outside: the same per-particle functions as k_pci_loop. */
+__global__ void __launch_bounds__(256) k_pci_predict(Const c, Bufs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c.n) pci_predict_one(c, b, i);
+}
+
+template <bool COMPAT>
+__global__ void __launch_bounds__(256) k_pci_update_pressure(Const c, Bufs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c.n) pci_update_one<COMPAT>(c, b, i);
+}
+
+/* p / rho^2 of every particle from the pressure and density fields as they stand (the
+ * update pass forms it as a by-product in the loop). */
+__global__ void __launch_bounds__(256) k_pci_quotient(Const c, Bufs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const float di = b.density[i];
+    b.pci_c[i] = b.pressure[i] / (di * di);
+}
+
+__global__ void __launch_bounds__(256) k_pci_pressure_force(Const c, Bufs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c.n) pci_pressure_force_one(c, b, i);
+}
+
 static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
+
+void launch_pci_predict(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    k_pci_predict<<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+}
+void launch_pci_update_pressure(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    if (c.compat) k_pci_update_pressure<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+    else k_pci_update_pressure<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+}
+void launch_pci_pressure_force(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
+    if (c.n <= 0) return;
+    k_pci_quotient<<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+    k_pci_pressure_force<<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+}
 
 void launch_pci_init_density(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     if (c.n <= 0) return;

@@ -127,7 +127,13 @@ enum sph_stage {
     SPH_S_PCI_INIT_FORCES = 12, /* fill F_p = 0 + compute_initial_forces (pcisph.cl:134-222) */
     SPH_S_PCI_LOOP = 13,        /* predict/update/force loop + clmax (pcisphsimluation.cpp:129-148) */
     SPH_S_PCI_INTEGRATE = 14,   /* predict_vel_n_pos (pcisph.cl:240-284) */
-    SPH_S_BOUNDARY_FORCES = 15  /* BoundaryHandler::apply_fluid_forces (boundaryhandler.cpp:296-349) */
+    SPH_S_BOUNDARY_FORCES = 15, /* BoundaryHandler::apply_fluid_forces (boundaryhandler.cpp:296-349) */
+    /* the three passes of one PCISPH loop iteration, each alone on the fields as they are
+     * (PCISPH contexts only): */
+    SPH_S_PCI_PREDICT = 16,     /* predict_pos (pcisph.cl:302-344): POS_PRED */
+    SPH_S_PCI_UPDATE_PRESSURE = 17, /* update_pressure (pcisph.cl:349-418): DENS_VAR, PRESSURE += */
+    SPH_S_PCI_PRESSURE_FORCE = 18   /* compute_pressure_force (pcisph.cl:420-504): FORCE_PRESSURE
+                                       from POS_SORTED, DENSITY, PRESSURE */
 };
 
 /* ---- parameters and lifetime ------------------------------------------------------ */

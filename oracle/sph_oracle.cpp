@@ -918,6 +918,10 @@ struct Oracle : OracleBase {
         case ORC_S_PCI_LOOP: pci_loop(cfg.pci_min_iter, cfg.pci_max_iter); break;
         case ORC_S_PCI_INTEGRATE: pci_integrate(); break;
         case ORC_S_BOUNDARY_FORCES: boundary_forces(); integrate_bodies(); break;
+        /* one iteration's passes alone (pcisph.cl:302-344, :349-418, :420-504) */
+        case ORC_S_PCI_PREDICT: pci_predict(); break;
+        case ORC_S_PCI_UPDATE_PRESSURE: pci_update_pressure(); break;
+        case ORC_S_PCI_PRESSURE_FORCE: pci_pressure_force(); break;
         default: return 1;
         }
         return 0;

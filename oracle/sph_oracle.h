@@ -55,7 +55,8 @@ enum {
     ORC_S_CELL_INTERVALS = 4, ORC_S_NEIGH_LIST = 5, ORC_S_SB_NEIGH_LIST = 6,
     ORC_S_WC_DENSITY = 7, ORC_S_NORMALS = 8, ORC_S_WC_ACCEL = 9, ORC_S_WC_INTEGRATE = 10,
     ORC_S_PCI_INIT_DENSITY = 11, ORC_S_PCI_INIT_FORCES = 12, ORC_S_PCI_LOOP = 13,
-    ORC_S_PCI_INTEGRATE = 14, ORC_S_BOUNDARY_FORCES = 15
+    ORC_S_PCI_INTEGRATE = 14, ORC_S_BOUNDARY_FORCES = 15,
+    ORC_S_PCI_PREDICT = 16, ORC_S_PCI_UPDATE_PRESSURE = 17, ORC_S_PCI_PRESSURE_FORCE = 18
 };
 
 enum {

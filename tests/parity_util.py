@@ -43,3 +43,14 @@ def make_pair(params, fluid, bodies, container, precision=0, vel=None):
     ctx.add_volume(fluid, vel)
     orc.set_fluid(fluid, vel)
     return ctx, orc
+
+
+def tait(density, params):
+    """compute_density_pressure's equation of state (kernels/wcsph.cl:32-79) in FP32 with
+    pown as left-to-right multiplication: p = max(0, k ((rho / rho0)^7 - 1))."""
+    with np.errstate(over="ignore", invalid="ignore"):
+        q = np.asarray(density, np.float32) / np.float32(params.rest_density)
+        pw = q.copy()
+        for _ in range(6):
+            pw = pw * q
+        return np.maximum(np.float32(0), np.float32(params.gas_stiffness) * (pw - np.float32(1)))

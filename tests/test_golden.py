@@ -142,6 +142,19 @@ def run_pcisph(kind):
     s.stage("PCI_INTEGRATE")
     check_field(kind, "pos", s.get("POS").reshape(-1, 4), g["pos_out"], 4)
     check_field(kind, "vel", s.get("VEL").reshape(-1, 4), g["vel_out"], 4, rtol=1e-4)
+    # The loop's last passes alone, on the reference's own inputs to them: update_pressure
+    # (pcisph.cl:349-418) on the final predicted positions gives the final density error,
+    # and compute_pressure_force (pcisph.cl:420-504) on the final pressure and the initial
+    # density gives the final pressure force, each within the 1e-5 bar.  The looser bar on
+    # the loop's outputs above is the iterations' accumulation, not these kernels.
+    s.set("POS_PRED", g["pos_pred"])
+    s.stage("PCI_UPDATE_PRESSURE")
+    check_field(kind, "dens_var (last update alone)", s.get("DENS_VAR"), g["dens_var"], scale=1000.0)
+    s.set("PRESSURE", g["pressure"])
+    s.set("DENSITY", g["density"])
+    s.stage("PCI_PRESSURE_FORCE")
+    check_field(kind, "force_pressure (last pass alone)", s.get("FORCE_PRESSURE").reshape(-1, 4),
+                g["force_pressure"], 4)
 
 
 def test_oracle_reproduces_golden_wcsph():

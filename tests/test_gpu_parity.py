@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from fluids_gb300 import capi
-from parity_util import assert_close, make_pair
+from parity_util import assert_close, make_pair, tait
 from scenes_np import small_scene
 
 pytestmark = pytest.mark.gpu
@@ -86,6 +86,10 @@ def test_wcsph_stages_match_oracle(gpu_lib, mode, lists):
         ctx.stage("WC_DENSITY")
         orc.stage("WC_DENSITY")
         assert_close("density", ctx.get("DENSITY"), orc.get("DENSITY"))
+        # the pressure is the equation of state of the GPU's density bit for bit; against
+        # the oracle's pressure it carries the density's last-place differences amplified
+        # by d p / d rho = 7 p / (rho - rho0), hence 1e-4 on that comparison
+        assert np.array_equal(ctx.get("PRESSURE"), tait(ctx.get("DENSITY"), ctx.params))
         assert_close("pressure", ctx.get("PRESSURE"), orc.get("PRESSURE"), rtol=1e-4)
         if mode == 0:
             # COMPAT densities are negative (poly6 of r): drive the force branch with
@@ -134,6 +138,25 @@ def test_pcisph_stages_match_oracle(gpu_lib, mode):
         assert_close("f_other", ctx.get("FORCE_OTHER"), orc.get("FORCE_OTHER"), 4)
         for f in ("DENSITY", "NORMAL", "FORCE_OTHER"):
             orc.set(f, ctx.get(f))
+        # one iteration's three passes alone on identical inputs, each at the 1e-5 bar
+        # (pressure and pressure force start at zero, as in the loop's first iteration)
+        ctx.stage("PCI_PREDICT")
+        orc.stage("PCI_PREDICT")
+        assert_close("pos_pred (alone)", ctx.get("POS_PRED"), orc.get("POS_PRED"), 4, rtol=1e-6)
+        orc.set("POS_PRED", ctx.get("POS_PRED"))
+        ctx.stage("PCI_UPDATE_PRESSURE")
+        orc.stage("PCI_UPDATE_PRESSURE")
+        assert np.abs(ctx.get("DENS_VAR").astype(np.float64) - orc.get("DENS_VAR")).max() <= 1e-5 * 1000.0
+        orc.set("PRESSURE", ctx.get("PRESSURE"))
+        ctx.stage("PCI_PRESSURE_FORCE")
+        orc.stage("PCI_PRESSURE_FORCE")
+        assert_close("f_press (alone)", ctx.get("FORCE_PRESSURE"), orc.get("FORCE_PRESSURE"), 4)
+        # the whole loop from the same start; its outputs accumulate the passes' last-place
+        # differences through rho* - rho0 over the iterations, hence 1e-4 on them
+        for o in (ctx, orc):
+            o.stage("PCI_INIT_FORCES")          # F_p = 0, as at the loop's start
+        o.set("PRESSURE", np.zeros(ctx.particle_count(), np.float32))   # p = 0, likewise
+        orc.set("FORCE_OTHER", ctx.get("FORCE_OTHER"))
         ctx.stage("PCI_LOOP")
         orc.stage("PCI_LOOP")
         assert ctx.get("PCI_ITERS")[0] == orc.get("PCI_ITERS")[0]
