@@ -155,7 +155,7 @@ def test_pcisph_stages_match_oracle(gpu_lib, mode):
         # differences through rho* - rho0 over the iterations, hence 1e-4 on them
         for o in (ctx, orc):
             o.stage("PCI_INIT_FORCES")          # F_p = 0, as at the loop's start
-        o.set("PRESSURE", np.zeros(ctx.particle_count(), np.float32))   # p = 0, likewise
+            o.set("PRESSURE", np.zeros(ctx.particle_count(), np.float32))   # p = 0, likewise
         orc.set("FORCE_OTHER", ctx.get("FORCE_OTHER"))
         ctx.stage("PCI_LOOP")
         orc.stage("PCI_LOOP")
