@@ -92,22 +92,45 @@ def load_workload(name, mode, seed=0):
     return workloads.pcisph_cube(mode=mode, seed=seed)
 
 
-def describe_workload(w, n, nb, params):
-    p = params
+def workload_config(name, method, n, nb, dx, h, dt, container, lists):
+    """The ``config`` of a bench line: what the workload is (both arms report the same one
+    for the same scene); how an arm computes it goes in its top-level keys."""
     return {
-        "workload": w["name"],
-        "method": "PCISPH" if p.method == 1 else "WCSPH",
+        "workload": name,
+        "method": method,
         "particles": n,
         "boundary_particles": nb,
-        "dx_m": w["dx"],
-        "h_m": p.support_radius,
-        "dt_s": p.time_step,
-        "container_m": list(w["container"]),
-        "mode": "physics" if p.mode == 1 else "compat",
-        "neighbors": "list" if p.neighbor_mode == 1 or p.method == 1 else "cell-scan",
+        "dx_m": dx,
+        "h_m": h,
+        "dt_s": dt,
+        "container_m": list(container),
+        "neighbors": "list" if lists else "cell-scan",
         "l2": ("inputs larger than L2 every step (particle state %.0f MB > 129 MB)" if n * 200 > 129e6 else
                "particle state %.0f MB (fits the 129 MB L2)") % (n * 200 / 1e6),
     }
+
+
+def describe_workload(w, n, nb, params):
+    p = params
+    return workload_config(w["name"], "PCISPH" if p.method == 1 else "WCSPH", n, nb, w["dx"], p.support_radius,
+                           p.time_step, w["container"], p.neighbor_mode == 1 or p.method == 1)
+
+
+def summary_of(line):
+    """The headline numbers of a bench line in a few keys, printed last so that a truncated
+    copy of the line still carries them."""
+    g = lambda d, *ks: (None if d is None else (d.get(ks[0]) if len(ks) == 1 else g(d.get(ks[0]), *ks[1:])))  # noqa
+    r = lambda x, k=4: None if x is None else float("%.*g" % (k, x))  # noqa
+    return {"updates_per_s": r(line.get("value")), "e2e_updates_per_s": r(g(line, "e2e", "value")),
+            "ms_per_step": r(line.get("ms_per_step")),
+            "dominant_kernel": g(line, "roofline", "kernel"), "hbm_frac": r(g(line, "roofline", "frac"), 3),
+            "issue_frac": r(g(line, "roofline", "issue", "frac"), 3),
+            "batched_speedup": r(g(line, "batched", "speedup"), 3),
+            "batched_mean_compression": r(g(line, "batched", "mean_density_error_batched"), 3),
+            "pcisph_358k_updates_per_s": r(g(line, "pcisph", "updates_per_s")),
+            "pcisph_4m_updates_per_s": r(g(line, "pcisph_4m", "updates_per_s")),
+            "adjoint_over_plain_time": r(g(line, "adjoint", "adjoint_over_plain_time"), 3),
+            "cpu_baseline_updates_per_s": r(g(line, "cpu_baseline", "value"))}
 
 
 class ClockSampler:
@@ -269,7 +292,11 @@ def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
             "speedup": tl / tb, "batched_ms_per_step": 1000 * tb / steps, "looped_ms_per_step": 1000 * tl / steps,
             "mean_density_error_batched": float(sb[:, 0].mean()), "mean_density_error_looped": float(sl[:, 0].mean()),
             "mean_abs_density_error_batched": float(sb[:, 1].mean()),
-            "mean_abs_density_error_looped": float(sl[:, 1].mean()), "device_flags": flags_b,
+            "mean_abs_density_error_looped": float(sl[:, 1].mean()),
+            "density_error_definitions": "mean_density_error_*: mean over particles of max(rho / rho0 - 1, 0), the "
+                                         "compression the <= 1 % criterion reads; mean_abs_density_error_*: mean "
+                                         "of |rho - rho0| / rho0 (free-surface particles count at their full "
+                                         "deficit)", "device_flags": flags_b,
             "block_size_batched": tuned_b["block_size"], "block_size_looped_by_size": tuned_l}
 
 
@@ -341,7 +368,12 @@ def bench_adjoint(torch, steps=200, every=20):
            "adjoint_updates_per_s": n * steps / (t_fwd + t_bwd),
            "adjoint_over_plain_time": (t_fwd + t_bwd) / t_plain,
            "gradients": {"d_mu": res["g_mu"], "d_c0": res["g_c0"], "d_k": res["g_k"]},
-           "fd_check_fp32": fd, "flags": adj.flags(), "tape_bytes": adj.tape_bytes()}
+           "fd_check_fp32": fd,
+           "fd_check_fp32_note": "informational: central differences of the FP32 GPU forward (FP32 rounding "
+                                 "dominates the differences in mu); the 1e-3 criterion is checked against FP64 "
+                                 "central differences and the FP64 adjoint on the 4,096-particle copy "
+                                 "(tests/test_gpu_adjoint.py)",
+           "flags": adj.flags(), "tape_bytes": adj.tape_bytes()}
     adj.close()
     ctx.close()
     return out
@@ -446,50 +478,59 @@ def bench_voxelize(reps=5):
 
 def run_reference(args):
     """The reference arm: the reference's own WCSPH kernels (kernels/*.cl through the CPU
-    runtime of oracle/ref_shim, work-groups on every host core) stepping a bounded sample of
-    the workload, launch for launch as WCSPHSimulation::simulate; where those kernels are
-    not built (or for PCISPH), the oracle's COMPAT restatement of them on all cores."""
+    runtime of oracle/ref_shim, work-groups on every host core) stepping the benchmark's
+    whole scene, launch for launch as WCSPHSimulation::simulate.  For the default workload
+    the scene comes from oracle.refscene (its walls from the reference's own
+    FishTank::surface_sampling), so this process loads none of the product's libraries.
+    Where the reference kernels are not built, or for the PCISPH workloads, the oracle's
+    COMPAT restatement of them runs instead on all cores."""
     rank, _, world = dist_env()
     if rank != 0:
         return
-    from fluids_gb300 import capi
-    w = load_workload(args.workload, capi.SPH_MODE_COMPAT)
-    # bounded sample: a slab of the workload (every particle in the lowest sixteenth in z)
-    z = w["fluid"][:, 2]
-    crop = np.nonzero(z < np.quantile(z, 1.0 / 16))[0] if args.workload == "wcsph4m" else None
-    fluid = w["fluid"] if crop is None else w["fluid"][crop]
     threads = os.cpu_count() or 1
-    nb = sum(len(b[0]) for b in w["bodies"])
-    p = w["params"]
     stepper = None
-    if p.method == capi.SPH_WCSPH and len(w["bodies"]) == 1:
+    if args.workload == "wcsph4m":
         try:
-            from oracle import refkernels
+            from oracle import refkernels, refscene
             if refkernels.build() is not None:
                 from oracle.refstep import RefWCSPH
-                stepper = RefWCSPH(fluid, w["bodies"][0][0], w["container"], p.time_step, p.max_vel, p.k_viscosity,
-                                   p.surface_tension, p.gas_stiffness, p.rest_density, p.gravity, p.particle_radius,
-                                   p.support_radius)
+                r = refscene.double_dam_4m()
+                fluid, walls, pr = r["fluid"], r["walls"], r["params"]
+                t0 = time.perf_counter()
+                stepper = RefWCSPH(fluid, walls, r["container"], pr["time_step"], pr["max_vel"], pr["k_viscosity"],
+                                   pr["surface_tension"], pr["gas_stiffness"], pr["rest_density"], pr["gravity"],
+                                   pr["particle_radius"], pr["support_radius"])
+                setup_s = time.perf_counter() - t0
+                f32 = lambda x: float(np.float32(x))  # noqa: E731 -- the solver's FP32 parameter values
+                cfg = workload_config(r["name"], "WCSPH", len(fluid), len(walls), r["dx"], f32(pr["support_radius"]),
+                                      f32(pr["time_step"]), r["container"], True)
         except Exception as e:  # noqa: BLE001 -- fall back to the restatement, say why
             print("reference kernels unavailable (%s); timing the oracle's restatement" % e, file=sys.stderr)
             stepper = None
     if stepper is not None:
         kind = "reference"
         what = ("the reference's own kernels (kernels/grid.cl, wcsph.cl, normals.cl) on a CPU OpenCL-C runtime "
-                "(oracle/ref_shim, %d threads; key sort = stable sort as clogs), COMPAT, 5 m grid with its 1 GB "
-                "cell table cleared every step" % threads)
+                "(oracle/ref_shim, %d threads; key sort = the stable sort clogs performs), its 5 m grid with the "
+                "1 GB cell table cleared every step; the whole %d-particle scene (set-up %.1f s untimed)"
+                % (threads, len(fluid), setup_s))
+        n, nb = len(fluid), len(walls)
 
         def run(k):
             for _ in range(k):
                 stepper.step()
     else:
+        from fluids_gb300 import capi
         from oracle import Oracle, kwargs_from_params
+        w = load_workload(args.workload, capi.SPH_MODE_COMPAT)
+        p = w["params"]
         o = Oracle(threads=threads, **kwargs_from_params(p, w["container"]))
         for pts, rot, mv, mass in w["bodies"]:
             o.add_boundary(pts, can_move=mv, rot3x4=rot, mass=mass)
-        o.set_fluid(fluid)
+        o.set_fluid(w["fluid"])
+        n, nb = len(w["fluid"]), sum(len(b[0]) for b in w["bodies"])
+        cfg = describe_workload(w, n, nb, p)
         kind = "port"
-        what = "reference kernels' CPU port (oracle, COMPAT mode: 5 m grid, 50-entry neighbour lists)"
+        what = "reference kernels' CPU port (oracle, COMPAT mode: 5 m grid, 50-entry neighbour lists), whole scene"
 
         def run(k):
             o.step(k)
@@ -497,14 +538,16 @@ def run_reference(args):
     t0 = time.perf_counter()
     run(args.steps)
     dt = time.perf_counter() - t0
-    n = len(fluid)
     v = n * args.steps / dt
-    sample = "%s; %d fluid particles (a z-slab of the workload) + %d boundary, %d steps in %.1f s" % (
-        what, n, nb, args.steps, dt)
+    sample = "%s; %d fluid + %d boundary particles, %d steps in %.1f s" % (what, n, nb, args.steps, dt)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * dt / max(args.steps, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": describe_workload(w, n, nb, p),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + jitter)",
+            "config": cfg,
+            "mode": ("compat: the reference's kernel text, defects included (its density passes r, not r^2, "
+                     "to poly6, so densities are negative and compute_acceleration skips the fluid pressure, "
+                     "viscosity and surface-tension pairs behind its density > 0 guard, wcsph.cl:61-62,152)"),
+            "parallelism": "%d host threads" % threads,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -661,16 +704,16 @@ def main():
                            "oracle PHYSICS FP32 (same step as the GPU path), z-slab of the workload", crop)
     if rank == 0:
         cfg = describe_workload(w, n, nb, params)
-        cfg["grid_cells"] = d["grid_dims"]
-        cfg["parallelism"] = "replicas" if world > 1 else "single GPU"
-        cfg["block_size"] = tuned["block_size"]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + jitter)",
-                "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "config": cfg, "mode": "physics" if params.mode == 1 else "compat",
+                "grid_cells": d["grid_dims"], "parallelism": "replicas" if world > 1 else "single GPU",
+                "block_size": tuned["block_size"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk,
                 "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched, "adjoint": adjoint,
                 "pcisph": pcisph, "pcisph_4m": pcisph4m, "render": rend, "voxelize": vox}
+        line["summary"] = summary_of(line)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

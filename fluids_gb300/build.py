@@ -103,9 +103,10 @@ def build_driver(force=False):
     return DRIVER
 
 
-def ptxas_report(src="sph_wcsph.cu"):
-    """Registers / spills / shared memory per kernel (nvcc -Xptxas -v) for one source."""
+def ptxas_report(src="sph_wcsph.cu", extra=None):
+    """Registers / spills / shared memory per kernel (nvcc -Xptxas -v) for one source, with
+    the flags the build gives it."""
     cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", os.devnull, "-std=c++17", "-O3", "-Xptxas", "-v",
-           "-I", INCLUDE, "-I", CSRC] + ARCH
+           "-I", INCLUDE, "-I", CSRC] + ARCH + SOURCE_FLAGS.get(src, []) + list(extra or [])
     r = subprocess.run(cmd, capture_output=True, text=True)
     return r.stdout + r.stderr

@@ -2,7 +2,9 @@
 # Builds oracle/_ref/libref_kernels.so: the reference's own OpenCL kernels
 # (kernels/grid.cl, wcsph.cl, normals.cl, pcisph.cl, boundary.cl, bilateral.cl,
 # curvatureflow.cl and their headers)
-# compiled for the CPU through oracle/ref_shim/clshim.hpp, and its mesh code
+# compiled for the CPU through oracle/ref_shim/clshim.hpp, its host scene samplers
+# (BoxVolume::particles, FishTank::surface_sampling, Cube::surface_sampling, through
+# oracle/ref_shim/ref_scene.cpp), and its mesh code
 # (mesh/modelmesh.cpp, mesh/icospheremesh.cpp, external/voxelizer/voxelizer.h).  Used only to pin the oracle
 # and to generate tests/golden/ fixtures, in a container where the reference is mounted.
 #
@@ -32,13 +34,22 @@ if [ "$have_ref" = 1 ]; then
     for f in "$ref"/kernels/*.cl "$ref"/kernels/*.h; do
         sed -E 's/\((int4|float4)\)[[:space:]]*\(/make_\1(/g' "$f" > "$out/src/$(basename "$f")"
     done
+    # the host scene samplers: each function's text, from its signature line to its closing
+    # brace, unchanged (the rest of those files is OpenGL / Qt / Bullet code)
+    extract() {   # file, signature prefix, output
+        awk -v sig="$2" 'index($0, sig) == 1 {on = 1} on {print} on && /^}/ {exit}' "$1" > "$3"
+        [ -s "$3" ] || { echo "build_ref: $2 not found in $1" >&2; exit 1; }
+    }
+    extract "$ref/fluid/simulation/boxvolume.cpp" "vector<cl_float4> BoxVolume::particles(" "$out/src/boxvolume_particles.inc"
+    extract "$ref/scene/fishtank.cpp" "vector<btVector3> FishTank::surface_sampling(" "$out/src/fishtank_surface_sampling.inc"
+    extract "$ref/scene/cube.cpp" "vector<btVector3> Cube::surface_sampling(" "$out/src/cube_surface_sampling.inc"
 fi
 # (without the reference mounted, e.g. on the GPU machine, the kernel copies made here
 # under oracle/_ref/src, which travel with the working tree, are compiled again)
 CXX="${CXX:-g++}"
 flags=(-O2 -std=c++17 -fPIC -ffp-contract=off -pthread -Wall -Wno-sign-compare -Wno-unused -Wno-narrowing -I "$here/ref_shim" -I "$out/src")
 pids=()
-for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary ref_render; do
+for u in clshim_runtime ref_grid ref_wcsph ref_normals ref_pcisph ref_boundary ref_render ref_scene; do
     "$CXX" "${flags[@]}" -c "$here/ref_shim/$u.cpp" -o "$out/obj/$u.o" &
     pids+=($!)
 done

@@ -1,6 +1,7 @@
 /*
  * btVector3.h -- stand-in for Bullet's vector type so that the reference's
- * mesh/icospheremesh.cpp compiles for the oracle without Bullet (not in this image).
+ * mesh/icospheremesh.cpp and its scene samplers compile for the oracle without Bullet (not
+ * in this image).
  * TEST INFRASTRUCTURE: built only by oracle/build_ref.sh into oracle/_ref/.
  * Single-precision components; length() = sqrt(x*x + y*y + z*z) summed left to right and
  * normalized() multiplies by the reciprocal of the length, the order of Bullet's scalar
@@ -16,6 +17,9 @@ class btVector3 {
     float x() const { return v_[0]; }
     float y() const { return v_[1]; }
     float z() const { return v_[2]; }
+    float getX() const { return v_[0]; }
+    float getY() const { return v_[1]; }
+    float getZ() const { return v_[2]; }
     btVector3 operator+(const btVector3& o) const { return btVector3(v_[0] + o.v_[0], v_[1] + o.v_[1], v_[2] + o.v_[2]); }
     btVector3 operator-(const btVector3& o) const { return btVector3(v_[0] - o.v_[0], v_[1] - o.v_[1], v_[2] - o.v_[2]); }
     btVector3 operator*(const float& s) const { return btVector3(v_[0] * s, v_[1] * s, v_[2] * s); }

@@ -271,3 +271,28 @@ def icosphere(radius, level):
     ix = np.zeros(ni.value, np.uint32)
     lib().ref_icosphere(f(radius), C.c_uint(level), P(v), nv, P(ix), ni, C.byref(nv), C.byref(ni))
     return v, ix
+
+
+def _sample(fn, *args):
+    n = fn(*args, None, i(0))
+    out = np.zeros((max(n, 0), 4), np.float32)
+    if n > 0:
+        fn(*args, P(out), i(n))
+    return out
+
+
+def scene_box_volume(size3, center3, particle_radius):
+    """BoxVolume::particles (fluid/simulation/boxvolume.cpp:11-40), the reference's own code."""
+    s = np.ascontiguousarray(size3, np.float32).reshape(3)
+    c = np.ascontiguousarray(center3, np.float32).reshape(3)
+    return _sample(lib().ref_scene_box_volume, P(s), P(c), f(particle_radius))
+
+
+def scene_fishtank(width, height, depth, spacing):
+    """FishTank::surface_sampling (scene/fishtank.cpp:108-141) in body coordinates."""
+    return _sample(lib().ref_scene_fishtank, f(width), f(height), f(depth), f(spacing))
+
+
+def scene_cube(side, spacing):
+    """Cube::surface_sampling (scene/cube.cpp:136-171) in body coordinates."""
+    return _sample(lib().ref_scene_cube, f(side), f(spacing))
