@@ -68,7 +68,10 @@ def parse():
     ap.add_argument("--neighbor-mode", type=int, default=1, help="0 = cell scan in every pass, 1 = lists")
     ap.add_argument("--batched-steps", type=int, default=500, help="0 skips the batched comparison")
     ap.add_argument("--adjoint-steps", type=int, default=200, help="0 skips the adjoint comparison")
-    ap.add_argument("--pcisph-steps", type=int, default=100, help="0 skips the PCISPH line")
+    ap.add_argument("--pcisph-steps", type=int, default=500,
+                    help="0 skips the PCISPH line (500 = the PCISPH configuration's stated length)")
+    ap.add_argument("--wcsph65k-steps", type=int, default=1000,
+                    help="0 skips the 65,536-particle dam-break line (1000 = its stated length)")
     ap.add_argument("--pcisph4m-steps", type=int, default=20, help="0 skips the PCISPH 4M line")
     ap.add_argument("--render-frames", type=int, default=20, help="0 skips the screen-space surface line")
     return ap.parse_args()
@@ -129,6 +132,7 @@ def summary_of(line):
             "batched_mean_compression": r(g(line, "batched", "mean_density_error_batched"), 3),
             "pcisph_358k_updates_per_s": r(g(line, "pcisph", "updates_per_s")),
             "pcisph_4m_updates_per_s": r(g(line, "pcisph_4m", "updates_per_s")),
+            "wcsph_65k_updates_per_s": r(g(line, "wcsph_65k", "updates_per_s")),
             "adjoint_over_plain_time": r(g(line, "adjoint", "adjoint_over_plain_time"), 3),
             "cpu_baseline_updates_per_s": r(g(line, "cpu_baseline", "value"))}
 
@@ -407,10 +411,39 @@ def bench_pcisph(torch, steps, warmup, large=False):
     flags = ctx.device_flags()
     prof = ctx.profile_step(1)
     prof_iters = int(ctx.get("PCI_ITERS")[0])
+    hist = {str(k): int(v) for k, v in zip(*np.unique(iters, return_counts=True))}
     out = {"workload": w["name"], "particles": n, "boundary_particles": nb, "steps": steps,
            "updates_per_s": n * steps / t, "ms_per_step": 1000 * t / steps,
-           "pci_iterations_mean": float(np.mean(iters)), "pci_iterations": iters, "device_flags": flags,
+           "pci_iterations_mean": float(np.mean(iters)), "pci_iterations_histogram": hist, "device_flags": flags,
            "kernel_ms_per_step": prof, "kernel_ms_iterations": prof_iters}
+    ctx.close()
+    return out
+
+
+def bench_wcsph65k(torch, steps, warmup):
+    """The plain WCSPH dam break (65,536 particles on a 32 x 64 x 32 lattice at dx = 0.015 m,
+    FishTank walls, dt = 2e-4 s), PHYSICS mode, for its stated 1000 steps: device time of the
+    graph-replayed steps on the context stream."""
+    from fluids_gb300 import autotune, capi, workloads
+    w = workloads.dam_break_65k(capi.SPH_MODE_PHYSICS)
+    stream = torch.cuda.Stream()
+    ctx = workloads.build_context(w)
+    ctx.set_stream(stream.cuda_stream)
+    tuned = autotune.tune(ctx, w["params"].method, w["params"].mode, False)
+    n, nb = ctx.particle_count(), ctx.boundary_particle_count()
+    ctx.simulate(warmup)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ctx.simulate(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1000.0
+    st = ctx.stats()
+    out = {"workload": w["name"], "particles": n, "boundary_particles": nb, "steps": steps,
+           "updates_per_s": n * steps / t, "ms_per_step": 1000 * t / steps, "block_size": tuned["block_size"],
+           "device_flags": ctx.device_flags(), "kernel_ms_per_step": ctx.profile_step(1),
+           "final_mean_compression": st["mean_compression"], "final_kinetic_energy_j": st["kinetic"]}
     ctx.close()
     return out
 
@@ -620,7 +653,11 @@ def main():
         roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes": bytes_launch,
                 "mean_list_lengths": {"fluid": mean_len[0], "boundary": mean_len[1]},
-                "traffic": tr, "ms_per_launch": kern[top]}
+                "traffic": tr,
+                "traffic_from": ("profiles/roofline_traffic.txt: dram__bytes_read.sum + dram__bytes_write.sum of "
+                                 "one ncu capture of this kernel on this workload, stored with the code (not "
+                                 "measured in this run)") if tr is not None else None,
+                "ms_per_launch": kern[top]}
     # the pair loops are bound by FP32 issue, not DRAM: the same kernel against the SM issue rate
     ins = measured_instructions(top)
     if roof is not None and ins is not None:
@@ -632,7 +669,9 @@ def main():
         ach = ins[0] * n / (kern[top] / 1000.0)
         roof["issue"] = {"bound": "fp32-issue", "achieved": ach, "peak": peak_ips, "unit": "warp-instructions/s",
                          "frac": ach / peak_ips, "warp_instructions_per_particle": ins[0],
-                         "instructions_from": "ncu smsp__inst_executed.sum, " + ins[1],
+                         "instructions_from": ("profiles/roofline_instructions.txt: ncu smsp__inst_executed.sum "
+                                               "of one capture on " + ins[1] + ", stored with the code (not "
+                                               "measured in this run)"),
                          "peak_from": "%d SMs x 4 schedulers x %.0f MHz (%s)" % (sms, mhz, mhz_from)}
     passes = (d["key_bits"] + 7) // 8
     launches_per_step = sum(1 for k in kern) + (passes if "sort" in kern else 0)
@@ -696,6 +735,9 @@ def main():
         pcisph = bench_pcisph(torch, args.pcisph_steps, max(args.warmup, 3))
     if args.pcisph4m_steps > 0 and args.workload == "wcsph4m":
         pcisph4m = bench_pcisph(torch, args.pcisph4m_steps, 3, large=True)
+    wcsph65k = None
+    if args.wcsph65k_steps > 0 and args.workload == "wcsph4m":
+        wcsph65k = bench_wcsph65k(torch, args.wcsph65k_steps, max(args.warmup, 3))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         z = w["fluid"][:, 2]
@@ -712,7 +754,7 @@ def main():
                 "block_size": tuned["block_size"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk,
                 "kernel_ms_per_step": kern, "device_flags": flags, "batched": batched, "adjoint": adjoint,
-                "pcisph": pcisph, "pcisph_4m": pcisph4m, "render": rend, "voxelize": vox}
+                "pcisph": pcisph, "pcisph_4m": pcisph4m, "wcsph_65k": wcsph65k, "render": rend, "voxelize": vox}
         line["summary"] = summary_of(line)
         print(json.dumps(line), flush=True)
     if world > 1:
