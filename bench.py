@@ -256,6 +256,7 @@ def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
     b.set_stream(stream.cuda_stream)
     n = b.particle_count()
     tuned_b = autotune.tune(b, shared.method, shared.mode, True)
+    tile_shape = b.tile_shape()
     b.simulate(warmup)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -301,7 +302,10 @@ def bench_batched(steps, warmup, torch, nscenes=256, rank=0, world=1):
                                          "compression the <= 1 % criterion reads; mean_abs_density_error_*: mean "
                                          "of |rho - rho0| / rho0 (free-surface particles count at their full "
                                          "deficit)", "device_flags": flags_b,
-            "block_size_batched": tuned_b["block_size"], "block_size_looped_by_size": tuned_l}
+            "block_size_batched": tuned_b["block_size"],
+            "tile_shape_batched": dict(tile_shape, tuned_from=tuned_b.get("source"),
+                                       seconds_per_step_by_shape=tuned_b.get("seconds_per_step")),
+            "block_size_looped_by_size": tuned_l}
 
 
 def bench_adjoint(torch, steps=200, every=20):

@@ -1,10 +1,13 @@
 """Launch-shape autotuner for a context's step.
 
 The threads per block of the step's kernels (sph_set_block_size) are chosen by timing a
-few steps of the live context at each candidate and keeping the fastest; the choice is
+few steps of the live context at each candidate and keeping the fastest; for a batched
+context the candidates are the shapes of its persistent tile launches -- threads per block
+and CTAs per SM (sph_set_tile_shape) of the grid whose warps take the 32-particle scene
+tiles.  The choice is
 stored in a JSON file keyed by GPU name, method, mode, batched or not, and the particle
 count rounded to a power of two, so later contexts of the same kind reuse it without
-timing.  The launch shape never changes results (tests/test_gpu_autotune.py), only speed.
+timing.  The launch shape never changes results (tests/test_autotune.py), only speed.
 
     from fluids_gb300 import autotune
     choice = autotune.tune(ctx, method=0, mode=1, batched=False)
@@ -17,6 +20,8 @@ import os
 import time
 
 CANDIDATES = (64, 128, 256)
+# CTAs per SM of a batched context's persistent tile launches (0: 2048 / block size)
+TILE_CTAS = (0, 2, 4)
 
 
 def cache_path():
@@ -60,9 +65,12 @@ def store(key, entry, path=None):
     os.replace(tmp, path)
 
 
-def measure(ctx, block_size, steps, warmup, clock=time.perf_counter):
-    """Seconds per step of ctx at block_size (the state advances by warmup + steps)."""
+def measure(ctx, block_size, steps, warmup, clock=time.perf_counter, ctas=None):
+    """Seconds per step of ctx at block_size (and, for a batched context, ctas CTAs per SM of
+    the tile launches); the state advances by warmup + steps."""
     ctx.set_block_size(block_size)
+    if ctas is not None:
+        ctx.set_tile_shape(ctas)
     ctx.simulate(warmup)
     ctx.synchronize()
     t0 = clock()
@@ -81,19 +89,31 @@ def tune(ctx, method, mode, batched, steps=10, warmup=3, candidates=CANDIDATES, 
     With restore, the particle state is put back after the timing steps, so a tuned context
     continues from where it was."""
     key = tune_key(device or device_name(), method, mode, batched, ctx.particle_count())
+    tiles = batched and hasattr(ctx, "set_tile_shape")
     if use_cache:
         hit = load_cache(path).get(key)
-        if hit and hit.get("block_size") in candidates:
+        if hit and hit.get("block_size") in candidates and (not tiles or "ctas_per_sm" in hit):
             ctx.set_block_size(hit["block_size"])
+            if tiles:
+                ctx.set_tile_shape(hit["ctas_per_sm"])
             return dict(hit, source="cache", key=key)
     saved = {f: ctx.get(f) for f in STATE_FIELDS} if restore and hasattr(ctx, "get") else None
-    tried = {int(bs): measure(ctx, bs, steps, warmup, clock) for bs in candidates}
+    if tiles:
+        shapes = [(int(bs), int(k)) for bs in candidates for k in TILE_CTAS]
+        tried = {sh: measure(ctx, sh[0], steps, warmup, clock, ctas=sh[1]) for sh in shapes}
+    else:
+        tried = {(int(bs), None): measure(ctx, bs, steps, warmup, clock) for bs in candidates}
     if saved is not None:
         for f, a in saved.items():
             ctx.set(f, a)
-    best = min(tried, key=lambda b: (tried[b], -b))
-    ctx.set_block_size(best)
-    entry = {"block_size": best, "seconds_per_step": {str(b): t for b, t in sorted(tried.items())}}
+    best = min(tried, key=lambda sh: (tried[sh], -sh[0], -(sh[1] or 0)))
+    ctx.set_block_size(best[0])
+    if tiles:
+        ctx.set_tile_shape(best[1])
+        entry = {"block_size": best[0], "ctas_per_sm": best[1],
+                 "seconds_per_step": {"%d/%d" % sh: t for sh, t in sorted(tried.items())}}
+    else:
+        entry = {"block_size": best[0], "seconds_per_step": {str(sh[0]): t for sh, t in sorted(tried.items())}}
     if use_cache:
         store(key, entry, path)
     return dict(entry, source="timed", key=key)

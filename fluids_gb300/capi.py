@@ -46,7 +46,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc", "sph_batch_create",
            "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid",
            "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
-           "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size", "sph_get_field_async",
+           "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size", "sph_set_tile_shape",
+           "sph_get_tile_shape", "sph_get_field_async",
            "sph_set_field_async",
            "sph_set_body_dynamics", "sph_get_body_state", "sph_render_depth", "sph_filter_bilateral",
            "sph_render_smooth", "sph_filter_curvature_flow", "sph_render_normals", "sph_scene_load_obj",
@@ -193,6 +194,9 @@ def lib():
             "sph_adj_flags": (ip, [vp, C.POINTER(C.c_uint)]),
             "sph_adj_tape_bytes": (ip, [vp, C.POINTER(C.c_size_t)]),
             "sph_set_block_size": (ip, [vp, ip]),
+            "sph_set_tile_shape": (ip, [vp, ip]),
+            "sph_get_tile_shape": (ip, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int)]),
             "sph_get_field_async": (ip, [vp, ip, vp, C.c_size_t]),
             "sph_set_field_async": (ip, [vp, ip, vp, C.c_size_t]),
             "sph_set_body_dynamics": (ip, [vp, ip, ip, fp, C.c_float]),
@@ -498,6 +502,16 @@ class BatchContext(Context):
         out = (C.c_double * (8 * self.nscenes))()
         self._c(self._lib.sph_batch_stats(self.h, out, self.nscenes))
         return np.array(out[:], dtype=np.float64).reshape(self.nscenes, 8)
+
+    def set_tile_shape(self, ctas_per_sm):
+        """CTAs per SM of the persistent per-scene tile launches (0: 2048 / block size)."""
+        self._c(self._lib.sph_set_tile_shape(self.h, int(ctas_per_sm)))
+
+    def tile_shape(self):
+        """{tile_particles, ctas_per_sm, tiles, blocks} of the persistent tile launches."""
+        v = [C.c_int() for _ in range(4)]
+        self._c(self._lib.sph_get_tile_shape(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("tile_particles", "ctas_per_sm", "tiles", "blocks"), [x.value for x in v]))
 
 
 class Adjoint:

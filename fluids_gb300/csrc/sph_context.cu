@@ -278,6 +278,35 @@ void carve(sph_ctx* x, Carver& cv) {
         x->d_scene_of = cv.take<int32_t>(n);
         x->d_scene_stats = cv.take<double>(8 * x->scene_in.size());
     }
+    /* persistent scene tiles: at most one per 32 particles of a scene plus one per scene */
+    b.tiles = cv.take<sph::SceneTile>(x->scene_in.empty() ? 1 : n / sph::kTileParticles + x->scene_in.size() + 1);
+    b.tile_next = cv.take<unsigned>(4);
+}
+
+/* The scene tile table of a batched context: each scene's particle range cut into tiles of
+ * at most 32 particles (one warp), in scene order; and the grid of the persistent launches
+ * whose CTAs take chunks of tiles from a counter.  Uploaded synchronously (a host vector). */
+int upload_tiles(sph_ctx* x) {
+    x->c.ntiles = 0;
+    x->c.tile_blocks = 0;
+    if (x->scene_in.empty() || x->N <= 0 || !x->b.tiles) return SPH_OK;
+    x->h_tiles.clear();
+    for (size_t sc = 0; sc < x->scene_in.size(); ++sc) {
+        const int first = x->scene_in[sc].first, count = x->scene_in[sc].count;
+        const int T = sph::kTileParticles;
+        for (int a = 0; a < count; a += T)
+            x->h_tiles.push_back(sph::SceneTile{(int)sc, first + a, count - a < T ? count - a : T, 0});
+    }
+    if (x->h_tiles.empty()) return SPH_OK;
+    const int per_sm = x->tile_ctas > 0 ? x->tile_ctas : (2048 / x->bs > 0 ? 2048 / x->bs : 1);
+    const long long blocks = (long long)x->num_sms * per_sm;
+    x->c.ntiles = (int)x->h_tiles.size();
+    const long long warps_needed = (x->c.ntiles + x->bs / 32 - 1) / (x->bs / 32);
+    x->c.tile_blocks = (int)(blocks < warps_needed ? blocks : warps_needed);
+    SPH_CUDA(x, cudaStreamSynchronize(x->stream));
+    SPH_CUDA(x, cudaMemcpy(const_cast<sph::SceneTile*>(x->b.tiles), x->h_tiles.data(),
+                           sizeof(sph::SceneTile) * x->h_tiles.size(), cudaMemcpyHostToDevice));
+    return SPH_OK;
 }
 
 void drop_graph(sph_ctx* x) {
@@ -693,6 +722,8 @@ int rebuild(sph_ctx* x, bool keep) {
         SPH_CUDA(x, cudaGetLastError());
     }
     x->coop_blocks = sph::pci_loop_blocks(x->num_sms, x->bs);
+    int trc = upload_tiles(x);
+    if (trc != SPH_OK) return trc;
     x->has_state = true;
     SPH_CUDA(x, cudaGetLastError());
     return SPH_OK;
@@ -1037,6 +1068,25 @@ int sph_set_block_size(sph_ctx* x, int block_size) {
     x->bs = block_size;
     x->coop_blocks = sph::pci_loop_blocks(x->num_sms, x->bs);
     drop_graph(x);
+    return upload_tiles(x);
+}
+
+int sph_set_tile_shape(sph_ctx* x, int ctas_per_sm) {
+    if (check_ctx(x)) return SPH_E_INVALID;
+    if (x->scene_in.empty()) return fail(x, SPH_E_INVALID, "sph_set_tile_shape: not a batched context");
+    if (ctas_per_sm < 0 || ctas_per_sm > 64) return fail(x, SPH_E_INVALID, "ctas_per_sm must be 0..64");
+    cudaStreamSynchronize(x->stream);
+    x->tile_ctas = ctas_per_sm;
+    drop_graph(x);
+    return upload_tiles(x);
+}
+
+int sph_get_tile_shape(const sph_ctx* x, int* tile_particles, int* ctas_per_sm, int* ntiles, int* blocks) {
+    if (!x || !tile_particles || !ctas_per_sm || !ntiles || !blocks) return SPH_E_INVALID;
+    *tile_particles = sph::kTileParticles;
+    *ctas_per_sm = x->tile_ctas;
+    *ntiles = x->c.ntiles;
+    *blocks = x->c.tile_blocks;
     return SPH_OK;
 }
 

@@ -42,6 +42,8 @@ struct sph_ctx {
     int max_iter_slots = 1;
     int coop_blocks = 0;
     int bs = 256;
+    int tile_ctas = 0;   /* batched: CTAs per SM of the persistent tile launches (0: 2048 / bs) */
+    std::vector<sph::SceneTile> h_tiles;
     bool graph_ok = true;
     cudaGraphExec_t gexec = nullptr;
     uint32_t* cur_keys = nullptr;

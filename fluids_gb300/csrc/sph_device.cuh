@@ -38,6 +38,8 @@ struct Const {
     float cull2;         /* (h_list / cell)^2 * (1 + 1e-4): face-distance bound for skipping cells */
     int batched;         /* 1: per-scene grid and parameters from a SceneDev table */
     int scene_shift;     /* Morton bits below the scene id in the sort key */
+    int ntiles;          /* batched: entries of the scene tile table (SceneTile) */
+    int tile_blocks;     /* batched: CTAs of a persistent launch over the tiles */
 };
 
 /* One scene of a batched context: its grid (origin, dimensions, offset of its cells in the
@@ -69,6 +71,51 @@ __device__ __forceinline__ long long scene_setup(Const& c, const SceneDev* scene
     apply_scene(c, sd);
     return sd.cell_base;
 }
+/* A per-scene tile of a batched context: particles [first, first + count) of scene
+ * `scene`, count at most 32 (one warp).  Tiles never straddle scenes. */
+constexpr int kTileParticles = 32;
+struct SceneTile {
+    int scene, first, count, pad;
+};
+
+/* Runs f(c, cell_base, i) for the particles of a launch.  Single scene (BATCH = false): one
+ * particle per thread of a flat grid, the parameter's constants.  Batched: a persistent
+ * grid of tile_blocks CTAs takes the scene tiles from a counter (*next, zero before the
+ * launch), one contiguous chunk of blockDim / 32 tiles per CTA at a time, one tile per
+ * warp, so the work balances dynamically however uneven the tiles are and the warps of a
+ * CTA work on adjacent particles (whose neighbour cells they share in L1); a tile's scene
+ * constants are read once, at a warp-uniform address, for its 32 particles (one per lane),
+ * instead of being looked up per particle.  f must not use warp-collective operations (a
+ * tile's lanes beyond its count are idle). */
+template <bool BATCH, class F>
+__device__ __forceinline__ void for_each_particle(const Const& c0, const SceneTile* __restrict__ tiles,
+                                                  const SceneDev* __restrict__ scenes, unsigned* next, F&& f) {
+    if constexpr (BATCH) {
+        __shared__ int s_chunk;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+#pragma unroll 1
+        for (;;) {
+            if (threadIdx.x == 0) s_chunk = (int)atomicAdd(next, (unsigned)warps);
+            __syncthreads();
+            const int t = s_chunk + warp;
+            __syncthreads();   /* every thread has read s_chunk before it is written again */
+            if (t - warp >= c0.ntiles) break;
+            if (t < c0.ntiles) {
+                const SceneTile tl = tiles[t];
+                if (lane < tl.count) {
+                    Const c = c0;
+                    const SceneDev& sd = scenes[tl.scene];
+                    apply_scene(c, sd);
+                    f(c, sd.cell_base, tl.first + lane);
+                }
+            }
+        }
+    } else {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < c0.n) f(c0, 0LL, i);
+    }
+}
+
 /* Compile-time choice: single-scene kernels (BATCH = false) use the parameter's grid and
  * carry no scene code at all; batched kernels always apply the particle's scene. */
 template <bool BATCH>

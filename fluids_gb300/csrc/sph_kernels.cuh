@@ -50,6 +50,8 @@ struct Bufs {
     /* batched contexts: scene table and the scene of each fluid particle (ranges never move) */
     const SceneDev* scenes;
     const int32_t* scene_of;
+    const SceneTile* tiles;                /* batched: per-scene tiles of 32 particles (Const::ntiles) */
+    unsigned* tile_next;                   /* batched: the tile counters of the four tiled passes */
     /* status */
     unsigned* flags;
     int32_t* pci_iters;

@@ -27,15 +27,13 @@ __device__ __forceinline__ float4 make_aux(float d, float p) {
 }
 
 template <bool COMPAT, bool LIST, bool BATCH>
-__global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl,
+__global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT> fl0, Neigh<LIST, COMPAT> bl0,
                                                     const float* __restrict__ bphi_s, float* __restrict__ dens,
                                                     float* __restrict__ pres, float4* __restrict__ aux,
                                                     const SceneDev* __restrict__ scenes,
-                                                    const int32_t* __restrict__ scene_of) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c0.n) return;
-    Const c = c0;
-    const long long base = scene_setup_t<BATCH>(c, scenes, scene_of, i);
+                                                    const SceneTile* __restrict__ tiles, unsigned* next) {
+  for_each_particle<BATCH>(c0, tiles, scenes, next, [&](const Const& c, long long base, int i) {
+    Neigh<LIST, COMPAT> fl = fl0, bl = bl0;
     fl.tab += base;
     bl.tab += base;
     const float4 pi = __ldg(&fl.npos[i]);
@@ -61,6 +59,7 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
     const float p = (0.f < pv) ? pv : 0.f;
     pres[i] = p;
     aux[i] = make_aux(di, p);
+  });
 }
 
 /* compute_neigh_list (kernels/grid.cl:145-182, fluid and boundary) fused with
@@ -80,25 +79,22 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
  * PCISPH step needs no separate initial-density pass. */
 template <bool COMPAT, bool BATCH, bool REMAP = false, bool PCI = false>
 __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Const c0, const float4* __restrict__ spos,
-                                                       const int2* __restrict__ tab,
+                                                       const int2* __restrict__ tab0,
                                                        const float4* __restrict__ bpos_s,
-                                                       const int2* __restrict__ btab,
+                                                       const int2* __restrict__ btab0,
                                                        const float* __restrict__ bphi_s, int* __restrict__ nlist,
                                                        int* __restrict__ nlen, int* __restrict__ sblist,
                                                        int* __restrict__ sblen, float* __restrict__ dens,
                                                        float* __restrict__ pres, float4* __restrict__ aux,
                                                        const SceneDev* __restrict__ scenes,
-                                                       const int32_t* __restrict__ scene_of,
+                                                       const SceneTile* __restrict__ tiles, unsigned* next,
                                                        const int32_t* __restrict__ remap = nullptr,
                                                        unsigned* __restrict__ flags = nullptr,
                                                        const uint8_t* __restrict__ bnear = nullptr,
                                                        const int32_t* __restrict__ noff = nullptr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c0.n) return;
-    Const c = c0;
-    const long long base = scene_setup_t<BATCH>(c, scenes, scene_of, i);
-    tab += base;
-    btab += base;
+  for_each_particle<BATCH>(c0, tiles, scenes, next, [&](const Const& c, long long base, int i) {
+    const int2* __restrict__ ftab = tab0 + base;
+    const int2* __restrict__ fbtab = btab0 + base;
     const float4 pi = spos[i];
     const float hh = PCI ? c.h_def * c.h_def : c.h * c.h;
     const int row = REMAP ? __ldg(&remap[i]) : i;
@@ -107,7 +103,7 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     float di = 0.f;
     char* const lrow = reinterpret_cast<char*>(nlist + row);
     const unsigned n4 = 4u * (unsigned)c.n;
-    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, tab, spos, BATCH ? nullptr : noff,
+    const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, ftab, spos, BATCH ? nullptr : noff,
                              [&](bool hit, int j, float r2, int slot) {
         if (hit) *list_slot(lrow, slot, n4) = REMAP ? __ldg(&remap[j]) : j;
         const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
@@ -123,7 +119,7 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     const bool scan_b = c.wrap || bnear == nullptr || bnear[base + cell_lin(c, cx, cy, cz)] != 0;
     if (c.nb > 0 && !REMAP && scan_b) {
         char* const brow = reinterpret_cast<char*>(sblist + i);
-        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, btab, bpos_s, BATCH ? nullptr : noff,
+        kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, fbtab, bpos_s, BATCH ? nullptr : noff,
                         [&](bool hit, int j, float r2, int slot) {
             if (hit) *list_slot(brow, slot, n4) = j;
             const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
@@ -146,6 +142,7 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     const float p = (0.f < pv) ? pv : 0.f;
     pres[row] = p;
     aux[row] = make_aux(di, p);
+  });
 }
 
 /* aux from the density / pressure fields (used when those fields were set from outside). */
@@ -157,16 +154,15 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
 }
 
 template <bool LIST, bool EXACT, bool BATCH>
-__global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl, const float4* __restrict__ aux,
+__global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl0, const float4* __restrict__ aux,
                                                  const float* __restrict__ dens, float4* __restrict__ normal,
                                                  const SceneDev* __restrict__ scenes,
-                                                 const int32_t* __restrict__ scene_of,
+                                                 const SceneTile* __restrict__ tiles, unsigned* next,
                                                  const float4* __restrict__ vel_s = nullptr,
                                                  float4* __restrict__ nrec = nullptr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c0.n) return;
-    Const c = c0;
-    fl.tab += scene_setup_t<BATCH>(c, scenes, scene_of, i);
+  for_each_particle<BATCH>(c0, tiles, scenes, next, [&](const Const& c, long long base, int i) {
+    Neigh<LIST, EXACT> fl = fl0;
+    fl.tab += base;
     const float4 pi = __ldg(&fl.npos[i]);
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
@@ -190,6 +186,7 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
         nrec[2 * (size_t)i] = make_float4(v.x, v.y, v.z, a.x);
         nrec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, a.y);
     }
+  });
 }
 
 /* predict_vel_n_pos (kernels/wcsph.cl:176-224) for one particle. */
@@ -234,11 +231,9 @@ __device__ __forceinline__ void wc_integrate_one(const Const& c, float4 p, float
  * three separate loads; rho_j = 1/(1/rho_j) enters only the symmetrised surface-tension
  * factor 2 rho0 / (rho_i + rho_j) = 2 rho0 R_j / (rho_i R_j + 1). */
 template <bool COMPAT, bool LIST, bool FUSE, bool WRITE_ACC, bool ST, bool BATCH, bool PACK = false>
-__global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const c0, Neigh<LIST, COMPAT> fl, Neigh<LIST, COMPAT> bl, Bufs b) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c0.n) return;
-    Const c = c0;
-    const long long base = scene_setup_t<BATCH>(c, b.scenes, b.scene_of, i);
+__global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const c0, Neigh<LIST, COMPAT> fl0, Neigh<LIST, COMPAT> bl0, Bufs b) {
+  for_each_particle<BATCH>(c0, b.tiles, b.scenes, b.tile_next + 3, [&](const Const& c, long long base, int i) {
+    Neigh<LIST, COMPAT> fl = fl0, bl = bl0;
     fl.tab += base;
     bl.tab += base;
     const float4 pi = __ldg(&b.pos_s[i]);
@@ -334,6 +329,7 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
         b.ids[i] = __ldg(&b.ids_s[i]);
         if (bad) atomicOr(b.flags, kFlagNan);
     }
+  });
 }
 
 __global__ void __launch_bounds__(256) k_wc_integrate(Const c0, Bufs b) {
@@ -353,6 +349,19 @@ __global__ void __launch_bounds__(256) k_wc_integrate(Const c0, Bufs b) {
 }
 
 static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
+/* grid of a launch: one particle per thread, or the persistent tile grid of a batched context */
+template <bool BATCH>
+static inline int grid_for(const Const& c, int bs) {
+    if constexpr (BATCH) return c.tile_blocks > 0 ? c.tile_blocks : 1;
+    return nblk(c.n, bs);
+}
+/* a batched pass's tile counter, zeroed on the stream before its launch (slot: 0 density,
+ * 1 list build, 2 normals, 3 forces) */
+static unsigned* tile_counter(cudaStream_t s, const Bufs& b, int slot, bool batched) {
+    if (!batched) return nullptr;
+    cudaMemsetAsync(b.tile_next + slot, 0, sizeof(unsigned), s);
+    return b.tile_next + slot;
+}
 
 template <bool LIST, bool EXACT>
 static Neigh<LIST, EXACT> fluid_src(const Bufs& b) {
@@ -365,9 +374,10 @@ static Neigh<LIST, EXACT> bnd_src(const Bufs& b) {
 
 template <bool COMPAT, bool LIST, bool BATCH>
 static void density_launch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
-    k_wc_density<COMPAT, LIST, BATCH><<<nblk(c.n, bs), bs, 0, s>>>(c, fluid_src<LIST, COMPAT>(b),
+    unsigned* next = tile_counter(s, b, 0, BATCH);
+    k_wc_density<COMPAT, LIST, BATCH><<<grid_for<BATCH>(c, bs), bs, 0, s>>>(c, fluid_src<LIST, COMPAT>(b),
                                                                    bnd_src<LIST, COMPAT>(b), b.bphi_s, b.density,
-                                                                   b.pressure, b.aux, b.scenes, b.scene_of);
+                                                                   b.pressure, b.aux, b.scenes, b.tiles, next);
 }
 
 /* Batched contexts exist only in PHYSICS mode, so the scene lookup is compiled for that mode alone. */
@@ -392,23 +402,24 @@ void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists
 
 template <bool COMPAT, bool BATCH>
 static void lists_density_launch(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
-    k_lists_density<COMPAT, BATCH><<<nblk(c.n, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s,
-                                                                b.nlist, b.nlen, b.sblist, b.sblen, b.density,
-                                                                b.pressure, b.aux, b.scenes, b.scene_of, nullptr,
-                                                                nullptr, b.bnear, b.noff);
+    unsigned* next = tile_counter(s, b, 1, BATCH);
+    k_lists_density<COMPAT, BATCH><<<grid_for<BATCH>(c, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab,
+                                                                b.bphi_s, b.nlist, b.nlen, b.sblist, b.sblen,
+                                                                b.density, b.pressure, b.aux, b.scenes, b.tiles,
+                                                                next, nullptr, nullptr, b.bnear, b.noff);
 }
 
 void launch_lists_density_pci(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     if (c.n <= 0) return;
     k_lists_density<false, false, false, true><<<nblk(c.n, bs), bs, 0, s>>>(
         c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist, b.nlen, b.sblist, b.sblen, b.density, b.pressure,
-        b.aux, b.scenes, b.scene_of, nullptr, nullptr, b.bnear, b.noff);
+        b.aux, b.scenes, b.tiles, nullptr, nullptr, nullptr, b.bnear, b.noff);
 }
 void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, const int32_t* remap, int bs) {
     if (c.n <= 0) return;
     k_lists_density<false, false, true><<<nblk(c.n, bs), bs, 0, s>>>(
         c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist, b.nlen, b.sblist, b.sblen, b.density, b.pressure,
-        b.aux, b.scenes, b.scene_of, remap, b.flags);
+        b.aux, b.scenes, b.tiles, nullptr, remap, b.flags);
 }
 
 void launch_lists_density(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
@@ -425,36 +436,33 @@ void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
 
 void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs, bool pack) {
     if (c.n <= 0) return;
-    const int g = nblk(c.n, bs);
+    const int g = nblk(c.n, bs), gt = grid_for<true>(c, bs);
     float4* nrec = pack ? b.nrec : nullptr;
+    unsigned* next = tile_counter(s, b, 2, c.batched != 0);
     if (lists) {
         if (c.batched)
-            k_normals<true, true, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,
-                                                      b.scenes,
-                                                         b.scene_of, b.vel_s, nrec);
+            k_normals<true, true, true><<<gt, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,
+                                                          b.scenes, b.tiles, next, b.vel_s, nrec);
         else
             k_normals<true, true, false><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,
-                                                      b.scenes,
-                                                          b.scene_of, b.vel_s, nrec);
+                                                          b.scenes, b.tiles, next, b.vel_s, nrec);
     } else if (c.compat) {
         k_normals<false, true, false><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.density, b.normal,
-                                                      b.scenes,
-                                                       b.scene_of);
+                                                       b.scenes, b.tiles, next);
     } else if (c.batched) {
-        k_normals<false, false, true><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.density, b.normal,
-                                                      b.scenes,
-                                                       b.scene_of);
+        k_normals<false, false, true><<<gt, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.density, b.normal,
+                                                        b.scenes, b.tiles, next);
     } else {
         k_normals<false, false, false><<<g, bs, 0, s>>>(c, fluid_src<false, false>(b), b.aux, b.density, b.normal,
-                                                      b.scenes,
-                                                        b.scene_of);
+                                                        b.scenes, b.tiles, next);
     }
 }
 
 template <bool COMPAT, bool LIST, bool BATCH>
 static void forces_launch(cudaStream_t s, const Const& c, const Bufs& b, bool fuse, bool write_acc, int bs,
                           bool pack) {
-    const int g = nblk(c.n, bs);
+    const int g = grid_for<BATCH>(c, bs);
+    tile_counter(s, b, 3, BATCH);
     const bool st = c.sigma != 0.f;
     auto fs = fluid_src<LIST, COMPAT>(b);
     auto bsrc = bnd_src<LIST, COMPAT>(b);

@@ -281,6 +281,19 @@ int sph_batch_stats(sph_ctx* ctx, double* out8, int nscenes);
  * reference fixes its local sizes in the host code (e.g. grid.cpp:53 runs with 32). */
 int sph_set_block_size(sph_ctx* ctx, int block_size);
 
+/* Batched contexts (no counterpart in the reference, which steps one scene): the neighbour
+ * passes of a batched step (list build + density, normals, forces + integration) run as
+ * persistent launches over per-scene tiles -- each scene's particle range cut into tiles of
+ * 32 particles, a tile never straddling two scenes -- whose CTAs take the next chunk of
+ * tiles (one per warp) from a counter; a warp reads its tile's scene constants once.  The shape of the persistent grid is
+ * block_size threads (sph_set_block_size) times SMs x ctas_per_sm CTAs (0 = 2048 /
+ * block_size).  The shape never changes results; fluids_gb300/autotune.py picks it.
+ * SPH_E_INVALID on a single-scene context. */
+int sph_set_tile_shape(sph_ctx* ctx, int ctas_per_sm);
+/* The current tile shape: particles per tile, CTAs per SM (0 = automatic), tile count and
+ * CTAs of the persistent launches. */
+int sph_get_tile_shape(const sph_ctx* ctx, int* tile_particles, int* ctas_per_sm, int* ntiles, int* blocks);
+
 /* ---- differentiable WCSPH (adjoint) ----------------------------------------------------
  * No counterpart in the reference, which has no gradients.  The forward step is the WCSPH
  * step of WCSPHSimulation::simulate (wcsphsimluation.cpp:40-106) in PHYSICS mode; the

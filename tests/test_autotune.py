@@ -81,3 +81,30 @@ def test_tune_on_a_context_keeps_its_state(gpu_lib, tmp_path):
     for f in ("POS", "VEL", "ID"):
         assert np.array_equal(ctx.get(f), ref.get(f)), f
     assert ctx.device_flags() & capi.FLAGS["NAN"] == 0
+
+
+class FakeBatch(FakeCtx):
+    """A batched stand-in: the cost depends on the block size and the CTAs per SM."""
+
+    def __init__(self, cost, n=5000):
+        super().__init__(cost, n)
+        self.ctas = 0
+
+    def set_tile_shape(self, k):
+        self.ctas = k
+
+    def simulate(self, steps):
+        self.now += steps * self.cost[(self.bs, self.ctas)]
+
+
+def test_batched_tunes_tile_shapes_and_caches(tmp_path):
+    path = str(tmp_path / "launch.json")
+    cost = {(bs, k): 5.0 for bs in autotune.CANDIDATES for k in autotune.TILE_CTAS}
+    cost[(128, 2)] = 1.0
+    ctx = FakeBatch(cost)
+    r = autotune.tune(ctx, 0, 1, True, steps=2, warmup=1, path=path, device="GB300", clock=ctx.clock)
+    assert (r["block_size"], r["ctas_per_sm"]) == (128, 2) and (ctx.bs, ctx.ctas) == (128, 2)
+    assert len(r["seconds_per_step"]) == len(autotune.CANDIDATES) * len(autotune.TILE_CTAS)
+    ctx2 = FakeBatch(cost)
+    r2 = autotune.tune(ctx2, 0, 1, True, path=path, device="GB300", clock=ctx2.clock)
+    assert r2["source"] == "cache" and (ctx2.bs, ctx2.ctas) == (128, 2)

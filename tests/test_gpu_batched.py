@@ -60,3 +60,30 @@ def test_batched_rejects_single_scene_edits(gpu_lib):
         batch.set_rect_limits(1, 1, 1)
     with pytest.raises(capi.SphError):
         batch.add_volume(np.zeros((4, 4), np.float32))
+
+
+def test_tile_shape_changes_no_result(gpu_lib):
+    """The persistent per-scene tile launches (sph_set_tile_shape): every shape covers each
+    scene's particles with tiles of 32 particles and gives the same state bit for bit (each
+    particle's arithmetic does not depend on which warp takes its tile)."""
+    scenes = small_batch(6, seed=5)
+    shared = workloads.batched_params()
+    out = []
+    for bs, ctas in ((256, 0), (64, 1), (128, 4), (32, 2)):
+        batch = capi.BatchContext(shared, scenes)
+        batch.set_block_size(bs)
+        batch.set_tile_shape(ctas)
+        sh = batch.tile_shape()
+        want = sum(-(-len(s["fluid"]) // 32) for s in scenes)
+        assert sh["tile_particles"] == 32 and sh["ctas_per_sm"] == ctas and sh["tiles"] == want
+        assert 1 <= sh["blocks"] <= -(-want // (bs // 32))
+        batch.simulate(10)
+        out.append((batch.get("POS"), batch.get("VEL"), batch.get("NEIGH_LEN")))
+        assert batch.device_flags() & (capi.FLAGS["NAN"] | capi.FLAGS["TIMEOUT"]) == 0
+        batch.close()
+    for o in out[1:]:
+        for a, b in zip(out[0], o):
+            assert np.array_equal(a, b)
+    single = workloads.build_scene_context(shared, scenes[0])
+    assert capi.lib().sph_set_tile_shape(single.h, 2) == capi.SPH_E_INVALID   # not a batched context
+    single.close()
