@@ -18,6 +18,7 @@ _lib = None
 
 SPH_WCSPH, SPH_PCISPH = 0, 1
 SPH_MODE_COMPAT, SPH_MODE_PHYSICS = 0, 1
+SPH_KERNELS_MULLER, SPH_KERNELS_MONAGHAN = 0, 1
 SPH_NEIGH_SCAN, SPH_NEIGH_LIST = 0, 1
 SPH_FAULT_NONE, SPH_FAULT_BARRIER_STALL, SPH_FAULT_ALLOC_FAIL = 0, 1, 2
 FLAGS = dict(NAN=1, ESCAPED=2, TIMEOUT=4, OVERFLOW=8, NONCONVERGED=16, NONSMOOTH=32)
@@ -65,7 +66,7 @@ class SphParams(C.Structure):
                 ("gas_stiffness", C.c_float), ("surface_tension", C.c_float), ("grid_size", C.c_float),
                 ("grid_margin", C.c_float), ("boundary_phi_coeff", C.c_float), ("neigh_cap", C.c_int),
                 ("relax_on_add", C.c_int), ("neighbor_mode", C.c_int), ("use_graph", C.c_int),
-                ("block_size", C.c_int)]
+                ("block_size", C.c_int), ("kernels", C.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -70,8 +70,13 @@ __global__ void k_bnd_phi(Const c, int nb, const float4* __restrict__ bpos_s, co
     float del = 0.f;
     scan_neighbors<true>(cu, pi.x, pi.y, pi.z, btab, bpos_s, [&](int j, float4, float dx, float dy, float dz) {
         if (__ldg(&body_s[j]) == bi) {
-            const float t = HH - r2_exact(dx, dy, dz);
-            del += (t * t) * t;
+            const float r2 = r2_exact(dx, dy, dz);
+            if (c.monaghan) {   /* W_DEFAULT(r^2, h) with the Monaghan kernels (boundary.cl:26) */
+                del += w_monaghan(r2, H, H);
+            } else {
+                const float t = HH - r2;
+                del += (t * t) * t;
+            }
         }
     });
     const float phi = (c.rho0 / (del * c.boundary_eval)) / phi_coeff;

@@ -87,6 +87,7 @@ int derive(sph_ctx* x) {
     if (!(h > 0.f) || !(r > 0.f) || !(rho0 > 0.f) || !(p.time_step > 0.f))
         return fail(x, SPH_E_INVALID, "support_radius, particle_radius, rest_density and time_step must be > 0");
     c.compat = compat ? 1 : 0;
+    c.monaghan = (compat && p.kernels == SPH_KERNELS_MONAGHAN) ? 1 : 0;
     c.cap = p.neigh_cap > 0 ? p.neigh_cap : 50;
     c.h = h;
     c.h_def = round6(h);
@@ -1004,6 +1005,9 @@ int sph_create(const sph_params* params, sph_ctx** out) {
         return fail(nullptr, SPH_E_INVALID, "method must be SPH_WCSPH or SPH_PCISPH");
     if (params->mode != SPH_MODE_COMPAT && params->mode != SPH_MODE_PHYSICS)
         return fail(nullptr, SPH_E_INVALID, "mode must be SPH_MODE_COMPAT or SPH_MODE_PHYSICS");
+    if (params->kernels != SPH_KERNELS_MULLER &&
+        !(params->kernels == SPH_KERNELS_MONAGHAN && params->mode == SPH_MODE_COMPAT))
+        return fail(nullptr, SPH_E_INVALID, "kernels must be SPH_KERNELS_MULLER, or SPH_KERNELS_MONAGHAN in COMPAT mode");
     if (!sph_cuda_available()) return fail(nullptr, SPH_E_CUDA, "no CUDA device visible");
     sph_ctx* x = new sph_ctx();
     x->p = *params;

@@ -38,6 +38,7 @@ struct Const {
     float cull2;         /* (h_list / cell)^2 * (1 + 1e-4): face-distance bound for skipping cells */
     int batched;         /* 1: per-scene grid and parameters from a SceneDev table */
     int scene_shift;     /* Morton bits below the scene id in the sort key */
+    int monaghan;        /* COMPAT with the Monaghan kernels (sph_params::kernels) */
     int ntiles;          /* batched: entries of the scene tile table (SceneTile) */
     int tile_blocks;     /* batched: CTAs of a persistent launch over the tiles */
 };
@@ -425,6 +426,53 @@ struct Neigh {
         else scan_neighbors<EXACT>(c, px, py, pz, tab, npos, f);
     }
 };
+
+/* kernels/monaghan_kernels.h:7-47, the Monaghan cubic spline that kernels/kernels.h
+ * selects when a program is built without USE_MULLER_KERNELS; hd = SUPPORT_RADIUS (the -D
+ * constant), the normalisers and the arithmetic in the kernel text's order.  Used only by
+ * COMPAT contexts with sph_params::kernels = SPH_KERNELS_MONAGHAN. */
+__device__ __forceinline__ float mon_eval(float hd) { return 1.0f / (3.14159265358979323846f * ((hd * hd) * hd)); }
+__device__ __forceinline__ float mon_grad(float hd) {
+    return -3.0f / (3.14159265358979323846f * (((hd * hd) * hd) * hd));
+}
+__device__ __forceinline__ float w_monaghan(float r, float h, float hd) {
+    const float q = r / h;
+    if (r <= h) return mon_eval(hd) * ((1.0f - 1.5f * (q * q)) + 0.75f * ((q * q) * q));
+    if (r <= 2.0f * h) {
+        const float t = 2.0f - q;
+        return (mon_eval(hd) * 0.25f) * ((t * t) * t);
+    }
+    return 0.f;
+}
+/* grad_w_monaghan(r, rn, h): the inner branch subtracts 0.75 rn / h^2 from every component */
+__device__ __forceinline__ void grad_w_monaghan(float rx, float ry, float rz, float rn, float h, float hd, float& gx,
+                                                float& gy, float& gz) {
+    const float g = mon_grad(hd);
+    if (rn <= h) {
+        const float c = 0.75f * (rn / (h * h)), ih = 1.0f / h;
+        gx = (g * rx) * ih - c;
+        gy = (g * ry) * ih - c;
+        gz = (g * rz) * ih - c;
+    } else if (rn <= 2.0f * h) {
+        const float ir = 1.0f / rn, t = 2.0f - rn / h, q = t * t;
+        gx = (((g * rx) * 0.25f) * ir) * q;
+        gy = (((g * ry) * 0.25f) * ir) * q;
+        gz = (((g * rz) * 0.25f) * ir) * q;
+    } else {
+        gx = rx * 0.f;
+        gy = ry * 0.f;
+        gz = rz * 0.f;
+    }
+}
+__device__ __forceinline__ float lapl_w_monaghan(float rn, float h, float hd) {
+    const float l = 3.0f * mon_grad(hd);
+    if (rn <= h) return l * (1.0f / h - 1.5f * (rn / (h * h)));
+    if (rn <= 2.0f * h) {
+        const float t = 2.0f - rn / h;
+        return l * (((1.0f / (0.25f * rn)) * (t * t) - 1.0f / rn) + rn / (4.0f * (h * h)));
+    }
+    return 0.f;
+}
 
 /* pown(x, n) restated as left-to-right repeated multiplication. */
 __device__ __forceinline__ float pown2(float x) { return x * x; }

@@ -139,8 +139,12 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         /* the range test as a select: a rejected pair adds +0 */
-        const float t = (COMPAT || r2 < HH) ? HH - r2 : 0.f;
-        pd += (t * t) * t;
+        if (COMPAT && c.monaghan) {
+            pd += w_monaghan(r2, H, H);   /* W_DEFAULT(r^2, h), Monaghan kernels (pcisph.cl:396) */
+        } else {
+            const float t = (COMPAT || r2 < HH) ? HH - r2 : 0.f;
+            pd += (t * t) * t;
+        }
     };
     int k = 0;
     if (len >= 2) {
@@ -170,7 +174,8 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
         const float4 pj = __ldg(&b.bpos_s[j]);
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (COMPAT || r2 < HH) { const float t = HH - r2; pdb += ((t * t) * t) * __ldg(&b.bphi_s[j]); }
+        if (COMPAT && c.monaghan) pdb += w_monaghan(r2, H, H) * __ldg(&b.bphi_s[j]);
+        else if (COMPAT || r2 < HH) { const float t = HH - r2; pdb += ((t * t) * t) * __ldg(&b.bphi_s[j]); }
     }
     pdb *= c.default_eval;
     const float e0 = pd + pdb - c.rho0_def;
@@ -186,6 +191,7 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
 /* compute_pressure_force for one particle (initial density, updated pressure):
  * (p_i / rho_i^2 + p_j / rho_j^2) per pair with both quotients from pci_c (written by this
  * kernel's update phase, so plain loads); walked two entries deep like the update phase. */
+template <bool MON = false>
 __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Bufs& b, int i) {
     const float4 pi = __ldg(&b.pos_s[i]);
     const float H = c.h_def;
@@ -197,6 +203,18 @@ __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Buf
     auto visit = [&](float4 pj, float cj) {
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
+        if constexpr (MON) {   /* GRAD_W_PRESSURE(r, l, h) with the Monaghan kernels (pcisph.cl:482) */
+            const float l = sqrtf(r2);
+            if (l >= 1e-5f) {
+                float gx, gy, gz;
+                grad_w_monaghan(dx, dy, dz, l, H, H, gx, gy, gz);
+                const float q = C + cj;
+                fx += q * gx;
+                fy += q * gy;
+                fz += q * gz;
+            }
+            return;
+        }
         const float il0 = rsqrtf(r2), l0 = r2 * il0;
         /* the distance guard as selects: a rejected pair (the particle itself) adds zeros */
         const bool ok = l0 >= 1e-5f;
@@ -241,6 +259,14 @@ __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Buf
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float l = sqrtf(dx * dx + dy * dy + dz * dz);
         const float q = __ldg(&b.bphi_s[j]) * (2.0f * C);
+        if constexpr (MON) {
+            float wx, wy, wz;
+            grad_w_monaghan(dx, dy, dz, l, H, H, wx, wy, wz);
+            gx += q * wx;
+            gy += q * wy;
+            gz += q * wz;
+            continue;
+        }
         const float il = 1.0f / l, t = (H - l) * (H - l);
         gx += q * ((dx * il) * t);
         gy += q * ((dy * il) * t);
@@ -261,13 +287,23 @@ __global__ void __launch_bounds__(256) k_pci_init_density(Const c, Bufs b) {
     float di = 0.f, bdi = 0.f;
     list_neighbors<2, true>(i, c.n, b.nlist, __ldg(&b.nlen[i]), b.pos_s, pi.x, pi.y, pi.z,
                    [&](int, float4, float dx, float dy, float dz) {
-                       const float t = HH - (dx * dx + dy * dy + dz * dz);
-                       di += (t * t) * t;
+                       const float r2 = dx * dx + dy * dy + dz * dz;
+                       if (COMPAT && c.monaghan) {   /* W_DEFAULT(r^2, h), Monaghan (pcisph.cl:81) */
+                           di += w_monaghan(r2, H, H);
+                       } else {
+                           const float t = HH - r2;
+                           di += (t * t) * t;
+                       }
                    });
     list_neighbors(i, c.n, b.sblist, __ldg(&b.sblen[i]), b.bpos_s, pi.x, pi.y, pi.z,
                    [&](int j, float4, float dx, float dy, float dz) {
-                       const float t = HH - (dx * dx + dy * dy + dz * dz);
-                       bdi += ((t * t) * t) * __ldg(&b.bphi_s[j]);
+                       const float r2 = dx * dx + dy * dy + dz * dz;
+                       if (COMPAT && c.monaghan) {
+                           bdi += w_monaghan(r2, H, H) * __ldg(&b.bphi_s[j]);
+                       } else {
+                           const float t = HH - r2;
+                           bdi += ((t * t) * t) * __ldg(&b.bphi_s[j]);
+                       }
                    });
     const float d = c.default_eval * ((di * c.mass_def) + bdi);
     b.density[i] = d;
@@ -280,7 +316,8 @@ __global__ void __launch_bounds__(256) k_pci_init_density(Const c, Bufs b) {
  * (h - r) / rho_j as (h - r) * (1/rho_j), and 2 rho0 / (rho_i + rho_j) as
  * 2 rho0 R_j / (rho_i R_j + 1) with a fast division (FP32 results within a few ulp of the
  * IEEE forms).  Without PACK the pair terms are the kernel text's IEEE divisions. */
-template <bool PACK>
+/* MON: LAPL_W_VISCOSITY(r, h) with the Monaghan kernels (pcisph.cl:208) instead of h - r. */
+template <bool PACK, bool MON = false>
 __global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
@@ -301,14 +338,15 @@ __global__ void __launch_bounds__(256) k_pci_init_forces(Const c, Bufs b) {
                            const float Rj = nj.w;
                            inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
                            rn = r2 * inv;
-                           w = (H - rn) * Rj;
+                           if constexpr (MON) rn = sqrtf(r2);
+                           w = (MON ? lapl_w_monaghan(rn, H, H) : H - rn) * Rj;
                            K = __fdividef(two_rho0 * Rj, di * Rj + 1.0f);
                        } else {
                            vj = __ldg(&b.vel_s[j]);
                            nj = __ldg(&b.normal[j]);
                            const float dj = __ldg(&b.density[j]);
                            rn = sqrtf(r2);
-                           w = (H - rn) / dj;
+                           w = (MON ? lapl_w_monaghan(rn, H, H) : H - rn) / dj;
                            K = st_corr(c.rho0_def, di, dj);
                            inv = rn > 0.f ? 1.0f / rn : 0.f;
                        }
@@ -351,7 +389,11 @@ __global__ void __launch_bounds__(256, SPH_PCI_LOOP_MIN_BLOCKS) k_pci_loop(Const
         if (threadIdx.x == 0) atomicMax(reinterpret_cast<unsigned*>(&b.pci_maxerr[it - 1]), __float_as_uint(lmax));
         if (!grid_barrier(b.barrier, b.flags, (unsigned)c.barrier_extra)) return;
         const float mx = *reinterpret_cast<volatile float*>(&b.pci_maxerr[it - 1]);
-        for (int i = tid; i < n; i += stride) pci_pressure_force_one(c, b, i);
+        if (COMPAT && c.monaghan) {
+            for (int i = tid; i < n; i += stride) pci_pressure_force_one<true>(c, b, i);
+        } else {
+            for (int i = tid; i < n; i += stride) pci_pressure_force_one(c, b, i);
+        }
         bool stop = false;
         if (it >= min_iter) {
             const float crit = COMPAT ? (mx - c.rho0) / c.rho0 : mx / c.rho0;
@@ -398,7 +440,9 @@ __global__ void __launch_bounds__(256) k_pci_quotient(Const c, Bufs b) {
 
 __global__ void __launch_bounds__(256) k_pci_pressure_force(Const c, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < c.n) pci_pressure_force_one(c, b, i);
+    if (i >= c.n) return;
+    if (c.monaghan) pci_pressure_force_one<true>(c, b, i);
+    else pci_pressure_force_one(c, b, i);
 }
 
 static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
@@ -425,6 +469,11 @@ void launch_pci_init_density(cudaStream_t s, const Const& c, const Bufs& b, int 
 }
 void launch_pci_init_forces(cudaStream_t s, const Const& c, const Bufs& b, int bs, bool pack) {
     if (c.n <= 0) return;
+    if (c.monaghan) {
+        if (pack) k_pci_init_forces<true, true><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+        else k_pci_init_forces<false, true><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
+        return;
+    }
     if (pack) k_pci_init_forces<true><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
     else k_pci_init_forces<false><<<nblk(c.n, bs), bs, 0, s>>>(c, b);
 }

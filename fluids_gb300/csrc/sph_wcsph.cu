@@ -26,6 +26,20 @@ __device__ __forceinline__ float4 make_aux(float d, float p) {
     return make_float4(p / (d * d), 1.0f / d, d, p);
 }
 
+/* W_DEFAULT(r_norm, support_radius) of compute_density_pressure (wcsph.cl:61-62,70-71):
+ * PHYSICS (h^2 - r^2)^3; COMPAT the kernel text's (h^2 - r)^3, or with the Monaghan kernels
+ * w_monaghan(r, h). */
+template <bool COMPAT>
+__device__ __forceinline__ float w_default(const Const& c, float r2, float hh) {
+    if constexpr (COMPAT) {
+        if (c.monaghan) return w_monaghan(sqrtf(r2), c.h, c.h_def);
+        const float t = hh - sqrtf(r2);
+        return (t * t) * t;
+    }
+    const float t = hh - r2;
+    return (t * t) * t;
+}
+
 template <bool COMPAT, bool LIST, bool BATCH>
 __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT> fl0, Neigh<LIST, COMPAT> bl0,
                                                     const float* __restrict__ bphi_s, float* __restrict__ dens,
@@ -41,16 +55,14 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
     float di = 0.f;
     fl.visit(c, i, pi.x, pi.y, pi.z, [&](int, float4, float dx, float dy, float dz) {
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const float t = hh - (COMPAT ? sqrtf(r2) : r2);
-        di += (t * t) * t;
+        di += w_default<COMPAT>(c, r2, hh);
     });
     di *= c.poly6_eval * c.mass;
     float bdi = 0.f;
     if (c.nb > 0) {
         bl.visit(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
             const float r2 = dx * dx + dy * dy + dz * dz;
-            const float t = hh - (COMPAT ? sqrtf(r2) : r2);
-            bdi += ((t * t) * t) * __ldg(&bphi_s[j]);
+            bdi += w_default<COMPAT>(c, r2, hh) * __ldg(&bphi_s[j]);
         });
     }
     di += c.poly6_eval * bdi;
@@ -106,8 +118,12 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     const int k = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, ftab, spos, BATCH ? nullptr : noff,
                              [&](bool hit, int j, float r2, int slot) {
         if (hit) *list_slot(lrow, slot, n4) = REMAP ? __ldg(&remap[j]) : j;
-        const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
-        di += (t * t) * t;
+        if (COMPAT && c.monaghan) {
+            if (hit) di += w_monaghan(sqrtf(r2), c.h, c.h_def);
+        } else {
+            const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
+            di += (t * t) * t;
+        }
     });
     nlen[row] = k;
     if (k >= c.cap && REMAP) atomicOr(flags, kFlagOverflow);
@@ -122,10 +138,14 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
         kb = build_scan(c, pi.x, pi.y, pi.z, cx, cy, cz, fbtab, bpos_s, BATCH ? nullptr : noff,
                         [&](bool hit, int j, float r2, int slot) {
             if (hit) *list_slot(brow, slot, n4) = j;
-            const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
             float w = 0.f;
             if (hit) w = __ldg(&bphi_s[j]);
-            bdi += ((t * t) * t) * w;
+            if (COMPAT && c.monaghan) {
+                if (hit) bdi += w_monaghan(sqrtf(r2), c.h, c.h_def) * w;
+            } else {
+                const float t = hit ? hh - (COMPAT ? sqrtf(r2) : r2) : 0.f;
+                bdi += ((t * t) * t) * w;
+            }
         });
     }
     if (!REMAP) sblen[i] = kb;
@@ -153,7 +173,9 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
     aux[i] = make_aux(dens[i], pres[i]);
 }
 
-template <bool LIST, bool EXACT, bool BATCH>
+/* MON: compute_normals with the Monaghan kernels, GRAD_W_DEFAULT(r, r.r, h) / rho_j
+ * (normals.cl:66; the kernel text passes r^2 where the function takes |r|). */
+template <bool LIST, bool EXACT, bool BATCH, bool MON = false>
 __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl0, const float4* __restrict__ aux,
                                                  const float* __restrict__ dens, float4* __restrict__ normal,
                                                  const SceneDev* __restrict__ scenes,
@@ -172,11 +194,20 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
          * for aux; the pass is bound by L1 throughput); __frcp_rn is the correctly rounded
          * reciprocal, the value aux holds */
         const float inv_rho = __frcp_rn(__ldg(&dens[j]));
-        const float t = HH - (dx * dx + dy * dy + dz * dz);
-        const float k = (t * t) * inv_rho;
-        nx += dx * k;
-        ny += dy * k;
-        nz += dz * k;
+        if constexpr (MON) {
+            float gx, gy, gz;
+            grad_w_monaghan(dx, dy, dz, dx * dx + dy * dy + dz * dz, H, H, gx, gy, gz);
+            const float dj = __ldg(&dens[j]);
+            nx += gx / dj;
+            ny += gy / dj;
+            nz += gz / dj;
+        } else {
+            const float t = HH - (dx * dx + dy * dy + dz * dz);
+            const float k = (t * t) * inv_rho;
+            nx += dx * k;
+            ny += dy * k;
+            nz += dz * k;
+        }
     });
     const float k = (c.poly6_grad * c.mass_def) * H;
     const float4 nv = make_float4(nx * k, ny * k, nz * k, 0.f);
@@ -439,6 +470,15 @@ void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, i
     const int g = nblk(c.n, bs), gt = grid_for<true>(c, bs);
     float4* nrec = pack ? b.nrec : nullptr;
     unsigned* next = tile_counter(s, b, 2, c.batched != 0);
+    if (c.monaghan) {   /* COMPAT only */
+        if (lists)
+            k_normals<true, true, false, true><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density,
+                                                                b.normal, b.scenes, b.tiles, next, b.vel_s, nrec);
+        else
+            k_normals<false, true, false, true><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.density,
+                                                                 b.normal, b.scenes, b.tiles, next);
+        return;
+    }
     if (lists) {
         if (c.batched)
             k_normals<true, true, true><<<gt, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,

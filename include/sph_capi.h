@@ -88,7 +88,16 @@ typedef struct sph_params {
     int neighbor_mode;               /* sph_neighbors (WCSPH only) */
     int use_graph;                   /* capture a step in a CUDA graph (1) */
     int block_size;                  /* threads per block of particle kernels (32..256), 0 = 256 */
+    int kernels;                     /* sph_kernels: smoothing-kernel family (SPH_KERNELS_MULLER) */
 } sph_params;
+
+/* Smoothing-kernel family (kernels/kernels.h:8-37).  The reference builds every program with
+ * USE_MULLER_KERNELS (wcsphsimluation.cpp:370, pcisphsimluation.cpp:505,
+ * boundaryhandler.cpp:413); without it the kernel text's W_DEFAULT, GRAD_W_DEFAULT,
+ * GRAD_W_PRESSURE and LAPL_W_VISCOSITY become the Monaghan cubic spline of
+ * kernels/monaghan_kernels.h:7-47 at the same call sites (the host constants are unchanged).
+ * SPH_KERNELS_MONAGHAN reproduces that build; it exists in COMPAT mode only. */
+enum sph_kernels { SPH_KERNELS_MULLER = 0, SPH_KERNELS_MONAGHAN = 1 };
 
 typedef struct sph_ctx sph_ctx;
 

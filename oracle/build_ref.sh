@@ -65,6 +65,12 @@ if [ "$have_ref" = 1 ]; then
     "$CXX" "${mflags[@]}" -c "$here/ref_shim/ref_mesh.cpp" -o "$out/obj/ref_mesh.o" &
     pids+=($!)
 fi
+# the same kernel files built without USE_MULLER_KERNELS (the Monaghan kernels of
+# kernels/monaghan_kernels.h, compiled out in the reference): entry points *_monaghan
+for u in ref_wcsph ref_normals ref_pcisph ref_boundary; do
+    "$CXX" "${flags[@]}" -DCLSHIM_MONAGHAN -c "$here/ref_shim/$u.cpp" -o "$out/obj/${u}_monaghan.o" &
+    pids+=($!)
+done
 for p in "${pids[@]}"; do wait "$p"; done
 "$CXX" -shared -pthread -o "$out/libref_kernels.so" "$out"/obj/*.o
 echo "build_ref: built $out/libref_kernels.so"

@@ -37,7 +37,7 @@ class OrcConfig(C.Structure):
                 ("rest_density", C.c_float), ("k_viscosity", C.c_float), ("gravity", C.c_float),
                 ("gas_stiffness", C.c_float), ("surface_tension", C.c_float), ("grid_size", C.c_float),
                 ("grid_margin", C.c_float), ("phi_coeff", C.c_float), ("container", C.c_float * 3),
-                ("relax_on_add", C.c_int), ("threads", C.c_int)]
+                ("relax_on_add", C.c_int), ("threads", C.c_int), ("kernels", C.c_int)]
 
 
 class OrcDerived(C.Structure):
@@ -68,7 +68,7 @@ def kwargs_from_params(p, container):
                 pci_relax_max_iter=p.pcisph_relax_max_iterations, rest_density=p.rest_density,
                 k_viscosity=p.k_viscosity, gravity=p.gravity, gas_stiffness=p.gas_stiffness,
                 surface_tension=p.surface_tension, grid_size=p.grid_size, grid_margin=p.grid_margin,
-                phi_coeff=p.boundary_phi_coeff, relax_on_add=p.relax_on_add)
+                phi_coeff=p.boundary_phi_coeff, relax_on_add=p.relax_on_add, kernels=getattr(p, "kernels", 0))
 
 
 def build_oracle(force=False):
@@ -143,7 +143,7 @@ class Oracle:
                         support_radius=0.03, pci_min_iter=3, pci_max_iter=3, pci_error_ratio=0.01,
                         pci_relax_max_iter=10000, rest_density=1000.0, k_viscosity=0.01, gravity=9.81,
                         gas_stiffness=57142.857, surface_tension=0.001, grid_size=5.0, grid_margin=2.0,
-                        phi_coeff=1.0, relax_on_add=0, threads=0)
+                        phi_coeff=1.0, relax_on_add=0, threads=0, kernels=0)
         defaults.update(kw)
         cfg.method, cfg.mode, cfg.precision = method, mode, precision
         for k, v in defaults.items():

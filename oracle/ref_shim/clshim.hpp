@@ -170,3 +170,14 @@ inline void barrier(int) { clshim::barrier_impl(); }
 #define M_PI_F 3.14159265358979323846f
 
 #endif
+
+/* Names of a glue unit: the Monaghan build of a kernel file (CLSHIM_MONAGHAN, kernels.h
+ * without USE_MULLER_KERNELS) puts its kernels in namespace <name>_monaghan and exports its
+ * entry points as <name>_monaghan, so both builds link into one library. */
+#ifdef CLSHIM_MONAGHAN
+#define REF_NS(n) n##_monaghan
+#define REF_FN(n) n##_monaghan
+#else
+#define REF_NS(n) n
+#define REF_FN(n) n
+#endif

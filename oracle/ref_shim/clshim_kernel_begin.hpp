@@ -26,7 +26,12 @@
 #define CELL_SIZE (::clshim::g_cell_size)
 #define GRID_SIZE (::clshim::g_grid_size)
 #define CELLS_PER_SIDE (::clshim::g_cells_per_side)
+/* the program's kernel family: Mueller unless this unit is the Monaghan build (the reference
+ * always defines it: wcsphsimluation.cpp:370, pcisphsimluation.cpp:505,
+ * boundaryhandler.cpp:413; kernels/kernels.h selects the Monaghan kernels otherwise) */
+#ifndef CLSHIM_MONAGHAN
 #define USE_MULLER_KERNELS 1
+#endif
 #define USE_MORTON_ENCODING 1
 #define COMPUTE_BOUNDARY 1
 

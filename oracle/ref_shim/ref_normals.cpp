@@ -7,7 +7,7 @@
 #include "clshim.hpp"
 
 #include "clshim_kernel_begin.hpp"
-namespace ref_normals {
+namespace REF_NS(ref_normals) {
 #include "normals.cl"
 }
 #include "clshim_kernel_end.hpp"
@@ -16,7 +16,7 @@ using namespace clshim;
 
 extern "C" {
 
-void ref_compute_normals(const float* pos4, const float* dens, float* nrm4, int n, const int32_t* len,
+void REF_FN(ref_compute_normals)(const float* pos4, const float* dens, float* nrm4, int n, const int32_t* len,
                          const int32_t* list, float w_grad, float mass_define, float support_define,
                          int local_size) {
     g_particle_count = n;
@@ -25,7 +25,7 @@ void ref_compute_normals(const float* pos4, const float* dens, float* nrm4, int 
     const size_t local = local_size > 0 ? (size_t)local_size : 64;
     image1d_buffer_t ip{pos4, 4}, id{dens, 1};
     run_ndrange((size_t)n, local, true, [&] {
-        ref_normals::compute_normals(ip, id, reinterpret_cast<float4*>(nrm4), len, list, w_grad, static_cast<float4*>(group_local(0, sizeof(float4) * local)),
+        REF_NS(ref_normals)::compute_normals(ip, id, reinterpret_cast<float4*>(nrm4), len, list, w_grad, static_cast<float4*>(group_local(0, sizeof(float4) * local)),
                                      static_cast<float*>(group_local(1, sizeof(float) * local)));
     });
 }

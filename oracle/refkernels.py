@@ -1,6 +1,7 @@
 """ctypes wrapper of oracle/_ref/libref_kernels.so -- the reference's own OpenCL kernels
 compiled for the CPU (TEST INFRASTRUCTURE; pins the oracle; available only where the
 reference is mounted and ``oracle/build_ref.sh`` has run)."""
+import contextlib
 import ctypes as C
 import os
 import subprocess
@@ -57,6 +58,30 @@ def lib():
     return _lib
 
 
+# entry points the reference's Monaghan build exports too (name + "_monaghan")
+_MONAGHAN = {"ref_wc_density_pressure", "ref_wc_acceleration", "ref_wc_integrate", "ref_compute_normals",
+             "ref_pci_initial_density", "ref_pci_initial_forces", "ref_pci_predict_pos", "ref_pci_update_pressure",
+             "ref_pci_pressure_force", "ref_pci_integrate", "ref_boundary_phi", "ref_transform_particles",
+             "ref_fluid_force"}
+_suffix = ""
+
+
+@contextlib.contextmanager
+def monaghan():
+    """Inside this block the kernel wrappers run the reference's kernels as built without
+    USE_MULLER_KERNELS (the Monaghan kernels of kernels/monaghan_kernels.h)."""
+    global _suffix
+    old, _suffix = _suffix, "_monaghan"
+    try:
+        yield
+    finally:
+        _suffix = old
+
+
+def _f(name):
+    return getattr(lib(), name + (_suffix if name in _MONAGHAN else ""))
+
+
 def P(a):
     """Pointer to a contiguous numpy array (or NULL)."""
     if a is None:
@@ -77,7 +102,7 @@ def compute_hashes(pos4, size, h, cps):
     n = len(pos4)
     hs = np.zeros(n, np.uint32)
     mk = np.zeros(n, np.int32)
-    lib().ref_compute_hashes(P(pos4), i(n), f(size), f(h), i(cps), P(hs), P(mk))
+    _f("ref_compute_hashes")(P(pos4), i(n), f(size), f(h), i(cps), P(hs), P(mk))
     return hs, mk
 
 
@@ -87,8 +112,8 @@ def compute_cell_intervals(spos4, hashes, size, h, cps, out=None):
         iv = np.zeros(2 * cps ** 3, np.int32)
     else:
         iv = out
-        lib().ref_fill_zero(P(iv), C.c_longlong(iv.size))
-    lib().ref_compute_cell_intervals(P(spos4), P(hashes), i(len(spos4)), f(size), f(h), i(cps), P(iv))
+        _f("ref_fill_zero")(P(iv), C.c_longlong(iv.size))
+    _f("ref_compute_cell_intervals")(P(spos4), P(hashes), i(len(spos4)), f(size), f(h), i(cps), P(iv))
     return iv
 
 
@@ -96,7 +121,7 @@ def compute_neigh_list(ref_pos4, neigh_pos4, intervals, size, h, h_define, cps, 
     n = len(ref_pos4)
     lst = np.zeros(cap * max(n, 1), np.int32)
     ln = np.zeros(n, np.int32)
-    lib().ref_compute_neigh_list(P(ref_pos4), i(n), P(neigh_pos4), P(intervals), f(size), f(h), f(h_define),
+    _f("ref_compute_neigh_list")(P(ref_pos4), i(n), P(neigh_pos4), P(intervals), f(size), f(h), f(h_define),
                                  i(cps), P(lst), P(ln))
     return lst, ln
 
@@ -105,7 +130,7 @@ def wc_density_pressure(spos4, flist, flen, bpos4, bphi, blist, blen, mass, h, g
     n = len(spos4)
     d = np.zeros(n, np.float32)
     p = np.zeros(n, np.float32)
-    lib().ref_wc_density_pressure(P(spos4), i(n), P(d), P(p), f(mass), f(h), f(gas_k), f(rho0), f(poly6),
+    _f("ref_wc_density_pressure")(P(spos4), i(n), P(d), P(p), f(mass), f(h), f(gas_k), f(rho0), f(poly6),
                                   P(flen), P(flist), P(blist), P(blen), P(bpos4), P(bphi), f(h_define))
     return d, p
 
@@ -116,7 +141,7 @@ def wc_acceleration(spos4, svel4, nrm4, dens, pres, flist, flen, bpos4, bphi, bl
     acc = np.zeros((n, 4), np.float32)
     g4 = np.array([0.0, -g, 0.0, 0.0], np.float32)
     sc = np.ascontiguousarray(sc9, np.float32)
-    lib().ref_wc_acceleration(P(spos4), P(svel4), P(nrm4), P(dens), P(pres), P(acc), i(n), P(g4), f(mass), f(h),
+    _f("ref_wc_acceleration")(P(spos4), P(svel4), P(nrm4), P(dens), P(pres), P(acc), i(n), P(g4), f(mass), f(h),
                               f(h * h), f(mu), f(sigma), f(rho0), P(sc), P(flen), P(flist), P(blist), P(blen),
                               P(bpos4), P(bphi), f(st_main), f(st_term), f(h_define))
     return acc
@@ -126,7 +151,7 @@ def wc_integrate(spos4, svel4, svh4, acc4, dt, max_vel, limits, h_define):
     n = len(spos4)
     op, ov, ovh = (np.zeros((n, 4), np.float32) for _ in range(3))
     lim = np.array(list(limits) + [0.0], np.float32)
-    lib().ref_wc_integrate(P(spos4), P(svel4), P(svh4), P(acc4), i(n), f(dt), P(op), P(ov), P(ovh), f(max_vel),
+    _f("ref_wc_integrate")(P(spos4), P(svel4), P(svh4), P(acc4), i(n), f(dt), P(op), P(ov), P(ovh), f(max_vel),
                            P(lim), f(h_define))
     return op, ov, ovh
 
@@ -134,7 +159,7 @@ def wc_integrate(spos4, svel4, svh4, acc4, dt, max_vel, limits, h_define):
 def compute_normals(spos4, dens, flist, flen, w_grad, mass_define, h_define, local_size=64):
     n = len(spos4)
     nrm = np.zeros((n, 4), np.float32)
-    lib().ref_compute_normals(P(spos4), P(dens), P(nrm), i(n), P(flen), P(flist), f(w_grad), f(mass_define),
+    _f("ref_compute_normals")(P(spos4), P(dens), P(nrm), i(n), P(flen), P(flist), f(w_grad), f(mass_define),
                               f(h_define), i(local_size))
     return nrm
 
@@ -142,7 +167,7 @@ def compute_normals(spos4, dens, flist, flen, w_grad, mass_define, h_define, loc
 def pci_initial_density(spos4, flist, flen, bpos4, bphi, blist, blen, w_eval, h_def, m_def, rho_def, local_size=64):
     n = len(spos4)
     d = np.zeros(n, np.float32)
-    lib().ref_pci_initial_density(P(spos4), P(d), i(n), P(flen), P(flist), P(blist), P(blen), P(bpos4), P(bphi),
+    _f("ref_pci_initial_density")(P(spos4), P(d), i(n), P(flen), P(flist), P(blist), P(blen), P(bpos4), P(bphi),
                                   f(w_eval), f(h_def), f(m_def), f(rho_def), i(local_size))
     return d
 
@@ -151,7 +176,7 @@ def pci_initial_forces(spos4, svel4, dens, nrm4, flist, flen, mu, sigma, visc_la
                        rho_def, local_size=64):
     n = len(spos4)
     fo = np.zeros((n, 4), np.float32)
-    lib().ref_pci_initial_forces(P(spos4), P(svel4), P(dens), P(nrm4), P(fo), i(n), f(mu), f(sigma), P(flen),
+    _f("ref_pci_initial_forces")(P(spos4), P(svel4), P(dens), P(nrm4), P(fo), i(n), f(mu), f(sigma), P(flen),
                                  P(flist), f(visc_lapl), f(st_main), f(st_term), f(h_def), f(m_def), f(rho_def),
                                  i(local_size))
     return fo
@@ -162,7 +187,7 @@ def pci_predict_pos(spos4, svel4, fo4, fp4, dt, g, max_vel, limits, h_def, m_def
     pred = np.zeros((n, 4), np.float32)
     g4 = np.array([0.0, -g, 0.0, 0.0], np.float32)
     lim = np.array(list(limits) + [0.0], np.float32)
-    lib().ref_pci_predict_pos(P(spos4), P(svel4), P(fo4), P(fp4), P(pred), i(n), f(dt), P(g4), f(max_vel), P(lim),
+    _f("ref_pci_predict_pos")(P(spos4), P(svel4), P(fo4), P(fp4), P(pred), i(n), f(dt), P(g4), f(max_vel), P(lim),
                               f(h_def), f(m_def), f(rho_def))
     return pred
 
@@ -172,7 +197,7 @@ def pci_update_pressure(pred4, pres, delta, flist, flen, bpos4, bphi, blist, ble
     n = len(pred4)
     dv = np.zeros(n, np.float32)
     p = np.ascontiguousarray(pres, np.float32).copy()
-    lib().ref_pci_update_pressure(P(pred4), P(dv), P(p), i(n), f(delta), P(flen), P(flist), P(blist), P(blen),
+    _f("ref_pci_update_pressure")(P(pred4), P(dv), P(p), i(n), f(delta), P(flen), P(flist), P(blist), P(blen),
                                   P(bpos4), P(bphi), f(w_eval), f(h_def), f(m_def), f(rho_def), i(local_size))
     return dv, p
 
@@ -181,7 +206,7 @@ def pci_pressure_force(spos4, dens, pres, size, h, cps, flist, flen, bpos4, bphi
                        rho_def, local_size=64):
     n = len(spos4)
     fp = np.zeros((n, 4), np.float32)
-    lib().ref_pci_pressure_force(P(spos4), P(dens), P(pres), P(fp), i(n), f(size), f(h), i(cps), P(flen), P(flist),
+    _f("ref_pci_pressure_force")(P(spos4), P(dens), P(pres), P(fp), i(n), f(size), f(h), i(cps), P(flen), P(flist),
                                  P(blist), P(blen), P(bpos4), P(bphi), f(w_grad), f(h_def), f(m_def), f(rho_def),
                                  i(local_size))
     return fp
@@ -192,7 +217,7 @@ def pci_integrate(spos4, svel4, fo4, fp4, dt, g, max_vel, limits, h_def, m_def, 
     op, ov = np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32)
     g4 = np.array([0.0, -g, 0.0, 0.0], np.float32)
     lim = np.array(list(limits) + [0.0], np.float32)
-    lib().ref_pci_integrate(P(spos4), P(svel4), P(fo4), P(fp4), P(op), P(ov), i(n), f(dt), P(g4), f(max_vel),
+    _f("ref_pci_integrate")(P(spos4), P(svel4), P(fo4), P(fp4), P(op), P(ov), i(n), f(dt), P(g4), f(max_vel),
                             P(lim), f(h_def), f(m_def), f(rho_def))
     return op, ov
 
@@ -200,7 +225,7 @@ def pci_integrate(spos4, svel4, fo4, fp4, dt, g, max_vel, limits, h_def, m_def, 
 def boundary_phi(pos4, rho0, w_eval, phi_coeff, h_define):
     n = len(pos4)
     phi = np.zeros(n, np.float32)
-    lib().ref_boundary_phi(P(pos4), P(phi), i(n), f(rho0), f(w_eval), f(phi_coeff), f(h_define))
+    _f("ref_boundary_phi")(P(pos4), P(phi), i(n), f(rho0), f(w_eval), f(phi_coeff), f(h_define))
     return phi
 
 
@@ -212,7 +237,7 @@ def transform_particles(raw4, rot3x4, lin, ang):
     cm = np.array([r[0, 3], r[1, 3], r[2, 3], 1.0], np.float32)
     li = np.array(list(lin)[:3] + [0.0], np.float32)
     an = np.array(list(ang)[:3] + [0.0], np.float32)
-    lib().ref_transform_particles(P(raw4), P(out), P(vel), P(m[0]), P(m[1]), P(m[2]), P(li), P(an), P(cm), i(n))
+    _f("ref_transform_particles")(P(raw4), P(out), P(vel), P(m[0]), P(m[1]), P(m[2]), P(li), P(an), P(cm), i(n))
     return out, vel
 
 
@@ -221,7 +246,7 @@ def fluid_force(bpos4, bphi, fpos4, fdens, fpres, intervals, mass, spiky_grad, s
     n = len(bpos4)
     force, torque = np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32)
     c4 = np.array(list(center)[:3] + [1.0], np.float32)
-    lib().ref_fluid_force(P(bpos4), P(bphi), P(fpos4), P(fdens), P(fpres), P(intervals), f(mass), f(spiky_grad),
+    _f("ref_fluid_force")(P(bpos4), P(bphi), P(fpos4), P(fdens), P(fpres), P(intervals), f(mass), f(spiky_grad),
                           f(size), f(h), i(cps), i(n), P(force), P(torque), P(c4), P(fvel4), P(bvel4), f(visc_lapl),
                           f(h_define))
     return force, torque
@@ -231,7 +256,7 @@ def bilateral_filter(depth):
     """kernels/bilateral.cl over a (height, width) float32 image."""
     img = np.ascontiguousarray(depth, np.float32)
     out = np.zeros_like(img)
-    lib().ref_bilateral_filter(P(img), P(out), i(img.shape[1]), i(img.shape[0]))
+    _f("ref_bilateral_filter")(P(img), P(out), i(img.shape[1]), i(img.shape[0]))
     return out
 
 
@@ -239,18 +264,18 @@ def curvature_flow(depth, inv_proj_x, inv_proj_y):
     """kernels/curvatureflow.cl over a (height, width) float32 image."""
     img = np.ascontiguousarray(depth, np.float32)
     out = np.zeros_like(img)
-    lib().ref_curvature_flow(P(img), P(out), i(img.shape[1]), i(img.shape[0]), f(inv_proj_x), f(inv_proj_y))
+    _f("ref_curvature_flow")(P(img), P(out), i(img.shape[1]), i(img.shape[0]), f(inv_proj_x), f(inv_proj_y))
     return out
 
 
 def load_obj(path):
     """ModelMesh(path): (vertices (n, 3) float32, indices (m,) uint32 holding its 16-bit values)."""
     nv, ni = C.c_int(), C.c_int()
-    if lib().ref_load_obj(path.encode(), None, 0, None, 0, C.byref(nv), C.byref(ni)) != 0:
+    if _f("ref_load_obj")(path.encode(), None, 0, None, 0, C.byref(nv), C.byref(ni)) != 0:
         raise RuntimeError("ModelMesh could not load " + path)
     v = np.zeros((nv.value, 3), np.float32)
     ix = np.zeros(ni.value, np.uint32)
-    lib().ref_load_obj(path.encode(), P(v), nv, P(ix), ni, C.byref(nv), C.byref(ni))
+    _f("ref_load_obj")(path.encode(), P(v), nv, P(ix), ni, C.byref(nv), C.byref(ni))
     return v, ix
 
 
@@ -258,18 +283,18 @@ def voxelize(vertices3, indices, spacing, precision):
     """vx_voxelize as Model::surface_sampling calls it: (n, 4) float32 output vertices."""
     v = np.ascontiguousarray(vertices3, np.float32)
     ix = np.ascontiguousarray(indices, np.uint32)
-    n = lib().ref_voxelize(P(v), i(len(v)), P(ix), i(len(ix)), f(spacing), f(precision), None, i(0))
+    n = _f("ref_voxelize")(P(v), i(len(v)), P(ix), i(len(ix)), f(spacing), f(precision), None, i(0))
     out = np.zeros((n, 4), np.float32)
-    lib().ref_voxelize(P(v), i(len(v)), P(ix), i(len(ix)), f(spacing), f(precision), P(out), i(n))
+    _f("ref_voxelize")(P(v), i(len(v)), P(ix), i(len(ix)), f(spacing), f(precision), P(out), i(n))
     return out
 
 
 def icosphere(radius, level):
     nv, ni = C.c_int(), C.c_int()
-    lib().ref_icosphere(f(radius), C.c_uint(level), None, 0, None, 0, C.byref(nv), C.byref(ni))
+    _f("ref_icosphere")(f(radius), C.c_uint(level), None, 0, None, 0, C.byref(nv), C.byref(ni))
     v = np.zeros((nv.value, 3), np.float32)
     ix = np.zeros(ni.value, np.uint32)
-    lib().ref_icosphere(f(radius), C.c_uint(level), P(v), nv, P(ix), ni, C.byref(nv), C.byref(ni))
+    _f("ref_icosphere")(f(radius), C.c_uint(level), P(v), nv, P(ix), ni, C.byref(nv), C.byref(ni))
     return v, ix
 
 

@@ -102,6 +102,40 @@ template <class R> inline V3<R> normalize(V3<R> a) {
     return {a.x / l, a.y / l, a.z / l};
 }
 template <class R> inline R pown(R x, int n) { R r = x; for (int k = 1; k < n; ++k) r = r * x; return r; }
+
+/* kernels/monaghan_kernels.h:7-47, the Monaghan cubic spline the reference selects when its
+ * programs are built without USE_MULLER_KERNELS (kernels/kernels.h:8-37).  M_PI_F, pown and
+ * INV as the kernel text has them, left to right; hd = SUPPORT_RADIUS (the -D constant). */
+constexpr float kPiF = 3.14159265358979323846f;
+template <class R> inline R mon_eval(R hd) { return R(1.0f) / (R(kPiF) * pown(hd, 3)); }
+template <class R> inline R mon_grad(R hd) { return R(-3.0f) / (R(kPiF) * pown(hd, 4)); }
+template <class R> inline R w_monaghan(R r, R h, R hd) {
+    if (r <= h) return mon_eval(hd) * ((R(1.0f) - R(1.5f) * pown(r / h, 2)) + R(0.75f) * pown(r / h, 3));
+    if (r <= R(2.0f) * h) return (mon_eval(hd) * R(0.25f)) * pown(R(2.0f) - r / h, 3);
+    return R(0);
+}
+template <class R> inline V3<R> grad_w_monaghan(V3<R> r, R rn, R h, R hd) {
+    const R g = mon_grad(hd);
+    if (rn <= h) {
+        const R c = R(0.75f) * (rn / pown(h, 2));   /* subtracted from every component */
+        const R ih = R(1.0f) / h;
+        return {(g * r.x) * ih - c, (g * r.y) * ih - c, (g * r.z) * ih - c};
+    }
+    if (rn <= R(2.0f) * h) {
+        const R ir = R(1.0f) / rn, q = pown(R(2.0f) - rn / h, 2);
+        return {(((g * r.x) * R(0.25f)) * ir) * q, (((g * r.y) * R(0.25f)) * ir) * q,
+                (((g * r.z) * R(0.25f)) * ir) * q};
+    }
+    return {r.x * R(0), r.y * R(0), r.z * R(0)};
+}
+template <class R> inline R lapl_w_monaghan(R rn, R h, R hd) {
+    const R l = R(3.0f) * mon_grad(hd);
+    if (rn <= h) return l * (R(1.0f) / h - R(1.5f) * (rn / pown(h, 2)));
+    if (rn <= R(2.0f) * h)
+        return l * (((R(1.0f) / (R(0.25f) * rn)) * pown(R(2.0f) - rn / h, 2) - R(1.0f) / rn) +
+                    rn / (R(4.0f) * pown(h, 2)));
+    return R(0);
+}
 /* OpenCL C spec: clamp = fmin(fmax(x, lo), hi); max(x, y) = (x < y) ? y : x */
 template <class R> inline R clampf(R x, R lo, R hi) { return std::fmin(std::fmax(x, lo), hi); }
 template <class R> inline R clmax(R x, R y) { return x < y ? y : x; }
@@ -196,6 +230,7 @@ struct Oracle : OracleBase {
     OrcConfig cfg;
     int N = 0, NB = 0, cap = 50;
     bool compat;
+    bool mon;   /* COMPAT with the Monaghan kernels (OrcConfig::kernels) */
     /* derived constants (reference host code restated) */
     R dt, vmax, rho0, rho0_def, mu, sigma, kgas, g;
     R mass, mass_def, h, h_def, h_list;          /* h_def: SUPPORT_RADIUS -D; h_list: CELL_SIZE -D */
@@ -218,6 +253,7 @@ struct Oracle : OracleBase {
 
     explicit Oracle(const OrcConfig& c) : cfg(c) {
         compat = cfg.mode == 0;
+        mon = compat && cfg.kernels == 1;
         cap = cfg.neigh_cap > 0 ? cfg.neigh_cap : 50;
         derive();
     }
@@ -428,14 +464,14 @@ struct Oracle : OracleBase {
                 int j = nlist[(size_t)k * N + i];
                 V3<R> d = pi - ld(pos_s, j);
                 R rr = compat ? length(d) : dot(d, d);
-                di += pown(pown(h, 2) - rr, 3);
+                di += mon ? w_monaghan(rr, h, h_def) : pown(pown(h, 2) - rr, 3);
             }
             di *= poly6_eval * mass;
             for (int k = 0; k < sblen[i]; ++k) {
                 int j = sblist[(size_t)k * N + i];
                 V3<R> d = pi - ld(bpos_s, j);
                 R rr = compat ? length(d) : dot(d, d);
-                bdi += pown(pown(h, 2) - rr, 3) * bphi_s[j];
+                bdi += (mon ? w_monaghan(rr, h, h_def) : pown(pown(h, 2) - rr, 3)) * bphi_s[j];
             }
             di += poly6_eval * bdi;
             density[i] = di;
@@ -453,6 +489,10 @@ struct Oracle : OracleBase {
             for (int k = 0; k < nlen[i]; ++k) {
                 int j = nlist[(size_t)k * N + i];
                 V3<R> r = pi - ld(pos_s, j);
+                if (mon) {
+                    n += grad_w_monaghan(r, dot(r, r), H, H) / density[j];
+                    continue;
+                }
                 R s = pown(pown(H, 2) - dot(r, r), 2);
                 n += (r * s) / density[j];
             }
@@ -546,12 +586,12 @@ struct Oracle : OracleBase {
             for (int k = 0; k < nlen[i]; ++k) {
                 int j = nlist[(size_t)k * N + i];
                 V3<R> r = pi - ld(pos_s, j);
-                di += pown(pown(H, 2) - dot(r, r), 3);
+                di += mon ? w_monaghan(dot(r, r), H, H) : pown(pown(H, 2) - dot(r, r), 3);
             }
             for (int k = 0; k < sblen[i]; ++k) {
                 int j = sblist[(size_t)k * N + i];
                 V3<R> r = pi - ld(bpos_s, j);
-                bdi += pown(pown(H, 2) - dot(r, r), 3) * bphi_s[j];
+                bdi += (mon ? w_monaghan(dot(r, r), H, H) : pown(pown(H, 2) - dot(r, r), 3)) * bphi_s[j];
             }
             density[i] = default_eval * ((di * mass_def) + bdi);
         }
@@ -571,7 +611,7 @@ struct Oracle : OracleBase {
                 R dj = density[j];
                 V3<R> r = pi - pj;
                 R rn = length(r);
-                fv += (vj - vi) * ((H - rn) / dj);
+                fv += (vj - vi) * ((mon ? lapl_w_monaghan(rn, H, H) : H - rn) / dj);
                 fcu += (ni - nj) * st_corr(rho0_def, di, dj);
                 fco += (normalize(r) * st_kernel(rn, H, st_term)) * st_corr(rho0_def, di, dj);
             }
@@ -608,14 +648,14 @@ struct Oracle : OracleBase {
                 int j = nlist[(size_t)k * N + i];
                 V3<R> r = pi - ld(pos_pred, j);
                 R r2 = dot(r, r);
-                if (compat || r2 < H2) pd += pown(pown(H, 2) - r2, 3);
+                if (compat || r2 < H2) pd += mon ? w_monaghan(r2, H, H) : pown(pown(H, 2) - r2, 3);
             }
             pd *= default_eval * mass_def;
             for (int k = 0; k < sblen[i]; ++k) {
                 int j = sblist[(size_t)k * N + i];
                 V3<R> r = pi - ld(bpos_s, j);
                 R r2 = dot(r, r);
-                if (compat || r2 < H2) pdb += pown(pown(H, 2) - r2, 3) * bphi_s[j];
+                if (compat || r2 < H2) pdb += (mon ? w_monaghan(r2, H, H) : pown(pown(H, 2) - r2, 3)) * bphi_s[j];
             }
             pdb *= default_eval;
             R dv = clmax(R(0), pd + pdb - rho0_def);
@@ -636,14 +676,17 @@ struct Oracle : OracleBase {
                 int j = nlist[(size_t)k * N + i];
                 V3<R> r = pi - ld(pos_s, j);
                 R l = length(r);
-                if (l >= R(1e-5f)) fp += (C + pressure[j] / pown(density[j], 2)) * ((r * (R(1) / l)) * pown(H - l, 2));
+                if (l >= R(1e-5f))
+                    fp += (C + pressure[j] / pown(density[j], 2)) *
+                          (mon ? grad_w_monaghan(r, l, H, H) : (r * (R(1) / l)) * pown(H - l, 2));
             }
             fp = fp * ((-pown(mass_def, 2)) * pressure_grad);
             for (int k = 0; k < sblen[i]; ++k) {
                 int j = sblist[(size_t)k * N + i];
                 V3<R> r = pi - ld(bpos_s, j);
                 R l = length(r);
-                fpb += (bphi_s[j] * (R(2) * C)) * ((r * (R(1) / l)) * pown(H - l, 2));
+                fpb += (bphi_s[j] * (R(2) * C)) *
+                       (mon ? grad_w_monaghan(r, l, H, H) : (r * (R(1) / l)) * pown(H - l, 2));
             }
             fpb = fpb * ((-mass_def) * pressure_grad);
             st(f_press, i, fp + fpb, R(0));
@@ -722,7 +765,7 @@ struct Oracle : OracleBase {
                         for (auto it = lo; it != cells.end() && it->first == id; ++it) {
                             V3<R> r = pi - ld(bpos, b.origin + it->second);
                             R r2 = dot(r, r);
-                            if (r2 < H2) del += pown(pown(H, 2) - r2, 3);
+                            if (r2 < H2) del += mon ? w_monaghan(r2, H, H) : pown(pown(H, 2) - r2, 3);
                         }
                     }
                     bphi[i] = (rho0 / (del * boundary_eval)) / R(cfg.phi_coeff);
@@ -737,7 +780,7 @@ struct Oracle : OracleBase {
                 for (int jj = 0; jj < b.count; ++jj) {
                     V3<R> r = pi - ld(bpos, b.origin + jj);
                     R r2 = dot(r, r);
-                    if (r2 < H2) del += pown(pown(H, 2) - r2, 3);
+                    if (r2 < H2) del += mon ? w_monaghan(r2, H, H) : pown(pown(H, 2) - r2, 3);
                 }
                 bphi[i] = (rho0 / (del * boundary_eval)) / R(cfg.phi_coeff);
             }

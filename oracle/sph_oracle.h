@@ -48,6 +48,7 @@ typedef struct OrcConfig {
     float container[3];    /* set_rect_limits(w, h, d) */
     int relax_on_add;      /* PCISPH: relaxation step + v:=0 after set_fluid */
     int threads;           /* OpenMP threads (0 = runtime default) */
+    int kernels;           /* 0 = Mueller (USE_MULLER_KERNELS, the reference's build), 1 = Monaghan (COMPAT) */
 } OrcConfig;
 
 enum {

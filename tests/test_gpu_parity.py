@@ -196,3 +196,61 @@ def test_pcisph_graph_step_matches_oracle(gpu_lib):
     assert ctx.get("PCI_ITERS")[0] == orc.get("PCI_ITERS")[0]
     assert_close("pos", ctx.get("POS"), orc.get("POS"), 4, rtol=1e-5)
     assert ctx.device_flags() & capi.FLAGS["TIMEOUT"] == 0
+
+
+def test_monaghan_wcsph_stages_match_oracle(gpu_lib):
+    """COMPAT with the Monaghan kernels (sph_params.kernels, kernels/monaghan_kernels.h:7-47 at
+    the call sites of kernels/kernels.h): boundary Psi, density and normals against the oracle
+    (pinned bit for bit to the reference's Monaghan build on the CPU)."""
+    fluid, bodies, container = scene()
+    for lists in (0, 1):
+        ctx, orc = make_pair(small_params(0, 0, neighbor_mode=lists, kernels=capi.SPH_KERNELS_MONAGHAN), fluid,
+                             bodies, container)
+        assert_close("phi", ctx.get("BPHI_SORTED"), orc.get("BPHI_SORTED"))
+        check_grid(ctx, orc)
+        check_lists(ctx, orc)
+        ctx.stage("WC_DENSITY")
+        orc.stage("WC_DENSITY")
+        assert_close("density", ctx.get("DENSITY"), orc.get("DENSITY"))
+        orc.set("DENSITY", ctx.get("DENSITY"))
+        ctx.stage("NORMALS")
+        orc.stage("NORMALS")
+        assert_close("normal", ctx.get("NORMAL"), orc.get("NORMAL"), 4)
+        ctx.close()
+
+
+def test_monaghan_pcisph_stages_match_oracle(gpu_lib):
+    fluid, bodies, container = scene()
+    ctx, orc = make_pair(small_params(1, 0, pcisph_max_iterations=3, kernels=capi.SPH_KERNELS_MONAGHAN), fluid,
+                         bodies, container)
+    check_grid(ctx, orc)
+    check_lists(ctx, orc)
+    for s in ("PCI_INIT_DENSITY", "NORMALS", "PCI_INIT_FORCES"):
+        ctx.stage(s)
+        orc.stage(s)
+        if s == "PCI_INIT_DENSITY":
+            assert_close("density", ctx.get("DENSITY"), orc.get("DENSITY"))
+            orc.set("DENSITY", ctx.get("DENSITY"))
+        elif s == "NORMALS":
+            assert_close("normal", ctx.get("NORMAL"), orc.get("NORMAL"), 4)
+            orc.set("NORMAL", ctx.get("NORMAL"))
+    assert_close("f_other", ctx.get("FORCE_OTHER"), orc.get("FORCE_OTHER"), 4)
+    orc.set("FORCE_OTHER", ctx.get("FORCE_OTHER"))
+    ctx.stage("PCI_PREDICT")
+    orc.stage("PCI_PREDICT")
+    orc.set("POS_PRED", ctx.get("POS_PRED"))
+    p0 = (50.0 * (1.0 + np.cos(np.arange(ctx.particle_count())))).astype(np.float32)
+    for o in (ctx, orc):
+        o.set("PRESSURE", p0)
+        o.stage("PCI_UPDATE_PRESSURE")
+    assert_close("pressure (update alone)", ctx.get("PRESSURE"), orc.get("PRESSURE"))
+    orc.set("PRESSURE", ctx.get("PRESSURE"))
+    ctx.stage("PCI_PRESSURE_FORCE")
+    orc.stage("PCI_PRESSURE_FORCE")
+    assert_close("f_press (alone)", ctx.get("FORCE_PRESSURE"), orc.get("FORCE_PRESSURE"), 4)
+    ctx.close()
+
+
+def test_monaghan_needs_compat():
+    with pytest.raises(capi.SphError):
+        capi.Context(small_params(0, 1, kernels=capi.SPH_KERNELS_MONAGHAN))

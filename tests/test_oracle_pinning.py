@@ -204,3 +204,79 @@ def test_boundary_transform_and_fluid_force_match_reference():
     assert np.linalg.norm(fsum) > 0
     assert np.allclose(of, fsum, rtol=1e-5, atol=1e-6 * np.abs(fsum).max())
     assert np.allclose(ot, tsum, rtol=1e-5, atol=1e-6 * np.abs(tsum).max())
+
+
+# ---- the Monaghan kernels (kernels/monaghan_kernels.h:7-47): the oracle with kernels = 1
+# against the reference's kernel files built without USE_MULLER_KERNELS
+
+def test_monaghan_boundary_phi_matches_reference():
+    o, sc = make(0, 0, kernels=1)
+    d = o.derived()
+    with rk.monaghan():
+        phi = rk.boundary_phi(f4(sc["boundary"]), 1000.0, d["boundary_eval"], 1.0, d["h_def"])
+    assert np.array_equal(phi, o.get("BPHI"))
+    o0, _ = make(0, 0)
+    assert not np.array_equal(phi, o0.get("BPHI"))   # the kernel family matters
+
+
+def test_monaghan_wcsph_density_and_normals_match_reference():
+    o, sc = make(0, 0, kernels=1)
+    d = o.derived()
+    check_grid_stages(o)
+    ps, fl, fn = f4(o.get("POS_SORTED")), c(o.get("NEIGH_LIST")), c(o.get("NEIGH_LEN"))
+    bp, bphi, bl, bn = f4(o.get("BPOS_SORTED")), c(o.get("BPHI_SORTED")), c(o.get("SB_NEIGH_LIST")), \
+        c(o.get("SB_NEIGH_LEN"))
+    o.stage("WC_DENSITY")
+    with rk.monaghan():
+        dens, pres = rk.wc_density_pressure(ps, fl, fn, bp, bphi, bl, bn, d["mass"], d["h"], 57142.857, 1000.0,
+                                            d["poly6_eval"], d["h_def"])
+    assert np.array_equal(dens, o.get("DENSITY")) and np.array_equal(pres, o.get("PRESSURE"))
+    phys_d = (1000.0 + 20.0 * np.sin(np.arange(len(ps)))).astype(np.float32)
+    o.set("DENSITY", phys_d)
+    o.stage("NORMALS")
+    with rk.monaghan():
+        nrm = rk.compute_normals(ps, phys_d, fl, fn, d["poly6_grad"], d["mass_def"], d["h_def"])
+    assert np.array_equal(nrm[:, :3], f4(o.get("NORMAL"))[:, :3])
+
+
+def test_monaghan_pcisph_stages_match_reference():
+    o, sc = make(1, 0, time_step=5e-4, max_vel=20.0, surface_tension=1.0, k_viscosity=0.01, pci_max_iter=3,
+                 kernels=1)
+    d = o.derived()
+    size, h, cps, _ = grid_args(o)
+    args = (d["h_def"], d["mass_def"], d["rest_density_def"])
+    check_grid_stages(o)
+    ps, sv, fl, fn = f4(o.get("POS_SORTED")), f4(o.get("VEL_SORTED")), c(o.get("NEIGH_LIST")), c(o.get("NEIGH_LEN"))
+    bp, bphi, bl, bn = f4(o.get("BPOS_SORTED")), c(o.get("BPHI_SORTED")), c(o.get("SB_NEIGH_LIST")), \
+        c(o.get("SB_NEIGH_LEN"))
+    with rk.monaghan():
+        o.stage("PCI_INIT_DENSITY")
+        dens = rk.pci_initial_density(ps, fl, fn, bp, bphi, bl, bn, d["default_eval"], *args)
+        assert np.array_equal(dens, o.get("DENSITY"))
+        o.stage("NORMALS")
+        nrm = rk.compute_normals(ps, dens, fl, fn, d["poly6_grad"], d["mass_def"], d["h_def"])
+        assert np.array_equal(nrm[:, :3], f4(o.get("NORMAL"))[:, :3])
+        # the oracle's normals carry w = 0; the kernel text's Monaghan gradient puts
+        # -0.75 r / h^2 into w as well, which no later pass reads
+        o.set("NORMAL", nrm)
+        o.stage("PCI_INIT_FORCES")
+        fo = rk.pci_initial_forces(ps, sv, dens, nrm, fl, fn, 0.01, 1.0, d["visc_lapl"], d["st_main"],
+                                   d["st_term"], *args)
+        assert np.array_equal(fo[:, :3], f4(o.get("FORCE_OTHER"))[:, :3])
+        # one loop iteration's passes on the oracle's inputs
+        o.set("FORCE_OTHER", fo)
+        lim = sc["container"]
+        fp = np.zeros_like(fo)
+        o.set("FORCE_PRESSURE", fp)
+        o.stage("PCI_PREDICT")
+        pred = rk.pci_predict_pos(ps, sv, fo, fp, 5e-4, 9.81, 20.0, lim, *args)
+        assert np.array_equal(pred[:, :3], f4(o.get("POS_PRED"))[:, :3])
+        pres0 = (50.0 * (1.0 + np.cos(np.arange(len(ps))))).astype(np.float32)
+        o.set("PRESSURE", pres0)
+        o.stage("PCI_UPDATE_PRESSURE")
+        dv, pres = rk.pci_update_pressure(pred, pres0.copy(), d["pci_delta"], fl, fn, bp, bphi, bl, bn,
+                                          d["default_eval"], *args)
+        assert np.array_equal(dv, o.get("DENS_VAR")) and np.array_equal(pres, o.get("PRESSURE"))
+        o.stage("PCI_PRESSURE_FORCE")
+        fpr = rk.pci_pressure_force(ps, dens, pres, size, h, cps, fl, fn, bp, bphi, bl, bn, d["spiky_grad"], *args)
+        assert np.array_equal(fpr[:, :3], f4(o.get("FORCE_PRESSURE"))[:, :3])
