@@ -11,14 +11,14 @@ from parity_util import make_pair
 pytestmark = pytest.mark.gpu
 
 
-def _stats_close(g, o, steps):
+def _stats_close(g, o, steps, dens_tol=2e-2):
     msg = "after %d steps: gpu %s oracle %s" % (steps, g, o)
     assert abs(g["kinetic"] - o["kinetic"]) <= 2e-2 * abs(o["kinetic"]) + 1e-9, msg
     assert abs(g["potential"] - o["potential"]) <= 1e-3 * abs(o["potential"]), msg
     for a in ("com_x", "com_y", "com_z"):
         assert abs(g[a] - o[a]) <= 1e-3, msg
     assert abs(g["mean_abs_density_error"] - o["mean_abs_density_error"]) <= \
-        2e-2 * o["mean_abs_density_error"] + 1e-4, msg
+        dens_tol * o["mean_abs_density_error"] + 1e-4, msg
     assert abs(g["mean_compression"] - o["mean_compression"]) <= 0.1 * o["mean_compression"] + 1e-4, msg
 
 
@@ -66,3 +66,21 @@ def test_dam_break_65k_full_length_rollout_statistics(gpu_lib):
     assert ctx.device_flags() & (capi.FLAGS["NAN"] | capi.FLAGS["TIMEOUT"]) == 0
     assert o["kinetic"] > 100.0   # the block has collapsed and is flowing
     _stats_close(g, o, 1000)
+
+
+def test_pcisph_cube_full_length_rollout_statistics(gpu_lib):
+    """The PCISPH scene at its full size and length: 358,400 particles in two 0.5 x 1.0 x 0.7 m
+    blocks around the static rotated cube, 500 steps of 5e-4 s (PHYSICS, 3..8 iterations, 1 %
+    tolerance).  The GPU's FP32 run against the FP64 oracle of the same step.  The oracle's own
+    FP32 and FP64 runs of this scene differ after 500 steps by 0.07 % in kinetic and 0.06 % in
+    potential energy, 0.1 mm in centre of mass and 3.1 % in the mean density error (which
+    follows the per-step iteration count of the pressure loop), so that statistic is held to
+    6 % here instead of 2 %."""
+    w = workloads.pcisph_cube(mode=capi.SPH_MODE_PHYSICS)
+    ctx, orc = make_pair(w["params"], w["fluid"], w["bodies"], w["container"], precision=1)
+    ctx.simulate(500)
+    orc.step(500)
+    g, o = ctx.stats(), orc.stats()
+    assert ctx.device_flags() & (capi.FLAGS["NAN"] | capi.FLAGS["TIMEOUT"]) == 0
+    assert o["kinetic"] > 1000.0   # both blocks have collapsed around the cube
+    _stats_close(g, o, 500, dens_tol=6e-2)
