@@ -251,6 +251,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.nlist = cv.take<int32_t>(cap * n); b.nlen = cv.take<int32_t>(n);
     b.sblist = cv.take<int32_t>(cap * n); b.sblen = cv.take<int32_t>(n);
     b.sort_ws = cv.take<char>(sph::sort_workspace_bytes((int)n, x->c.key_bits));
+    b.inc_ws = cv.take<char>(sph::sort_inc_workspace_bytes((int)n));
     b.braw = cv.take<float4>(nb); b.bpos = cv.take<float4>(nb); b.bvel = cv.take<float4>(nb);
     b.bpos_s = cv.take<float4>(nb);
     b.bphi = cv.take<float>(nb); b.bphi_s = cv.take<float>(nb);
@@ -355,8 +356,11 @@ int run_stage_impl(sph_ctx* x, int stage) {
         x->cur_mask = b.mask;
         break;
     case SPH_S_SORT:
-        sph::sort_pairs(s, b.keys, b.mask, b.keys_alt, b.mask_alt, x->N, c.key_bits, b.sort_ws, b.flags, x->num_sms,
-                        &b.keys_sorted, &b.mask_sorted);
+        /* the stable sort of the keys as an update of the last step's order */
+        sph::sort_pairs_incremental(s, b.keys, x->N, c.key_bits, b.keys_alt, b.mask_alt, b.inc_ws, b.sort_ws,
+                                    b.flags, x->num_sms);
+        b.keys_sorted = b.keys_alt;
+        b.mask_sorted = b.mask_alt;
         x->cur_keys = b.keys_sorted;
         x->cur_mask = b.mask_sorted;
         break;
@@ -448,7 +452,13 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
     const char* pre_names[] = {"boundary_sync", "k_hashes", "sort"};
     for (int k = 0; k < 3; ++k) {
         if (pre[k] == SPH_S_BOUNDARY_SYNC && !(x->NB > 0 && x->any_movable)) continue;
-        if ((rc = run_stage_impl(x, pre[k])) != SPH_OK) return rc;
+        if (pre[k] == SPH_S_HASHES) {
+            sph::launch_hashes(s, c, b.pos, x->N, b.keys, nullptr, b.tab, b.cell_prev, b.flags, bs, b.scenes,
+                               b.scene_of);
+            x->cur_keys = b.keys;
+        } else if ((rc = run_stage_impl(x, pre[k])) != SPH_OK) {
+            return rc;
+        }
         mark(x, pre_names[k]);
     }
     /* the SHUFFLE and CELL_INTERVALS stages in one pass */

@@ -35,7 +35,7 @@ __global__ void k_hashes(Const c0, const float4* __restrict__ pos, int n, uint32
     cell_of(c, p.x, p.y, p.z, cx, cy, cz);
     /* batched: the scene id above the Morton bits keeps every scene's range contiguous */
     keys[i] = (sid << c.scene_shift) | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
-    mask[i] = i;
+    if (mask) mask[i] = i;   /* the identity values of the stage API (the step's sort needs none) */
     if (!c.wrap) {
         /* PHYSICS grid clamps: report particles outside it (informational) */
         const float fx = floorf(__fdiv_rn(__fsub_rn(p.x, c.ox), c.cell));

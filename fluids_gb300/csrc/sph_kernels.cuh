@@ -29,6 +29,7 @@ struct Bufs {
     int32_t* noff;                         /* 27 linear neighbour-cell offsets (single-scene grid) */
     int32_t *nlist, *nlen, *sblist, *sblen;
     void* sort_ws;
+    void* inc_ws;                          /* the incremental sort's workspace (holds the last result) */
     /* boundary */
     float4 *braw, *bpos, *bvel, *bpos_s;
     float *bphi, *bphi_s;
@@ -65,6 +66,13 @@ int sort_passes(int key_bits);
 size_t sort_workspace_bytes(int n, int key_bits);
 void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t* v1, int n, int key_bits,
                 void* ws, unsigned* flags, int num_sms, uint32_t** kres, int32_t** vres);
+/* The stable sort of keys[0, n) (values: the indices) into kout / vout, computed as an update
+ * of the previous call's result kept in inc_ws (bytes: sort_inc_workspace_bytes(n), zeroed
+ * once before the first call; sort_ws: sort_workspace_bytes(n, key_bits)).  Same result as
+ * sort_pairs over (keys, identity) for every input. */
+size_t sort_inc_workspace_bytes(int n);
+void sort_pairs_incremental(cudaStream_t s, const uint32_t* keys, int n, int key_bits, uint32_t* kout,
+                            int32_t* vout, void* inc_ws, void* sort_ws, unsigned* flags, int num_sms);
 
 /* sph_grid.cu */
 /* scenes: the context's scene table (never null); scene_of: scene of each particle, or

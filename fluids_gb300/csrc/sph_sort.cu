@@ -74,8 +74,9 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_
  * together; per key and pass, the lanes holding the same digit add their count once. */
 constexpr int kHistItems = 8;
 __global__ void __launch_bounds__(kThreads) k_sort_hist(const uint32_t* __restrict__ keys, int n, int passes,
-                                                        uint32_t* __restrict__ hist) {
+                                                        uint32_t* __restrict__ hist, const unsigned* __restrict__ gate) {
     __shared__ uint32_t s_hist[4][256];
+    if (gate && *gate == 0u) return;   /* a sort that an earlier kernel found unnecessary */
     for (int t = threadIdx.x; t < 4 * 256; t += kThreads) (&s_hist[0][0])[t] = 0u;
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
                                                        int shift, int pass, int tiles,
                                                        const uint32_t* __restrict__ hist,
                                                        uint32_t* __restrict__ counters, uint32_t* __restrict__ status,
-                                                       unsigned* __restrict__ flags) {
+                                                       unsigned* __restrict__ flags, const unsigned* __restrict__ gate) {
     __shared__ uint32_t s_keys[kTile];
     __shared__ int32_t s_vals[kTile];
     __shared__ uint32_t s_whist[kWarps][256];
@@ -122,11 +123,16 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
     __shared__ uint32_t s_scan[kWarps];
     __shared__ uint32_t s_tile;
 
+    if (gate && *gate == 0u) return;   /* the whole grid leaves together */
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    /* a grid smaller than the tile count loops: each CTA takes tiles until none is left
+     * (a tile's look-back waits only on tiles taken before it, by CTAs that are running) */
+    for (;;) {
     if (tid == 0) s_tile = atomicAdd(&counters[pass], 1u);
     for (int t = tid; t < kWarps * 256; t += kThreads) (&s_whist[0][0])[t] = 0u;
     __syncthreads();
     const int tile = (int)s_tile;
+    if (tile >= tiles) return;
     const long long base = (long long)tile * kTile;
     const long long wbase = base + (long long)warp * (32 * kItems);
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -139,7 +145,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
         const long long idx = wbase + k * 32 + lane;
         const bool valid = idx < n;
         key[k] = valid ? __ldg(&kin[idx]) : 0xffffffffu;   /* tail keys sort last and are not written */
-        val[k] = valid ? __ldg(&vin[idx]) : 0;
+        val[k] = valid ? (vin ? __ldg(&vin[idx]) : (int32_t)idx) : 0;   /* no vin: the identity */
     }
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
@@ -211,6 +217,9 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
         kout[dest] = kk;
         vout[dest] = s_vals[s];
     }
+    if ((int)gridDim.x >= tiles) return;   /* one tile per CTA */
+    __syncthreads();                        /* the next tile reuses the shared arrays */
+    }
 }
 
 int sort_passes(int key_bits) { return key_bits <= 0 ? 0 : (key_bits + 7) / 8; }
@@ -221,29 +230,391 @@ size_t sort_workspace_bytes(int n, int key_bits) {
     return (size_t)(4 * 256 + 64) * 4 + (size_t)passes * sort_tiles(n) * 256 * 4;
 }
 
-void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t* v1, int n, int key_bits,
-                void* ws, unsigned* flags, int num_sms, uint32_t** kres, int32_t** vres) {
-    *kres = k0;
-    *vres = v0;
+/* gate: null, or a flag word an earlier kernel of the stream wrote; every kernel of the sort
+ * leaves at once while it is 0.  v0 may be null for identity values. */
+static void sort_pairs_impl(cudaStream_t s, const uint32_t* k0, const int32_t* v0, uint32_t* k1, int32_t* v1,
+                            uint32_t* k2, int32_t* v2, int n, const unsigned* gate, int key_bits, void* ws,
+                            unsigned* flags, int num_sms, uint32_t** kres, int32_t** vres) {
     const int passes = sort_passes(key_bits);
-    if (n <= 1 || passes == 0) return;
     const int tiles = sort_tiles(n);
     uint32_t* hist = reinterpret_cast<uint32_t*>(ws);
     uint32_t* counters = hist + 4 * 256;
     uint32_t* status = counters + 64;
     cudaMemsetAsync(ws, 0, sort_workspace_bytes(n, key_bits), s);
-    int hblocks = min((n + kThreads * kHistItems - 1) / (kThreads * kHistItems), 4 * num_sms);
+    /* a gated sort usually leaves at once: its grids are one wave of looping CTAs */
+    int hblocks = min((n + kThreads * kHistItems - 1) / (kThreads * kHistItems), (gate ? 1 : 4) * num_sms);
     if (hblocks < 1) hblocks = 1;
-    k_sort_hist<<<hblocks, kThreads, 0, s>>>(k0, n, passes, hist);
-    uint32_t *ki = k0, *ko = k1;
-    int32_t *vi = v0, *vo = v1;
+    const int sblocks = gate ? min(tiles, 2 * num_sms) : tiles;
+    k_sort_hist<<<hblocks, kThreads, 0, s>>>(k0, n, passes, hist, gate);
+    /* pass p reads the previous pass's output and writes (k1, v1) or (k2, v2) in turn */
+    const uint32_t* ki = k0;
+    const int32_t* vi = v0;
     for (int p = 0; p < passes; ++p) {
-        k_onesweep<<<tiles, kThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, p, tiles, hist, counters, status, flags);
-        uint32_t* tk = ki; ki = ko; ko = tk;
-        int32_t* tv = vi; vi = vo; vo = tv;
+        uint32_t* ko = (p & 1) ? k2 : k1;
+        int32_t* vo = (p & 1) ? v2 : v1;
+        k_onesweep<<<sblocks, kThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, p, tiles, hist, counters, status, flags,
+                                                gate);
+        ki = ko;
+        vi = vo;
     }
-    *kres = ki;
-    *vres = vi;
+    *kres = const_cast<uint32_t*>(ki);
+    *vres = const_cast<int32_t*>(vi);
+}
+
+void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t* v1, int n, int key_bits,
+                void* ws, unsigned* flags, int num_sms, uint32_t** kres, int32_t** vres) {
+    *kres = k0;
+    *vres = v0;
+    if (n <= 1 || sort_passes(key_bits) == 0) return;
+    sort_pairs_impl(s, k0, v0, k1, v1, k0, v0, n, nullptr, key_bits, ws, flags, num_sms, kres, vres);
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Incremental stable sort of a step's cell keys against the previous step's sorted keys.
+ *
+ * The fluid arrays stay in the previous step's sorted order between steps, so particle i
+ * of this step was sorted particle i of the last one and prev[i] is its key then.  Call a
+ * particle "stayed" when its key did not change (keys[i] == prev[i]) and "moved" otherwise.
+ * prev is non-decreasing, so the stayed particles are already in (key, index) order, and
+ * the stable sort of all keys is their merge, by (key, index), with the moved ones.  That
+ * holds for any non-decreasing prev.  prev is the workspace's own copy of the last result
+ * (written beside the output, so that writes to the output from outside cannot unsort it).
+ *
+ *   k_inc_flags  per tile of kIncTile positions: the moved flags as ballot words (bits) and
+ *                the tile's count of moved particles.
+ *   k_inc_place  per moved particle (k, i): p = the first position whose (prev[p], p) is
+ *                not below (k, i), by a binary search over a table of each tile's first
+ *                prev key and then within the tile.  (k, i, p) goes to bucket p / kIncTile.
+ *                The stayed particles at positions [t kIncTile, (t + 1) kIncTile) are all
+ *                above the moved particles of the buckets below t and below those of the
+ *                buckets above t, so only bucket t's need comparing with them.
+ *   k_inc_merge  per tile t: the bucket's particles ranked among themselves in shared
+ *                memory; a moved particle goes to (stayed before p) + (moved particles of the
+ *                buckets below t) + its rank, a stayed particle of stayed rank a to a + (moved
+ *                particles of the buckets below t) + (bucket particles below it).
+ * A bucket holds kIncBucket particles.  When one overflows, or there is no previous result
+ * (the first call), the overflow word opens the gated full onesweep sort of all keys (its
+ * kernels read the word and leave at once while it is 0) and k_inc_merge only keeps that
+ * result as prev.  Moved particles are 1-2 % of a flowing scene per step: the passes over
+ * all particles then read 8 bytes and write 12 bytes per particle.
+ * ------------------------------------------------------------------------------------- */
+namespace {
+constexpr int kIncItems = 8;
+constexpr int kIncTile = kThreads * kIncItems;   /* 2048 positions = 64 ballot words */
+constexpr int kIncShift = 11;
+constexpr int kIncWords = kIncTile / 32;
+constexpr int kIncBucket = 256;                  /* moved particles per merge tile before overflow */
+
+struct IncLayout {
+    size_t valid, prev, first, bits, list, store, zero, over, lcount, done, bcnt, tcnt, tpre, boff, vscr, total,
+        zero_bytes;
+    int tiles, words;
+    IncLayout(int n) {
+        const size_t nn = (size_t)(n > 0 ? n : 1);
+        tiles = (int)((nn + kIncTile - 1) / kIncTile);
+        words = (int)((nn + 31) / 32);
+        size_t off = 0;
+        auto take = [&](size_t bytes) {
+            const size_t at = off;
+            off = (off + bytes + 255) & ~size_t(255);
+            return at;
+        };
+        valid = take(4);
+        prev = take(4 * nn);
+        first = take(4 * (size_t)tiles);
+        bits = take(4 * (size_t)words);
+        list = take(4 * nn);
+        store = take(16 * (size_t)tiles * kIncBucket);
+        /* zeroed by every call: the overflow word, the list length, the count of finished
+         * placing CTAs and the bucket counts (the other arrays are written whole) */
+        zero_bytes = 4 * (3 + (size_t)tiles);
+        zero = take(zero_bytes);
+        over = zero;
+        lcount = over + 4;
+        done = lcount + 4;
+        bcnt = done + 4;
+        tcnt = take(4 * (size_t)tiles);
+        tpre = take(4 * (size_t)tiles);
+        boff = take(4 * (size_t)tiles);
+        vscr = take(4 * nn);   /* the gated full sort's second value array */
+        total = off;
+    }
+};
+
+/* a key and its index, ordered by key then index */
+__device__ __forceinline__ bool pair_less(uint32_t ka, int32_t ia, uint32_t kb, int32_t ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kThreads) k_inc_flags(const uint32_t* __restrict__ keys,
+                                                        const uint32_t* __restrict__ prev, int n,
+                                                        const unsigned* __restrict__ valid,
+                                                        uint32_t* __restrict__ bits, uint32_t* __restrict__ tcnt,
+                                                        unsigned* __restrict__ over, int32_t* __restrict__ list,
+                                                        uint32_t* __restrict__ lcount) {
+    __shared__ uint32_t s_wcnt[kWarps];
+    __shared__ uint32_t s_base;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long wbase = ((long long)blockIdx.x << kIncShift) + (long long)warp * (32 * kIncItems);
+    const bool have_prev = *valid != 0u;
+    if (!have_prev && blockIdx.x == 0 && tid == 0) *over = 1u;   /* no previous result: a full sort */
+    uint32_t key[kIncItems], old[kIncItems];
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) {
+        const long long idx = wbase + k * 32 + lane;
+        key[k] = idx < n ? __ldg(&keys[idx]) : 0u;
+        old[k] = idx < n ? __ldg(&prev[idx]) : 0u;
+    }
+    uint32_t cnt = 0, word[kIncItems];
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) {
+        const long long w0 = wbase + k * 32;
+        const bool moved = w0 + lane < n && (!have_prev || key[k] != old[k]);
+        word[k] = __ballot_sync(0xffffffffu, moved);
+        if (lane == 0 && w0 < n) bits[w0 >> 5] = word[k];
+        cnt += (uint32_t)__popc(word[k]);
+    }
+    if (lane == 0) s_wcnt[warp] = cnt;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t total = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) total += s_wcnt[w];
+        tcnt[blockIdx.x] = total;
+        /* the moved positions go to a list in any order (one atomic per tile): the places
+         * are computed from (key, index) alone */
+        s_base = have_prev && total ? atomicAdd(lcount, total) : 0u;
+    }
+    __syncthreads();
+    if (!have_prev) return;
+    uint32_t run = s_base;
+    for (int w = 0; w < warp; ++w) run += s_wcnt[w];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) {
+        if ((word[k] >> lane) & 1u) list[run + (uint32_t)__popc(word[k] & lt)] = (int32_t)(wbase + k * 32 + lane);
+        run += (uint32_t)__popc(word[k]);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_inc_place(const uint32_t* __restrict__ keys,
+                                                        const int32_t* __restrict__ list,
+                                                        const uint32_t* __restrict__ lcount,
+                                                        const uint32_t* __restrict__ prev,
+                                                        const uint32_t* __restrict__ first, int n, int tiles,
+                                                        const unsigned* __restrict__ valid,
+                                                        uint32_t* __restrict__ bcnt, int4* __restrict__ store,
+                                                        unsigned* __restrict__ over, unsigned* __restrict__ done,
+                                                        const uint32_t* __restrict__ tcnt,
+                                                        uint32_t* __restrict__ tpre, uint32_t* __restrict__ boff) {
+    __shared__ uint32_t s_scan[kWarps];
+    __shared__ bool s_last;
+    if (*valid == 0u) return;   /* no previous result: the full sort runs */
+    const int m = (int)*lcount;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const int i = __ldg(&list[r]);
+        const uint32_t k = __ldg(&keys[i]);
+        /* the number of tiles whose first (prev, position) is below (k, i) ... */
+        int lo = 0, hi = tiles;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (pair_less(__ldg(&first[mid]), mid << kIncShift, k, i)) lo = mid + 1;
+            else hi = mid;
+        }
+        /* ... puts p after the first position of tile lo - 1 and at most at tile lo's first */
+        int plo = lo > 0 ? ((lo - 1) << kIncShift) : 0;
+        int phi = lo > 0 ? min(lo << kIncShift, n) : 0;
+        while (plo < phi) {
+            const int mid = (plo + phi) >> 1;
+            if (pair_less(__ldg(&prev[mid]), mid, k, i)) plo = mid + 1;
+            else phi = mid;
+        }
+        const int b = min(plo >> kIncShift, tiles - 1);
+        const uint32_t slot = atomicAdd(&bcnt[b], 1u);
+        if (slot < (uint32_t)kIncBucket) store[(size_t)b * kIncBucket + slot] = make_int4((int)k, i, plo, 0);
+        else *over = 1u;
+    }
+    /* the last CTA to finish turns the tile counts and bucket counts into exclusive
+     * prefixes (tpre, boff) for the merge */
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int per = (tiles + kThreads - 1) / kThreads;
+    const int t0 = threadIdx.x * per;
+    uint32_t a = 0, c = 0;
+    for (int t = t0; t < min(t0 + per, tiles); ++t) {
+        a += __ldcg(&tcnt[t]);
+        c += __ldcg(&bcnt[t]);
+    }
+    uint32_t ra = block_exclusive_scan_256(a, s_scan);
+    uint32_t rc = block_exclusive_scan_256(c, s_scan);
+    for (int t = t0; t < min(t0 + per, tiles); ++t) {
+        tpre[t] = ra;
+        boff[t] = rc;
+        ra += __ldcg(&tcnt[t]);
+        rc += __ldcg(&bcnt[t]);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_inc_merge(const uint32_t* __restrict__ keys, int n,
+                                                        const uint32_t* __restrict__ bits,
+                                                        const uint32_t* __restrict__ tcnt,
+                                                        const uint32_t* __restrict__ tpre,
+                                                        const uint32_t* __restrict__ boff,
+                                                        const uint32_t* __restrict__ bcnt,
+                                                        const int4* __restrict__ store,
+                                                        const unsigned* __restrict__ over,
+                                                        uint32_t* __restrict__ kout, int32_t* __restrict__ vout,
+                                                        uint32_t* __restrict__ prev, uint32_t* __restrict__ first,
+                                                        unsigned* __restrict__ valid) {
+    __shared__ uint32_t s_k[kIncBucket], s_sk[kIncBucket];
+    __shared__ int32_t s_i[kIncBucket], s_si[kIncBucket], s_p[kIncBucket];
+    __shared__ uint32_t s_word[kIncWords], s_wpre[kIncWords];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int t = blockIdx.x;
+    const long long tbase = (long long)t << kIncShift;
+    const long long tend = min(tbase + kIncTile, (long long)n);
+    if (t == 0 && tid == 0) *valid = 1u;
+    if (*over != 0u) {
+        /* the gated full sort wrote kout and vout (a single pair needs no sort): keep its
+         * keys as the next call's prev */
+        if (n == 1 && tid == 0) {
+            kout[0] = __ldg(&keys[0]);
+            vout[0] = 0;
+        }
+        __syncthreads();
+        for (long long j = tbase + tid; j < tend; j += kThreads) {
+            const uint32_t k = kout[j];
+            prev[j] = k;
+            if ((j & (kIncTile - 1)) == 0) first[j >> kIncShift] = k;
+        }
+        return;
+    }
+    /* this tile's keys and moved words first (their loads in flight together) */
+    const long long wbase = tbase + (long long)warp * (32 * kIncItems);
+    uint32_t key[kIncItems], word[kIncItems];
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) {
+        const long long idx = wbase + k * 32 + lane;
+        key[k] = idx < n ? __ldg(&keys[idx]) : 0u;
+        word[k] = wbase + k * 32 < n ? __ldg(&bits[(wbase + k * 32) >> 5]) : 0u;
+    }
+    /* moved particles before this tile, and bucket particles of the buckets below it */
+    const uint32_t tile_pre = __ldg(&tpre[t]), off = __ldg(&boff[t]), tile_moved = __ldg(&tcnt[t]);
+    /* moved particles before each word of the tile */
+    uint32_t wc = 0;
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) wc += (uint32_t)__popc(word[k]);
+    if (lane == 0) s_wpre[warp] = wc;   /* per-warp totals, scanned below */
+    const int c = min((int)__ldg(&bcnt[t]), kIncBucket);   /* no overflow: at most kIncBucket */
+    for (int e = tid; e < c; e += kThreads) {
+        const int4 v = __ldg(&store[(size_t)t * kIncBucket + e]);
+        s_k[e] = (uint32_t)v.x;
+        s_i[e] = v.y;
+        s_p[e] = v.z;
+    }
+    __syncthreads();
+    uint32_t wrun = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) wrun += w < warp ? s_wpre[w] : 0u;
+    __syncthreads();   /* every warp has read the per-warp totals */
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < kIncItems; ++k) {
+            s_word[warp * kIncItems + k] = word[k];
+            s_wpre[warp * kIncItems + k] = wrun;
+            wrun += (uint32_t)__popc(word[k]);
+        }
+    }
+    __syncthreads();
+    /* the bucket's particles: rank among themselves, then their places */
+    for (int e = tid; e < c; e += kThreads) {
+        const uint32_t k = s_k[e];
+        const int32_t i = s_i[e];
+        int r = 0;
+        for (int f = 0; f < c; ++f) r += pair_less(s_k[f], s_i[f], k, i) ? 1 : 0;
+        s_sk[r] = k;
+        s_si[r] = i;
+        const long long p = s_p[e];
+        uint32_t mb = tile_pre + tile_moved;   /* p at the tile's end */
+        if (p < tend) {
+            const int lw = (int)((p - tbase) >> 5);
+            mb = tile_pre + s_wpre[lw] + (uint32_t)__popc(s_word[lw] & ((1u << (p & 31)) - 1u));
+        }
+        const long long at = p - (long long)mb + off + r;
+        if (at < 0 || at >= n) continue;   /* never with consistent inputs */
+        kout[at] = k;
+        vout[at] = i;
+        prev[at] = k;
+        if ((at & (kIncTile - 1)) == 0) first[at >> kIncShift] = k;
+    }
+    __syncthreads();
+    /* the stayed particles of this tile */
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) {
+        const long long idx = wbase + k * 32 + lane;
+        if (idx < n && !((word[k] >> lane) & 1u)) {
+            const int32_t i = (int32_t)idx;
+            int lo = 0, hi = c;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (pair_less(s_sk[mid], s_si[mid], key[k], i)) lo = mid + 1;
+                else hi = mid;
+            }
+            const int lw = warp * kIncItems + k;
+            const long long at = idx - (long long)(tile_pre + s_wpre[lw] + (uint32_t)__popc(word[k] & lt)) + off + lo;
+            if (at < 0 || at >= n) continue;
+            kout[at] = key[k];
+            vout[at] = i;
+            prev[at] = key[k];
+            if ((at & (kIncTile - 1)) == 0) first[at >> kIncShift] = key[k];
+        }
+    }
+}
+
+size_t sort_inc_workspace_bytes(int n) { return IncLayout(n).total; }
+
+void sort_pairs_incremental(cudaStream_t s, const uint32_t* keys, int n, int key_bits, uint32_t* kout,
+                            int32_t* vout, void* inc_ws, void* sort_ws, unsigned* flags, int num_sms) {
+    if (n <= 0) return;
+    const IncLayout L(n);
+    char* w = static_cast<char*>(inc_ws);
+    unsigned* valid = reinterpret_cast<unsigned*>(w + L.valid);
+    uint32_t* prev = reinterpret_cast<uint32_t*>(w + L.prev);
+    uint32_t* first = reinterpret_cast<uint32_t*>(w + L.first);
+    uint32_t* bits = reinterpret_cast<uint32_t*>(w + L.bits);
+    int4* store = reinterpret_cast<int4*>(w + L.store);
+    unsigned* over = reinterpret_cast<unsigned*>(w + L.over);
+    uint32_t* bcnt = reinterpret_cast<uint32_t*>(w + L.bcnt);
+    uint32_t* tcnt = reinterpret_cast<uint32_t*>(w + L.tcnt);
+    uint32_t* tpre = reinterpret_cast<uint32_t*>(w + L.tpre);
+    uint32_t* boff = reinterpret_cast<uint32_t*>(w + L.boff);
+    int32_t* list = reinterpret_cast<int32_t*>(w + L.list);
+    uint32_t* lcount = reinterpret_cast<uint32_t*>(w + L.lcount);
+    unsigned* done = reinterpret_cast<unsigned*>(w + L.done);
+    cudaMemsetAsync(w + L.zero, 0, L.zero_bytes, s);
+    k_inc_flags<<<L.tiles, kThreads, 0, s>>>(keys, prev, n, valid, bits, tcnt, over, list, lcount);
+    k_inc_place<<<2 * num_sms, kThreads, 0, s>>>(keys, list, lcount, prev, first, n, L.tiles, valid, bcnt, store, over,
+                                                 done, tcnt, tpre, boff);
+    if (n > 1 && sort_passes(key_bits) > 0) {
+        /* the full sort of (keys, identity), run only when the overflow word is set; prev is
+         * its scratch (rewritten from kout below) and its last pass writes kout / vout */
+        uint32_t* kr;
+        int32_t* vr;
+        int32_t* vscr = reinterpret_cast<int32_t*>(w + L.vscr);
+        const bool odd = (sort_passes(key_bits) & 1) != 0;
+        sort_pairs_impl(s, keys, nullptr, odd ? kout : prev, odd ? vout : vscr, odd ? prev : kout,
+                        odd ? vscr : vout, n, over, key_bits, sort_ws, flags, num_sms, &kr, &vr);
+    }
+    k_inc_merge<<<L.tiles, kThreads, 0, s>>>(keys, n, bits, tcnt, tpre, boff, bcnt, store, over, kout, vout, prev,
+                                             first, valid);
 }
 
 }  // namespace sph

@@ -43,10 +43,10 @@
 #include "sph_kernels.cuh"
 
 namespace sph {
-__global__ void k_sort_hist(const uint32_t* keys, int n, int passes, uint32_t* hist);
+__global__ void k_sort_hist(const uint32_t* keys, int n, int passes, uint32_t* hist, const unsigned* gate);
 __global__ void k_onesweep(const uint32_t* kin, const int32_t* vin, uint32_t* kout, int32_t* vout, int n,
                            int shift, int pass, int tiles, const uint32_t* hist, uint32_t* counters,
-                           uint32_t* status, unsigned* flags);
+                           uint32_t* status, unsigned* flags, const unsigned* gate);
 int sort_tiles(int n);
 }  // namespace sph
 
@@ -150,7 +150,7 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* d_keys_in, const int32_t* 
         cudaGetLastError();
         return SPH_E_CUDA;
     }
-    sph::k_sort_hist<<<2 * sms, kCtaThreads, 0, s>>>(d_keys_in, n, passes, hist);
+    sph::k_sort_hist<<<2 * sms, kCtaThreads, 0, s>>>(d_keys_in, n, passes, hist, nullptr);
     /* pass p writes the caller's output when (passes - 1 - p) is even, the copy otherwise,
      * so the last pass lands in the output and the input is never written */
     const uint32_t* ki = d_keys_in;
@@ -160,7 +160,7 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* d_keys_in, const int32_t* 
         uint32_t* ko = to_out ? d_keys_out : kalt;
         int32_t* vo = to_out ? d_vals_out : valt;
         sph::k_onesweep<<<tiles, kCtaThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, p, tiles, hist, counters, status,
-                                                      flags);
+                                                      flags, nullptr);
         ki = ko;
         vi = vo;
     }
