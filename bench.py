@@ -677,8 +677,8 @@ def main():
                                                "of one capture on " + ins[1] + ", stored with the code (not "
                                                "measured in this run)"),
                          "peak_from": "%d SMs x 4 schedulers x %.0f MHz (%s)" % (sms, mhz, mhz_from)}
-    passes = (d["key_bits"] + 7) // 8
-    launches_per_step = sum(1 for k in kern) + (passes if "sort" in kern else 0)
+    # kernel nodes of the step's CUDA graph (the timed region replays it)
+    launches_per_step = ctx.step_kernel_launches()
     # e2e through the C ABI with pinned host buffers: state in, result out, every step
     e2e = None
     if not args.no_e2e:

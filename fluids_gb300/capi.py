@@ -44,7 +44,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_synchronize", "sph_device_flags", "sph_field_elems", "sph_field_kind", "sph_get_field",
            "sph_set_field", "sph_field_device_ptr", "sph_body_forces", "sph_stats", "sph_sort_pairs",
            "sph_scene_box_volume", "sph_scene_fishtank", "sph_scene_cube", "sph_jitter", "sph_cuda_available",
-           "sph_describe", "sph_profile_step", "sph_sort_pairs_noalloc", "sph_batch_create",
+           "sph_describe", "sph_profile_step", "sph_step_kernel_launches", "sph_sort_pairs_noalloc",
+           "sph_batch_create",
            "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid",
            "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
            "sph_adj_flags", "sph_adj_tape_bytes", "sph_set_block_size", "sph_set_tile_shape",
@@ -180,6 +181,7 @@ def lib():
             "sph_cuda_available": (ip, []),
             "sph_describe": (ip, [PP, fp, C.POINTER(SphDerived)]),
             "sph_profile_step": (ip, [vp, ip, C.POINTER(C.c_float), ip, C.POINTER(ip), C.c_char_p, C.c_size_t]),
+            "sph_step_kernel_launches": (ip, [vp, C.POINTER(ip)]),
             "sph_sort_pairs_noalloc": (ip, [vp, vp, vp, vp, ip, ip, vp]),
             "sph_batch_create": (ip, [PP, ip, C.POINTER(SceneDesc), C.POINTER(vp)]),
             "sph_batch_scene_count": (ip, [vp]),
@@ -451,6 +453,12 @@ class Context:
         self._c(self._lib.sph_profile_step(self.h, int(nsteps), ms, 64, C.byref(ng), names, 4096))
         keys = names.value.decode().split(",") if ng.value else []
         return dict(zip(keys, [float(ms[i]) for i in range(ng.value)]))
+
+    def step_kernel_launches(self):
+        """Kernel launches in one step's CUDA graph (0 without a graph)."""
+        n = C.c_int()
+        self._c(self._lib.sph_step_kernel_launches(self.h, C.byref(n)))
+        return n.value
 
     def stats(self):
         out = (C.c_double * 8)()

@@ -358,7 +358,7 @@ int run_stage_impl(sph_ctx* x, int stage) {
     case SPH_S_SORT:
         /* the stable sort of the keys as an update of the last step's order */
         sph::sort_pairs_incremental(s, b.keys, x->N, c.key_bits, b.keys_alt, b.mask_alt, b.inc_ws, b.sort_ws,
-                                    b.flags, x->num_sms);
+                                    b.flags, x->num_sms, x->side, x->ev_fork, x->ev_join);
         b.keys_sorted = b.keys_alt;
         b.mask_sorted = b.mask_alt;
         x->cur_keys = b.keys_sorted;
@@ -453,9 +453,18 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
     for (int k = 0; k < 3; ++k) {
         if (pre[k] == SPH_S_BOUNDARY_SYNC && !(x->NB > 0 && x->any_movable)) continue;
         if (pre[k] == SPH_S_HASHES) {
-            sph::launch_hashes(s, c, b.pos, x->N, b.keys, nullptr, b.tab, b.cell_prev, b.flags, bs, b.scenes,
-                               b.scene_of);
+            /* the hashes with the incremental sort's first pass */
+            sph::sort_inc_begin(s, b.inc_ws, x->N);
+            sph::launch_hashes_flags(s, c, b.pos, x->N, b.keys, b.tab, b.cell_prev, b.flags, b.scenes, b.scene_of,
+                                     sph::sort_inc_flags_args(b.inc_ws, x->N));
             x->cur_keys = b.keys;
+        } else if (pre[k] == SPH_S_SORT) {
+            sph::sort_pairs_incremental(s, b.keys, x->N, c.key_bits, b.keys_alt, b.mask_alt, b.inc_ws, b.sort_ws,
+                                        b.flags, x->num_sms, x->side, x->ev_fork, x->ev_join, true);
+            b.keys_sorted = b.keys_alt;
+            b.mask_sorted = b.mask_alt;
+            x->cur_keys = b.keys_sorted;
+            x->cur_mask = b.mask_sorted;
         } else if ((rc = run_stage_impl(x, pre[k])) != SPH_OK) {
             return rc;
         }
@@ -543,6 +552,20 @@ int build_graph(sph_ctx* x) {
         x->graph_ok = false;
         x->err.clear();
         return SPH_OK;
+    }
+    {
+        size_t nn = 0;
+        x->graph_kernels = 0;
+        if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn > 0) {
+            std::vector<cudaGraphNode_t> nodes(nn);
+            if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+                for (size_t k = 0; k < nn; ++k) {
+                    cudaGraphNodeType t;
+                    if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+                        ++x->graph_kernels;
+                }
+        }
+        cudaGetLastError();
     }
     e = cudaGraphInstantiate(&x->gexec, g, 0);
     cudaGraphDestroy(g);
@@ -838,6 +861,14 @@ SortCache g_sort;
 
 int sph_ctx_fail(sph_ctx* x, int code, const std::string& msg) { return fail(x, code, msg); }
 
+static void release_side(sph_ctx* x) {
+    if (x->side) cudaStreamDestroy(x->side);
+    if (x->ev_fork) cudaEventDestroy(x->ev_fork);
+    if (x->ev_join) cudaEventDestroy(x->ev_join);
+    x->side = nullptr;
+    x->ev_fork = x->ev_join = nullptr;
+}
+
 extern "C" {
 
 void sph_default_params(int method, sph_params* p) {
@@ -1034,10 +1065,17 @@ int sph_create(const sph_params* params, sph_ctx** out) {
         return fail(nullptr, SPH_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
     }
     x->own_stream = true;
+    if (cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();   /* then everything runs on the main stream */
+        release_side(x);
+    }
     int rc = derive(x);
     if (rc != SPH_OK) {
         std::string m = x->err;
         cudaStreamDestroy(x->stream);
+        release_side(x);
         delete x;
         return fail(nullptr, rc, m);
     }
@@ -1054,6 +1092,8 @@ int sph_destroy(sph_ctx* x) {
     cudaFree(x->render_sort);
     cudaFree(x->frame_buf);
     if (x->own_stream && x->stream) cudaStreamDestroy(x->stream);
+    if (x->side) cudaStreamSynchronize(x->side);
+    release_side(x);
     delete x;
     return SPH_OK;
 }
@@ -1276,6 +1316,12 @@ int sph_simulate(sph_ctx* x, int nsteps) {
             if (rc != SPH_OK) return rc;
         }
     }
+    if (nsteps > 0) {
+        /* the HASHES and MASK fields show the last step's sort (a graph launch does not run
+         * enqueue_step's host code, and a stage call may have pointed them elsewhere) */
+        x->cur_keys = x->b.keys_sorted;
+        x->cur_mask = x->b.mask_sorted;
+    }
     return SPH_OK;
 }
 
@@ -1347,6 +1393,17 @@ int sph_run_stage(sph_ctx* x, int stage) {
     if (check_ctx(x)) return SPH_E_INVALID;
     if (!x->has_state) return fail(x, SPH_E_STATE, "no particles added");
     return run_stage_impl(x, stage);
+}
+
+int sph_step_kernel_launches(sph_ctx* x, int* launches) {
+    if (check_ctx(x) || !launches) return SPH_E_INVALID;
+    *launches = 0;
+    if (x->p.use_graph && x->graph_ok && !x->gexec && x->has_state && x->N > 0) {
+        int rc = build_graph(x);
+        if (rc != SPH_OK) return rc;
+    }
+    if (x->gexec) *launches = x->graph_kernels;
+    return SPH_OK;
 }
 
 int sph_synchronize(sph_ctx* x) {

@@ -28,6 +28,10 @@ struct sph_ctx {
     Bufs b{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    /* a second stream and fork / join events: work that may run beside the main stream's
+     * (the gated full sort of the step's incremental sort) */
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int device = 0, num_sms = 1;
     std::string err;
     float lim[3] = {0.f, 0.f, 0.f};
@@ -46,6 +50,7 @@ struct sph_ctx {
     std::vector<sph::SceneTile> h_tiles;
     bool graph_ok = true;
     cudaGraphExec_t gexec = nullptr;
+    int graph_kernels = 0;   /* kernel nodes of the step graph */
     uint32_t* cur_keys = nullptr;
     int32_t* cur_mask = nullptr;
     bool has_state = false;

@@ -3,7 +3,9 @@
  *
  *   k_hashes      compute_hashes (kernels/grid.cl:20-39): Morton key + identity mask; also
  *                 clears the cell-table entries the previous step wrote, so the table never
- *                 needs the O(cells) fill of fluid/simulation/grid.cpp:41.
+ *                 needs the O(cells) fill of fluid/simulation/grid.cpp:41.  k_hashes_flags
+ *                 is the fused step's form, which also runs the incremental sort's first
+ *                 pass on the keys.
  *   k_gather      clshuffle (opencl/algorithms/clshuffle.h:12-58) for every fluid array in
  *                 one pass: dst[i] = src[mask[i]].
  *   k_cell_ranges compute_cell_intervals (kernels/grid.cl:60-123): [start, end) per occupied
@@ -17,25 +19,18 @@
 
 namespace sph {
 
-__global__ void k_hashes(Const c0, const float4* __restrict__ pos, int n, uint32_t* __restrict__ keys,
-                         int32_t* __restrict__ mask, int2* __restrict__ tab, const int32_t* __restrict__ cell_prev,
-                         unsigned* __restrict__ flags, const SceneDev* __restrict__ scenes,
-                         const int32_t* __restrict__ scene_of) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (cell_prev) {
-        const int pc = cell_prev[i];
-        if (pc >= 0) tab[pc] = make_int2(0, 0);
-    }
+/* compute_hashes for particle i: clears the cell-table entry its previous cell left, returns
+ * its key (and reports a particle outside a PHYSICS grid). */
+__device__ __forceinline__ uint32_t hash_particle(const Const& c0, const float4 p, int i, int2* __restrict__ tab,
+                                                  int pc, unsigned* __restrict__ flags,
+                                                  const SceneDev* __restrict__ scenes,
+                                                  const int32_t* __restrict__ scene_of) {
+    if (pc >= 0) tab[pc] = make_int2(0, 0);
     Const c = c0;
     const uint32_t sid = scene_of ? (uint32_t)scene_of[i] : 0u;
     scene_setup(c, scenes, scene_of, i);
-    const float4 p = pos[i];
     int cx, cy, cz;
     cell_of(c, p.x, p.y, p.z, cx, cy, cz);
-    /* batched: the scene id above the Morton bits keeps every scene's range contiguous */
-    keys[i] = (sid << c.scene_shift) | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
-    if (mask) mask[i] = i;   /* the identity values of the stage API (the step's sort needs none) */
     if (!c.wrap) {
         /* PHYSICS grid clamps: report particles outside it (informational) */
         const float fx = floorf(__fdiv_rn(__fsub_rn(p.x, c.ox), c.cell));
@@ -44,6 +39,79 @@ __global__ void k_hashes(Const c0, const float4* __restrict__ pos, int n, uint32
         const bool out = !(fx >= 0.f && fx < (float)c.nx && fy >= 0.f && fy < (float)c.ny && fz >= 0.f &&
                            fz < (float)c.nz);
         if (out) atomicOr(flags, kFlagEscaped);
+    }
+    /* batched: the scene id above the Morton bits keeps every scene's range contiguous */
+    return (sid << c.scene_shift) | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+}
+
+__global__ void k_hashes(Const c0, const float4* __restrict__ pos, int n, uint32_t* __restrict__ keys,
+                         int32_t* __restrict__ mask, int2* __restrict__ tab, const int32_t* __restrict__ cell_prev,
+                         unsigned* __restrict__ flags, const SceneDev* __restrict__ scenes,
+                         const int32_t* __restrict__ scene_of) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = hash_particle(c0, pos[i], i, tab, cell_prev ? cell_prev[i] : -1, flags, scenes, scene_of);
+    if (mask) mask[i] = i;   /* the identity values of the stage API */
+}
+
+/* k_hashes of the fused step with the incremental sort's first pass (k_inc_flags of
+ * sph_sort.cu) on the keys it computes: tiles of kIncTile particles, kIncItems a thread. */
+__global__ void __launch_bounds__(256) k_hashes_flags(Const c0, const float4* __restrict__ pos, int n,
+                                                      uint32_t* __restrict__ keys, int2* __restrict__ tab,
+                                                      const int32_t* __restrict__ cell_prev,
+                                                      unsigned* __restrict__ flags,
+                                                      const SceneDev* __restrict__ scenes,
+                                                      const int32_t* __restrict__ scene_of, IncFlags inc) {
+    constexpr int kItems = kIncItems;
+    __shared__ uint32_t s_wcnt[8];
+    __shared__ uint32_t s_base;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wbase = ((int)blockIdx.x * kIncTile) + warp * (32 * kItems);   /* n < 2^31 */
+    const bool have_prev = *inc.valid != 0u;
+    if (!have_prev && blockIdx.x == 0 && tid == 0) *inc.over = 1u;   /* no previous result: a full sort */
+    float4 p[kItems];
+    int pc[kItems];
+    uint32_t old[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int idx = wbase + k * 32 + lane;
+        const bool in = idx < n;
+        p[k] = in ? __ldg(&pos[idx]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        pc[k] = in && cell_prev ? __ldg(&cell_prev[idx]) : -1;
+        old[k] = in ? __ldg(&inc.prev[idx]) : 0u;
+    }
+    uint32_t cnt = 0, word[kItems], key[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int w0 = wbase + k * 32, idx = w0 + lane;
+        key[k] = 0u;
+        if (idx < n) {
+            key[k] = hash_particle(c0, p[k], idx, tab, pc[k], flags, scenes, scene_of);
+            keys[idx] = key[k];
+        }
+        word[k] = __ballot_sync(0xffffffffu, idx < n && (!have_prev || key[k] != old[k]));
+        if (lane == 0 && w0 < n) inc.bits[w0 >> 5] = word[k];
+        cnt += (uint32_t)__popc(word[k]);
+    }
+    if (lane == 0) s_wcnt[warp] = cnt;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t total = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) total += s_wcnt[w];
+        inc.tcnt[blockIdx.x] = total;
+        s_base = have_prev && total ? atomicAdd(inc.lcount, total) : 0u;
+    }
+    __syncthreads();
+    if (!have_prev || cnt == 0) return;
+    uint32_t run = s_base;
+    for (int w = 0; w < warp; ++w) run += s_wcnt[w];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        if ((word[k] >> lane) & 1u)
+            inc.list[run + (uint32_t)__popc(word[k] & lt)] = make_int2(wbase + k * 32 + lane, (int)key[k]);
+        run += (uint32_t)__popc(word[k]);
     }
 }
 
@@ -182,6 +250,13 @@ void launch_hashes(cudaStream_t s, const Const& c, const float4* pos, int n, uin
                    const int32_t* scene_of) {
     if (n <= 0) return;
     k_hashes<<<blocks_for(n, bs), bs, 0, s>>>(c, pos, n, keys, mask, tab, cell_prev, flags, scenes, scene_of);
+}
+void launch_hashes_flags(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int2* tab,
+                         const int32_t* cell_prev, unsigned* flags, const SceneDev* scenes, const int32_t* scene_of,
+                         const IncFlags& inc) {
+    if (n <= 0) return;
+    k_hashes_flags<<<blocks_for(n, kIncTile), 256, 0, s>>>(c, pos, n, keys, tab, cell_prev, flags, scenes, scene_of,
+                                                           inc);
 }
 void launch_gather(cudaStream_t s, int n, const int32_t* perm, const float4* a, float4* as, const float4* b,
                    float4* bs_, const float4* c3, float4* cs, const int32_t* ids, int32_t* ids_s, int bs) {

@@ -69,10 +69,28 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
 /* The stable sort of keys[0, n) (values: the indices) into kout / vout, computed as an update
  * of the previous call's result kept in inc_ws (bytes: sort_inc_workspace_bytes(n), zeroed
  * once before the first call; sort_ws: sort_workspace_bytes(n, key_bits)).  Same result as
- * sort_pairs over (keys, identity) for every input. */
+ * sort_pairs over (keys, identity) for every input.  side / fork / join (all or none): a
+ * second stream and two events on which the gated full sort runs beside the merge. */
 size_t sort_inc_workspace_bytes(int n);
+/* The incremental sort's first pass fused into the step's hash kernel: the sort then starts
+ * with sort_inc_begin (before the hash kernel) and skips that pass (flags_done). */
+constexpr int kIncItems = 8;
+constexpr int kIncTile = 256 * kIncItems;
+struct IncFlags {
+    const unsigned* valid;
+    const uint32_t* prev;
+    uint32_t* bits;
+    uint32_t* tcnt;
+    unsigned* over;
+    int2* list;
+    uint32_t* lcount;
+};
+IncFlags sort_inc_flags_args(void* inc_ws, int n);
+void sort_inc_begin(cudaStream_t s, void* inc_ws, int n);
 void sort_pairs_incremental(cudaStream_t s, const uint32_t* keys, int n, int key_bits, uint32_t* kout,
-                            int32_t* vout, void* inc_ws, void* sort_ws, unsigned* flags, int num_sms);
+                            int32_t* vout, void* inc_ws, void* sort_ws, unsigned* flags, int num_sms,
+                            cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr,
+                            bool flags_done = false);
 
 /* sph_grid.cu */
 /* scenes: the context's scene table (never null); scene_of: scene of each particle, or
@@ -80,6 +98,9 @@ void sort_pairs_incremental(cudaStream_t s, const uint32_t* keys, int n, int key
 void launch_hashes(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int32_t* mask,
                    int2* tab, const int32_t* cell_prev, unsigned* flags, int bs, const SceneDev* scenes,
                    const int32_t* scene_of);
+void launch_hashes_flags(cudaStream_t s, const Const& c, const float4* pos, int n, uint32_t* keys, int2* tab,
+                         const int32_t* cell_prev, unsigned* flags, const SceneDev* scenes, const int32_t* scene_of,
+                         const IncFlags& inc);
 void launch_gather_ranges(cudaStream_t s, const Const& c, int n, const int32_t* perm, const float4* a, float4* as,
                           const float4* b, float4* bs_, const float4* c3, float4* cs, const int32_t* ids,
                           int32_t* ids_s, const uint32_t* keys, int2* tab, int32_t* cell_out, unsigned* flags, int bs,

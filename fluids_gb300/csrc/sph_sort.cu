@@ -283,8 +283,9 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
  *   k_inc_flags  per tile of kIncTile positions: the moved flags as ballot words (bits) and
  *                the tile's count of moved particles.
  *   k_inc_place  per moved particle (k, i): p = the first position whose (prev[p], p) is
- *                not below (k, i), by a binary search over a table of each tile's first
- *                prev key and then within the tile.  (k, i, p) goes to bucket p / kIncTile.
+ *                not below (k, i), by binary searches over each tile's first prev key (a
+ *                table staged in shared memory), then each word's first prev key within
+ *                the tile, then prev within the word.  (k, i, p) goes to bucket p / kIncTile.
  *                The stayed particles at positions [t kIncTile, (t + 1) kIncTile) are all
  *                above the moved particles of the buckets below t and below those of the
  *                buckets above t, so only bucket t's need comparing with them.
@@ -292,21 +293,21 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
  *                memory; a moved particle goes to (stayed before p) + (moved particles of the
  *                buckets below t) + its rank, a stayed particle of stayed rank a to a + (moved
  *                particles of the buckets below t) + (bucket particles below it).
+ *   k_inc_keep   after an overflow, keeps the full sort's keys as prev; marks prev valid.
  * A bucket holds kIncBucket particles.  When one overflows, or there is no previous result
  * (the first call), the overflow word opens the gated full onesweep sort of all keys (its
- * kernels read the word and leave at once while it is 0) and k_inc_merge only keeps that
- * result as prev.  Moved particles are 1-2 % of a flowing scene per step: the passes over
- * all particles then read 8 bytes and write 12 bytes per particle.
+ * kernels read the word and leave at once while it is 0; they run on a side stream beside
+ * k_inc_merge, which then leaves at once).  Moved particles are 1-2 % of a flowing scene per
+ * step: the passes over all particles then read 8 bytes and write 12 bytes per particle.
  * ------------------------------------------------------------------------------------- */
 namespace {
-constexpr int kIncItems = 8;
-constexpr int kIncTile = kThreads * kIncItems;   /* 2048 positions = 64 ballot words */
+static_assert(kIncTile == kThreads * kIncItems, "2048 positions = 64 ballot words");
 constexpr int kIncShift = 11;
 constexpr int kIncWords = kIncTile / 32;
 constexpr int kIncBucket = 256;                  /* moved particles per merge tile before overflow */
 
 struct IncLayout {
-    size_t valid, prev, first, bits, list, store, zero, over, lcount, done, bcnt, tcnt, tpre, boff, vscr, total,
+    size_t valid, prev, first, sub, bits, list, store, zero, over, lcount, done, bcnt, tcnt, tpre, boff, vscr, total,
         zero_bytes;
     int tiles, words;
     IncLayout(int n) {
@@ -321,9 +322,10 @@ struct IncLayout {
         };
         valid = take(4);
         prev = take(4 * nn);
-        first = take(4 * (size_t)tiles);
+        first = take(4 * (size_t)tiles);   /* prev at each tile's first position */
+        sub = take(4 * (size_t)words);     /* prev at each word's first position */
         bits = take(4 * (size_t)words);
-        list = take(4 * nn);
+        list = take(8 * nn);
         store = take(16 * (size_t)tiles * kIncBucket);
         /* zeroed by every call: the overflow word, the list length, the count of finished
          * placing CTAs and the bucket counts (the other arrays are written whole) */
@@ -351,27 +353,26 @@ __global__ void __launch_bounds__(kThreads) k_inc_flags(const uint32_t* __restri
                                                         const uint32_t* __restrict__ prev, int n,
                                                         const unsigned* __restrict__ valid,
                                                         uint32_t* __restrict__ bits, uint32_t* __restrict__ tcnt,
-                                                        unsigned* __restrict__ over, int32_t* __restrict__ list,
+                                                        unsigned* __restrict__ over, int2* __restrict__ list,
                                                         uint32_t* __restrict__ lcount) {
     __shared__ uint32_t s_wcnt[kWarps];
     __shared__ uint32_t s_base;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long wbase = ((long long)blockIdx.x << kIncShift) + (long long)warp * (32 * kIncItems);
+    const int wbase = ((int)blockIdx.x << kIncShift) + warp * (32 * kIncItems);   /* n < 2^31 */
     const bool have_prev = *valid != 0u;
     if (!have_prev && blockIdx.x == 0 && tid == 0) *over = 1u;   /* no previous result: a full sort */
     uint32_t key[kIncItems], old[kIncItems];
 #pragma unroll
     for (int k = 0; k < kIncItems; ++k) {
-        const long long idx = wbase + k * 32 + lane;
+        const int idx = wbase + k * 32 + lane;
         key[k] = idx < n ? __ldg(&keys[idx]) : 0u;
         old[k] = idx < n ? __ldg(&prev[idx]) : 0u;
     }
     uint32_t cnt = 0, word[kIncItems];
 #pragma unroll
     for (int k = 0; k < kIncItems; ++k) {
-        const long long w0 = wbase + k * 32;
-        const bool moved = w0 + lane < n && (!have_prev || key[k] != old[k]);
-        word[k] = __ballot_sync(0xffffffffu, moved);
+        const int w0 = wbase + k * 32;
+        word[k] = __ballot_sync(0xffffffffu, w0 + lane < n && (!have_prev || key[k] != old[k]));
         if (lane == 0 && w0 < n) bits[w0 >> 5] = word[k];
         cnt += (uint32_t)__popc(word[k]);
     }
@@ -382,57 +383,79 @@ __global__ void __launch_bounds__(kThreads) k_inc_flags(const uint32_t* __restri
 #pragma unroll
         for (int w = 0; w < kWarps; ++w) total += s_wcnt[w];
         tcnt[blockIdx.x] = total;
-        /* the moved positions go to a list in any order (one atomic per tile): the places
+        /* the moved particles go to a list in any order (one atomic per tile): their places
          * are computed from (key, index) alone */
         s_base = have_prev && total ? atomicAdd(lcount, total) : 0u;
     }
     __syncthreads();
-    if (!have_prev) return;
+    if (!have_prev || cnt == 0) return;
     uint32_t run = s_base;
     for (int w = 0; w < warp; ++w) run += s_wcnt[w];
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < kIncItems; ++k) {
-        if ((word[k] >> lane) & 1u) list[run + (uint32_t)__popc(word[k] & lt)] = (int32_t)(wbase + k * 32 + lane);
+        if ((word[k] >> lane) & 1u)
+            list[run + (uint32_t)__popc(word[k] & lt)] = make_int2(wbase + k * 32 + lane, (int)key[k]);
         run += (uint32_t)__popc(word[k]);
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_inc_place(const uint32_t* __restrict__ keys,
-                                                        const int32_t* __restrict__ list,
+constexpr int kIncSmemTiles = 8192;   /* tile-first table staged in shared memory up to 16.7M positions */
+
+__global__ void __launch_bounds__(kThreads) k_inc_place(const int2* __restrict__ list,
                                                         const uint32_t* __restrict__ lcount,
                                                         const uint32_t* __restrict__ prev,
-                                                        const uint32_t* __restrict__ first, int n, int tiles,
+                                                        const uint32_t* __restrict__ first,
+                                                        const uint32_t* __restrict__ sub, int n, int tiles,
                                                         const unsigned* __restrict__ valid,
                                                         uint32_t* __restrict__ bcnt, int4* __restrict__ store,
                                                         unsigned* __restrict__ over, unsigned* __restrict__ done,
                                                         const uint32_t* __restrict__ tcnt,
                                                         uint32_t* __restrict__ tpre, uint32_t* __restrict__ boff) {
+    extern __shared__ uint32_t s_first[];   /* min(tiles, kIncSmemTiles) entries */
     __shared__ uint32_t s_scan[kWarps];
     __shared__ bool s_last;
     if (*valid == 0u) return;   /* no previous result: the full sort runs */
+    const bool staged = tiles <= kIncSmemTiles;
+    if (staged)
+        for (int t = threadIdx.x; t < tiles; t += blockDim.x) s_first[t] = __ldg(&first[t]);
+    __syncthreads();
     const int m = (int)*lcount;
+    const int words = (n + 31) >> 5;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
-        const int i = __ldg(&list[r]);
-        const uint32_t k = __ldg(&keys[i]);
-        /* the number of tiles whose first (prev, position) is below (k, i) ... */
+        const int2 e = __ldg(&list[r]);
+        const int i = e.x;
+        const uint32_t k = (uint32_t)e.y;
+        /* tiles whose first (prev, position) is below (k, i) */
         int lo = 0, hi = tiles;
         while (lo < hi) {
             const int mid = (lo + hi) >> 1;
-            if (pair_less(__ldg(&first[mid]), mid << kIncShift, k, i)) lo = mid + 1;
+            const uint32_t fk = staged ? s_first[mid] : __ldg(&first[mid]);
+            if (pair_less(fk, mid << kIncShift, k, i)) lo = mid + 1;
             else hi = mid;
         }
-        /* ... puts p after the first position of tile lo - 1 and at most at tile lo's first */
-        int plo = lo > 0 ? ((lo - 1) << kIncShift) : 0;
-        int phi = lo > 0 ? min(lo << kIncShift, n) : 0;
-        while (plo < phi) {
-            const int mid = (plo + phi) >> 1;
-            if (pair_less(__ldg(&prev[mid]), mid, k, i)) plo = mid + 1;
-            else phi = mid;
+        int p = 0;
+        if (lo > 0) {
+            /* p lies after tile lo - 1's first position: words of that tile whose first
+             * (prev, position) is below (k, i) (its first word is) ... */
+            int wlo = ((lo - 1) << (kIncShift - 5)) + 1, whi = min(lo << (kIncShift - 5), words);
+            while (wlo < whi) {
+                const int mid = (wlo + whi) >> 1;
+                if (pair_less(__ldg(&sub[mid]), mid << 5, k, i)) wlo = mid + 1;
+                else whi = mid;
+            }
+            /* ... then p after the first position of word wlo - 1, at most at word wlo's */
+            int plo = ((wlo - 1) << 5) + 1, phi = min(wlo << 5, n);
+            while (plo < phi) {
+                const int mid = (plo + phi) >> 1;
+                if (pair_less(__ldg(&prev[mid]), mid, k, i)) plo = mid + 1;
+                else phi = mid;
+            }
+            p = plo;
         }
-        const int b = min(plo >> kIncShift, tiles - 1);
+        const int b = min(p >> kIncShift, tiles - 1);
         const uint32_t slot = atomicAdd(&bcnt[b], 1u);
-        if (slot < (uint32_t)kIncBucket) store[(size_t)b * kIncBucket + slot] = make_int4((int)k, i, plo, 0);
+        if (slot < (uint32_t)kIncBucket) store[(size_t)b * kIncBucket + slot] = make_int4((int)k, i, p, 0);
         else *over = 1u;
     }
     /* the last CTA to finish turns the tile counts and bucket counts into exclusive
@@ -446,15 +469,41 @@ __global__ void __launch_bounds__(kThreads) k_inc_place(const uint32_t* __restri
     if (!s_last) return;
     __threadfence();
     const int per = (tiles + kThreads - 1) / kThreads;
-    const int t0 = threadIdx.x * per;
+    const int t0 = threadIdx.x * per, t1 = min(t0 + per, tiles);
     uint32_t a = 0, c = 0;
-    for (int t = t0; t < min(t0 + per, tiles); ++t) {
+    if (per <= 8) {
+        uint32_t va[8], vc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            va[u] = t0 + u < t1 ? __ldcg(&tcnt[t0 + u]) : 0u;
+            vc[u] = t0 + u < t1 ? __ldcg(&bcnt[t0 + u]) : 0u;
+        }
+        uint32_t ra = 0, rc = 0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            a += va[u];
+            c += vc[u];
+        }
+        ra = block_exclusive_scan_256(a, s_scan);
+        rc = block_exclusive_scan_256(c, s_scan);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (t0 + u < t1) {
+                tpre[t0 + u] = ra;
+                boff[t0 + u] = rc;
+            }
+            ra += va[u];
+            rc += vc[u];
+        }
+        return;
+    }
+    for (int t = t0; t < t1; ++t) {
         a += __ldcg(&tcnt[t]);
         c += __ldcg(&bcnt[t]);
     }
     uint32_t ra = block_exclusive_scan_256(a, s_scan);
     uint32_t rc = block_exclusive_scan_256(c, s_scan);
-    for (int t = t0; t < min(t0 + per, tiles); ++t) {
+    for (int t = t0; t < t1; ++t) {
         tpre[t] = ra;
         boff[t] = rc;
         ra += __ldcg(&tcnt[t]);
@@ -462,6 +511,10 @@ __global__ void __launch_bounds__(kThreads) k_inc_place(const uint32_t* __restri
     }
 }
 
+/* The merge of tile t.  A bucket particle e with insertion point p_e is below the stayed
+ * particle at position j exactly when p_e <= j (the positions before p_e hold pairs below e,
+ * the stayed ones from p_e on pairs above it), so each stayed particle's count of bucket
+ * particles below it is a prefix sum of the bucket's insertion points over the tile. */
 __global__ void __launch_bounds__(kThreads) k_inc_merge(const uint32_t* __restrict__ keys, int n,
                                                         const uint32_t* __restrict__ bits,
                                                         const uint32_t* __restrict__ tcnt,
@@ -472,58 +525,47 @@ __global__ void __launch_bounds__(kThreads) k_inc_merge(const uint32_t* __restri
                                                         const unsigned* __restrict__ over,
                                                         uint32_t* __restrict__ kout, int32_t* __restrict__ vout,
                                                         uint32_t* __restrict__ prev, uint32_t* __restrict__ first,
-                                                        unsigned* __restrict__ valid) {
-    __shared__ uint32_t s_k[kIncBucket], s_sk[kIncBucket];
-    __shared__ int32_t s_i[kIncBucket], s_si[kIncBucket], s_p[kIncBucket];
+                                                        uint32_t* __restrict__ sub) {
+    __shared__ uint32_t s_k[kIncBucket];
+    __shared__ int32_t s_i[kIncBucket], s_p[kIncBucket];
+    __shared__ uint32_t s_at[kIncTile + 1];   /* bucket particles inserted at each position */
     __shared__ uint32_t s_word[kIncWords], s_wpre[kIncWords];
+    __shared__ uint32_t s_scan[kWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int t = blockIdx.x;
-    const long long tbase = (long long)t << kIncShift;
-    const long long tend = min(tbase + kIncTile, (long long)n);
-    if (t == 0 && tid == 0) *valid = 1u;
-    if (*over != 0u) {
-        /* the gated full sort wrote kout and vout (a single pair needs no sort): keep its
-         * keys as the next call's prev */
-        if (n == 1 && tid == 0) {
-            kout[0] = __ldg(&keys[0]);
-            vout[0] = 0;
-        }
-        __syncthreads();
-        for (long long j = tbase + tid; j < tend; j += kThreads) {
-            const uint32_t k = kout[j];
-            prev[j] = k;
-            if ((j & (kIncTile - 1)) == 0) first[j >> kIncShift] = k;
-        }
-        return;
-    }
+    const int tbase = t << kIncShift;
+    const int tlen = min(kIncTile, n - tbase);
+    if (*over != 0u) return;   /* the gated full sort writes the result */
     /* this tile's keys and moved words first (their loads in flight together) */
-    const long long wbase = tbase + (long long)warp * (32 * kIncItems);
+    const int wbase = warp * (32 * kIncItems);   /* tile-local */
     uint32_t key[kIncItems], word[kIncItems];
 #pragma unroll
     for (int k = 0; k < kIncItems; ++k) {
-        const long long idx = wbase + k * 32 + lane;
-        key[k] = idx < n ? __ldg(&keys[idx]) : 0u;
-        word[k] = wbase + k * 32 < n ? __ldg(&bits[(wbase + k * 32) >> 5]) : 0u;
+        const int j = wbase + k * 32 + lane;
+        key[k] = j < tlen ? __ldg(&keys[tbase + j]) : 0u;
+        word[k] = wbase + k * 32 < tlen ? __ldg(&bits[(tbase + wbase + k * 32) >> 5]) : 0u;
     }
-    /* moved particles before this tile, and bucket particles of the buckets below it */
     const uint32_t tile_pre = __ldg(&tpre[t]), off = __ldg(&boff[t]), tile_moved = __ldg(&tcnt[t]);
-    /* moved particles before each word of the tile */
+    const int c = min((int)__ldg(&bcnt[t]), kIncBucket);   /* no overflow: at most kIncBucket */
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) s_at[tid * kIncItems + k] = 0u;
+    if (tid == 0) s_at[kIncTile] = 0u;
     uint32_t wc = 0;
 #pragma unroll
     for (int k = 0; k < kIncItems; ++k) wc += (uint32_t)__popc(word[k]);
     if (lane == 0) s_wpre[warp] = wc;   /* per-warp totals, scanned below */
-    const int c = min((int)__ldg(&bcnt[t]), kIncBucket);   /* no overflow: at most kIncBucket */
+    __syncthreads();
     for (int e = tid; e < c; e += kThreads) {
         const int4 v = __ldg(&store[(size_t)t * kIncBucket + e]);
         s_k[e] = (uint32_t)v.x;
         s_i[e] = v.y;
         s_p[e] = v.z;
+        atomicAdd(&s_at[v.z - tbase], 1u);   /* p in [tbase, tbase + tlen] */
     }
-    __syncthreads();
     uint32_t wrun = 0;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) wrun += w < warp ? s_wpre[w] : 0u;
-    __syncthreads();   /* every warp has read the per-warp totals */
+    __syncthreads();   /* every warp has read the per-warp totals; s_at is complete */
     if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < kIncItems; ++k) {
@@ -532,63 +574,105 @@ __global__ void __launch_bounds__(kThreads) k_inc_merge(const uint32_t* __restri
             wrun += (uint32_t)__popc(word[k]);
         }
     }
+    /* inclusive prefix of s_at over the tile's positions (thread tid owns 8 in a row) */
+    uint32_t loc[kIncItems], run = 0;
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) {
+        run += s_at[tid * kIncItems + k];
+        loc[k] = run;
+    }
+    const uint32_t before = block_exclusive_scan_256(run, s_scan);   /* syncs the block */
+#pragma unroll
+    for (int k = 0; k < kIncItems; ++k) s_at[tid * kIncItems + k] = before + loc[k];
     __syncthreads();
-    /* the bucket's particles: rank among themselves, then their places */
+    /* the bucket's particles: those with a smaller insertion point are below; equal points
+     * compare by (key, index) */
     for (int e = tid; e < c; e += kThreads) {
         const uint32_t k = s_k[e];
         const int32_t i = s_i[e];
-        int r = 0;
-        for (int f = 0; f < c; ++f) r += pair_less(s_k[f], s_i[f], k, i) ? 1 : 0;
-        s_sk[r] = k;
-        s_si[r] = i;
-        const long long p = s_p[e];
+        const int p = s_p[e];
+        const int lp = p - tbase;
+        int r = lp > 0 ? (int)s_at[lp - 1] : 0;
+        for (int f = 0; f < c; ++f) r += (s_p[f] == p && pair_less(s_k[f], s_i[f], k, i)) ? 1 : 0;
         uint32_t mb = tile_pre + tile_moved;   /* p at the tile's end */
-        if (p < tend) {
-            const int lw = (int)((p - tbase) >> 5);
-            mb = tile_pre + s_wpre[lw] + (uint32_t)__popc(s_word[lw] & ((1u << (p & 31)) - 1u));
+        if (lp < tlen) {
+            const int lw = lp >> 5;
+            mb = tile_pre + s_wpre[lw] + (uint32_t)__popc(s_word[lw] & ((1u << (lp & 31)) - 1u));
         }
-        const long long at = p - (long long)mb + off + r;
+        const int at = p - (int)mb + (int)off + r;
         if (at < 0 || at >= n) continue;   /* never with consistent inputs */
         kout[at] = k;
         vout[at] = i;
         prev[at] = k;
+        if ((at & 31) == 0) sub[at >> 5] = k;
         if ((at & (kIncTile - 1)) == 0) first[at >> kIncShift] = k;
     }
-    __syncthreads();
     /* the stayed particles of this tile */
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < kIncItems; ++k) {
-        const long long idx = wbase + k * 32 + lane;
-        if (idx < n && !((word[k] >> lane) & 1u)) {
-            const int32_t i = (int32_t)idx;
-            int lo = 0, hi = c;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (pair_less(s_sk[mid], s_si[mid], key[k], i)) lo = mid + 1;
-                else hi = mid;
-            }
+        const int j = wbase + k * 32 + lane;
+        if (j < tlen && !((word[k] >> lane) & 1u)) {
             const int lw = warp * kIncItems + k;
-            const long long at = idx - (long long)(tile_pre + s_wpre[lw] + (uint32_t)__popc(word[k] & lt)) + off + lo;
+            const int at = tbase + j - (int)(tile_pre + s_wpre[lw] + (uint32_t)__popc(word[k] & lt)) + (int)off +
+                           (int)s_at[j];
             if (at < 0 || at >= n) continue;
             kout[at] = key[k];
-            vout[at] = i;
+            vout[at] = tbase + j;
             prev[at] = key[k];
+            if ((at & 31) == 0) sub[at >> 5] = key[k];
             if ((at & (kIncTile - 1)) == 0) first[at >> kIncShift] = key[k];
         }
     }
 }
 
+/* After the gated full sort: its keys become prev (with the word and tile tables); a
+ * single pair needs no sort.  Marks prev valid for the next call either way. */
+__global__ void __launch_bounds__(kThreads) k_inc_keep(const uint32_t* __restrict__ keys, int n,
+                                                       const unsigned* __restrict__ over, uint32_t* __restrict__ kout,
+                                                       int32_t* __restrict__ vout, uint32_t* __restrict__ prev,
+                                                       uint32_t* __restrict__ first, uint32_t* __restrict__ sub,
+                                                       unsigned* __restrict__ valid) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *valid = 1u;
+    if (*over == 0u) return;
+    if (n == 1 && blockIdx.x == 0 && threadIdx.x == 0) {
+        kout[0] = __ldg(&keys[0]);
+        vout[0] = 0;
+    }
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        const uint32_t k = n == 1 ? __ldg(&keys[0]) : kout[j];
+        prev[j] = k;
+        if ((j & 31) == 0) sub[j >> 5] = k;
+        if ((j & (kIncTile - 1)) == 0) first[j >> kIncShift] = k;
+    }
+}
+
 size_t sort_inc_workspace_bytes(int n) { return IncLayout(n).total; }
 
+IncFlags sort_inc_flags_args(void* inc_ws, int n) {
+    const IncLayout L(n);
+    char* w = static_cast<char*>(inc_ws);
+    return IncFlags{reinterpret_cast<const unsigned*>(w + L.valid), reinterpret_cast<const uint32_t*>(w + L.prev),
+                    reinterpret_cast<uint32_t*>(w + L.bits),        reinterpret_cast<uint32_t*>(w + L.tcnt),
+                    reinterpret_cast<unsigned*>(w + L.over),        reinterpret_cast<int2*>(w + L.list),
+                    reinterpret_cast<uint32_t*>(w + L.lcount)};
+}
+
+void sort_inc_begin(cudaStream_t s, void* inc_ws, int n) {
+    const IncLayout L(n);
+    cudaMemsetAsync(static_cast<char*>(inc_ws) + L.zero, 0, L.zero_bytes, s);
+}
+
 void sort_pairs_incremental(cudaStream_t s, const uint32_t* keys, int n, int key_bits, uint32_t* kout,
-                            int32_t* vout, void* inc_ws, void* sort_ws, unsigned* flags, int num_sms) {
+                            int32_t* vout, void* inc_ws, void* sort_ws, unsigned* flags, int num_sms,
+                            cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, bool flags_done) {
     if (n <= 0) return;
     const IncLayout L(n);
     char* w = static_cast<char*>(inc_ws);
     unsigned* valid = reinterpret_cast<unsigned*>(w + L.valid);
     uint32_t* prev = reinterpret_cast<uint32_t*>(w + L.prev);
     uint32_t* first = reinterpret_cast<uint32_t*>(w + L.first);
+    uint32_t* sub = reinterpret_cast<uint32_t*>(w + L.sub);
     uint32_t* bits = reinterpret_cast<uint32_t*>(w + L.bits);
     int4* store = reinterpret_cast<int4*>(w + L.store);
     unsigned* over = reinterpret_cast<unsigned*>(w + L.over);
@@ -596,25 +680,37 @@ void sort_pairs_incremental(cudaStream_t s, const uint32_t* keys, int n, int key
     uint32_t* tcnt = reinterpret_cast<uint32_t*>(w + L.tcnt);
     uint32_t* tpre = reinterpret_cast<uint32_t*>(w + L.tpre);
     uint32_t* boff = reinterpret_cast<uint32_t*>(w + L.boff);
-    int32_t* list = reinterpret_cast<int32_t*>(w + L.list);
+    int2* list = reinterpret_cast<int2*>(w + L.list);
     uint32_t* lcount = reinterpret_cast<uint32_t*>(w + L.lcount);
     unsigned* done = reinterpret_cast<unsigned*>(w + L.done);
-    cudaMemsetAsync(w + L.zero, 0, L.zero_bytes, s);
-    k_inc_flags<<<L.tiles, kThreads, 0, s>>>(keys, prev, n, valid, bits, tcnt, over, list, lcount);
-    k_inc_place<<<2 * num_sms, kThreads, 0, s>>>(keys, list, lcount, prev, first, n, L.tiles, valid, bcnt, store, over,
-                                                 done, tcnt, tpre, boff);
+    if (!flags_done) {
+        cudaMemsetAsync(w + L.zero, 0, L.zero_bytes, s);
+        k_inc_flags<<<L.tiles, kThreads, 0, s>>>(keys, prev, n, valid, bits, tcnt, over, list, lcount);
+    }
+    const size_t fsm = L.tiles <= kIncSmemTiles ? 4 * (size_t)L.tiles : 0;
+    k_inc_place<<<2 * num_sms, kThreads, fsm, s>>>(list, lcount, prev, first, sub, n, L.tiles, valid, bcnt, store,
+                                                   over, done, tcnt, tpre, boff);
+    /* the gated full sort of (keys, identity) on the side stream, beside the merge (one of
+     * the two writes the result); prev is its scratch and its last pass writes kout / vout */
+    const bool fork_side = side != nullptr && fork != nullptr && join != nullptr;
+    cudaStream_t gs = fork_side ? side : s;
+    if (fork_side) {
+        cudaEventRecord(fork, s);
+        cudaStreamWaitEvent(side, fork, 0);
+    }
     if (n > 1 && sort_passes(key_bits) > 0) {
-        /* the full sort of (keys, identity), run only when the overflow word is set; prev is
-         * its scratch (rewritten from kout below) and its last pass writes kout / vout */
         uint32_t* kr;
         int32_t* vr;
         int32_t* vscr = reinterpret_cast<int32_t*>(w + L.vscr);
         const bool odd = (sort_passes(key_bits) & 1) != 0;
-        sort_pairs_impl(s, keys, nullptr, odd ? kout : prev, odd ? vout : vscr, odd ? prev : kout,
+        sort_pairs_impl(gs, keys, nullptr, odd ? kout : prev, odd ? vout : vscr, odd ? prev : kout,
                         odd ? vscr : vout, n, over, key_bits, sort_ws, flags, num_sms, &kr, &vr);
     }
+    if (fork_side) cudaEventRecord(join, side);
     k_inc_merge<<<L.tiles, kThreads, 0, s>>>(keys, n, bits, tcnt, tpre, boff, bcnt, store, over, kout, vout, prev,
-                                             first, valid);
+                                             first, sub);
+    if (fork_side) cudaStreamWaitEvent(s, join, 0);
+    k_inc_keep<<<2 * num_sms, kThreads, 0, s>>>(keys, n, over, kout, vout, prev, first, sub, valid);
 }
 
 }  // namespace sph

@@ -211,6 +211,10 @@ int sph_run_stage(sph_ctx* ctx, int stage);
  * names, comma-separated, to names. */
 int sph_profile_step(sph_ctx* ctx, int nsteps, float* ms_out, int max_groups, int* ngroups, char* names,
                      size_t names_len);
+/* The number of kernel launches in one step's CUDA graph (building the graph if the context
+ * steps through one and has none yet); 0 when the context steps without a graph.  No
+ * counterpart in the reference, whose launches are the enqueue calls of the step. */
+int sph_step_kernel_launches(sph_ctx* ctx, int* launches);
 /* Waits for the context stream. */
 int sph_synchronize(sph_ctx* ctx);
 
