@@ -150,8 +150,8 @@ __host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uin
 
 /* One axis of get_grid_coordinates (grid.h:74-91): floor((p - origin) / h) with IEEE
  * subtraction and division; COMPAT wraps modulo n, PHYSICS clamps into [0, n). */
-__device__ __forceinline__ int axis_cell(float p, float o, float h, int n, int wrap) {
-    float f = floorf(__fdiv_rn(__fsub_rn(p, o), h));
+__device__ __forceinline__ float axis_floor(float p, float o, float h) { return floorf(__fdiv_rn(__fsub_rn(p, o), h)); }
+__device__ __forceinline__ int axis_clamp(float f, int n, int wrap) {
     if (wrap) {
         if (!(f > -1e9f && f < 1e9f)) f = 0.f;
         int c = (int)f + n;
@@ -160,6 +160,9 @@ __device__ __forceinline__ int axis_cell(float p, float o, float h, int n, int w
     if (!(f >= 0.f)) return 0;
     if (f > (float)(n - 1)) return n - 1;
     return (int)f;
+}
+__device__ __forceinline__ int axis_cell(float p, float o, float h, int n, int wrap) {
+    return axis_clamp(axis_floor(p, o, h), n, wrap);
 }
 __device__ __forceinline__ void cell_of(const Const& c, float x, float y, float z, int& cx, int& cy, int& cz) {
     cx = axis_cell(x, c.ox, c.cell, c.nx, c.wrap);

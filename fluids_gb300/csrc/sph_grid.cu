@@ -29,17 +29,16 @@ __device__ __forceinline__ uint32_t hash_particle(const Const& c0, const float4 
     Const c = c0;
     const uint32_t sid = scene_of ? (uint32_t)scene_of[i] : 0u;
     scene_setup(c, scenes, scene_of, i);
-    int cx, cy, cz;
-    cell_of(c, p.x, p.y, p.z, cx, cy, cz);
+    /* cell_of, with each axis's division done once for the cell and the escape test */
+    const float fx = axis_floor(p.x, c.ox, c.cell), fy = axis_floor(p.y, c.oy, c.cell),
+                fz = axis_floor(p.z, c.oz, c.cell);
     if (!c.wrap) {
         /* PHYSICS grid clamps: report particles outside it (informational) */
-        const float fx = floorf(__fdiv_rn(__fsub_rn(p.x, c.ox), c.cell));
-        const float fy = floorf(__fdiv_rn(__fsub_rn(p.y, c.oy), c.cell));
-        const float fz = floorf(__fdiv_rn(__fsub_rn(p.z, c.oz), c.cell));
         const bool out = !(fx >= 0.f && fx < (float)c.nx && fy >= 0.f && fy < (float)c.ny && fz >= 0.f &&
                            fz < (float)c.nz);
         if (out) atomicOr(flags, kFlagEscaped);
     }
+    const int cx = axis_clamp(fx, c.nx, c.wrap), cy = axis_clamp(fy, c.ny, c.wrap), cz = axis_clamp(fz, c.nz, c.wrap);
     /* batched: the scene id above the Morton bits keeps every scene's range contiguous */
     return (sid << c.scene_shift) | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
 }
