@@ -44,7 +44,8 @@ EXPORTS = ["sph_default_params", "sph_create", "sph_destroy", "sph_last_error", 
            "sph_synchronize", "sph_device_flags", "sph_field_elems", "sph_field_kind", "sph_get_field",
            "sph_set_field", "sph_field_device_ptr", "sph_body_forces", "sph_stats", "sph_sort_pairs",
            "sph_scene_box_volume", "sph_scene_fishtank", "sph_scene_cube", "sph_jitter", "sph_cuda_available",
-           "sph_describe", "sph_profile_step", "sph_step_kernel_launches", "sph_sort_pairs_noalloc",
+           "sph_describe", "sph_profile_step", "sph_step_kernel_launches", "sph_simulate_host",
+           "sph_sort_pairs_noalloc",
            "sph_batch_create",
            "sph_batch_scene_count", "sph_batch_scene_range", "sph_batch_stats", "sph_batch_scene_grid",
            "sph_adj_create", "sph_adj_destroy", "sph_adj_last_error", "sph_adj_forward", "sph_adj_backward",
@@ -182,6 +183,7 @@ def lib():
             "sph_describe": (ip, [PP, fp, C.POINTER(SphDerived)]),
             "sph_profile_step": (ip, [vp, ip, C.POINTER(C.c_float), ip, C.POINTER(ip), C.c_char_p, C.c_size_t]),
             "sph_step_kernel_launches": (ip, [vp, C.POINTER(ip)]),
+            "sph_simulate_host": (ip, [vp, fp, fp, fp, ip]),
             "sph_sort_pairs_noalloc": (ip, [vp, vp, vp, vp, ip, ip, vp]),
             "sph_batch_create": (ip, [PP, ip, C.POINTER(SceneDesc), C.POINTER(vp)]),
             "sph_batch_scene_count": (ip, [vp]),
@@ -453,6 +455,17 @@ class Context:
         self._c(self._lib.sph_profile_step(self.h, int(nsteps), ms, 64, C.byref(ng), names, 4096))
         keys = names.value.decode().split(",") if ng.value else []
         return dict(zip(keys, [float(ms[i]) for i in range(ng.value)]))
+
+    def simulate_host(self, pos4, vel4, vhalf4=None, steps=1):
+        """sph_simulate_host: steps with the state in host arrays (float32, (N, 4), C order),
+        updated in place; waits for the context stream before returning."""
+        arrs = [pos4, vel4] + ([vhalf4] if vhalf4 is not None else [])
+        for a in arrs:
+            if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"] or a.size != 4 * self.particle_count():
+                raise ValueError("host state arrays must be C-contiguous float32 of shape (N, 4)")
+        self._c(self._lib.sph_simulate_host(self.h, pos4.ctypes.data, vel4.ctypes.data,
+                                            vhalf4.ctypes.data if vhalf4 is not None else None, int(steps)))
+        self._c(self._lib.sph_synchronize(self.h))
 
     def step_kernel_launches(self):
         """Kernel launches in one step's CUDA graph (0 without a graph)."""

@@ -316,7 +316,13 @@ void drop_graph(sph_ctx* x) {
         cudaGraphExecDestroy(x->gexec);
         x->gexec = nullptr;
     }
+    if (x->host_gexec) {
+        cudaGraphExecDestroy(x->host_gexec);
+        x->host_gexec = nullptr;
+    }
+    x->host_key[0] = x->host_key[1] = x->host_key[2] = nullptr;
     x->graph_ok = true;
+    x->host_graph_ok = true;
 }
 
 /* Sorts the boundary particles (boundaryhandler.cpp:216-236) and builds their cell table. */
@@ -440,7 +446,9 @@ void mark(sph_ctx* x, const char* name) {
     x->prof_names.push_back(name);
 }
 
-int enqueue_step(sph_ctx* x, int pci_max_iter) {
+/* vel_ready: null, or an event after which the unsorted velocities are in place (the host
+ * step's uploads); the step then gathers them after the list pass, which does not read them. */
+int enqueue_step(sph_ctx* x, int pci_max_iter, cudaEvent_t vel_ready) {
     if (x->N <= 0) return SPH_OK;
     Bufs& b = x->b;
     const Const& c = x->c;
@@ -471,10 +479,20 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
         mark(x, pre_names[k]);
     }
     /* the SHUFFLE and CELL_INTERVALS stages in one pass */
-    sph::launch_gather_ranges(s, c, x->N, b.mask_sorted, b.pos, b.pos_s, b.vel, b.vel_s,
-                              x->p.method == SPH_WCSPH ? b.vhalf : nullptr, b.vhalf_s, b.ids, b.ids_s, b.keys_sorted,
-                              b.tab, b.cell_prev, b.flags, bs, b.scenes, b.scene_of);
+    const bool late_vel = vel_ready != nullptr;
+    float4* const vh = x->p.method == SPH_WCSPH ? b.vhalf : nullptr;
+    sph::launch_gather_ranges(s, c, x->N, b.mask_sorted, b.pos, b.pos_s, late_vel ? nullptr : b.vel, b.vel_s,
+                              late_vel ? nullptr : vh, b.vhalf_s, b.ids, b.ids_s, b.keys_sorted, b.tab, b.cell_prev,
+                              b.flags, bs, b.scenes, b.scene_of);
     mark(x, "k_gather_ranges");
+    /* the velocities' part of the gather, once they have arrived (after the list pass) */
+    auto gather_vel = [&]() {
+        if (!late_vel) return;
+        cudaStreamWaitEvent(s, vel_ready, 0);
+        sph::launch_gather(s, x->N, b.mask_sorted, b.vel, b.vel_s, vh, b.vhalf_s, nullptr, nullptr, nullptr, nullptr,
+                           bs);
+        mark(x, "k_gather_vel");
+    };
     if (x->p.method == SPH_WCSPH) {
         const bool lists = x->p.neighbor_mode == SPH_NEIGH_LIST;
         if (lists) {
@@ -484,6 +502,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
             sph::launch_wc_density(s, c, b, false, bs);
             mark(x, "k_wc_density");
         }
+        gather_vel();
         const bool pack = lists && c.sigma != 0.f;
         if (c.sigma != 0.f) {
             sph::launch_normals(s, c, b, lists, bs, pack);
@@ -508,6 +527,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter) {
             sph::launch_pci_init_density(s, c, b, bs);
             mark(x, "k_pci_init_density");
         }
+        gather_vel();
         /* with surface tension the normal pass also writes the packed per-neighbour records
          * (velocity, normal, 1/rho) that the force pass reads */
         const bool pack = c.sigma != 0.f;
@@ -544,7 +564,7 @@ int build_graph(sph_ctx* x) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) { x->graph_ok = false; cudaGetLastError(); return SPH_OK; }
-    int rc = enqueue_step(x, x->c.pci_max_iter);
+    int rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
     e = cudaStreamEndCapture(x->stream, &g);
     if (rc != SPH_OK || e != cudaSuccess || !g) {
         if (g) cudaGraphDestroy(g);
@@ -767,7 +787,7 @@ int rebuild(sph_ctx* x, bool keep) {
 int relax(sph_ctx* x) {
     if (x->p.method != SPH_PCISPH || !x->p.relax_on_add || x->N <= 0) return SPH_OK;
     int relax_iter = x->p.pcisph_relax_max_iterations > 0 ? x->p.pcisph_relax_max_iterations : 10000;
-    int rc = enqueue_step(x, relax_iter);
+    int rc = enqueue_step(x, relax_iter, nullptr);
     if (rc != SPH_OK) return rc;
     SPH_CUDA(x, cudaMemsetAsync(x->b.vel, 0, 16 * (size_t)x->N, x->stream));
     return SPH_OK;
@@ -861,12 +881,53 @@ SortCache g_sort;
 
 int sph_ctx_fail(sph_ctx* x, int code, const std::string& msg) { return fail(x, code, msg); }
 
+static bool same_or_built(const sph_ctx* x, const void* const* key) {
+    return x->host_key[0] == key[0] && x->host_key[1] == key[1] && x->host_key[2] == key[2];
+}
+
 static void release_side(sph_ctx* x) {
     if (x->side) cudaStreamDestroy(x->side);
     if (x->ev_fork) cudaEventDestroy(x->ev_fork);
     if (x->ev_join) cudaEventDestroy(x->ev_join);
-    x->side = nullptr;
-    x->ev_fork = x->ev_join = nullptr;
+    if (x->copy_stream) cudaStreamDestroy(x->copy_stream);
+    if (x->ev_copy) cudaEventDestroy(x->ev_copy);
+    if (x->ev_vel) cudaEventDestroy(x->ev_vel);
+    x->side = x->copy_stream = nullptr;
+    x->ev_fork = x->ev_join = x->ev_copy = x->ev_vel = nullptr;
+}
+
+/* One step with the state on the host (sph_simulate_host): position in on the context
+ * stream, velocities in on the copy stream (the step waits for them only before its
+ * velocity gather, after the list pass), the step, the state back out. */
+static int enqueue_host_step(sph_ctx* x, float* pos4, float* vel4, float* vhalf4) {
+    const cudaStream_t s = x->stream;
+    const size_t bytes = 16 * (size_t)x->N;
+    Bufs& b = x->b;
+    const bool wc = x->p.method == SPH_WCSPH && vhalf4 != nullptr;
+    if (cudaMemcpyAsync(b.pos, pos4, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return cuda_fail(x, cudaGetLastError(), "position upload");
+    cudaEvent_t vel_ready = nullptr;
+    if (x->copy_stream && x->ev_copy && x->ev_vel) {
+        cudaEventRecord(x->ev_copy, s);
+        cudaStreamWaitEvent(x->copy_stream, x->ev_copy, 0);
+        cudaMemcpyAsync(b.vel, vel4, bytes, cudaMemcpyHostToDevice, x->copy_stream);
+        if (wc) cudaMemcpyAsync(b.vhalf, vhalf4, bytes, cudaMemcpyHostToDevice, x->copy_stream);
+        cudaEventRecord(x->ev_vel, x->copy_stream);
+        vel_ready = x->ev_vel;
+    } else {
+        cudaMemcpyAsync(b.vel, vel4, bytes, cudaMemcpyHostToDevice, s);
+        if (wc) cudaMemcpyAsync(b.vhalf, vhalf4, bytes, cudaMemcpyHostToDevice, s);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(x, e, "velocity upload");
+    int rc = enqueue_step(x, x->c.pci_max_iter, vel_ready);
+    if (rc != SPH_OK) return rc;
+    cudaMemcpyAsync(pos4, b.pos, bytes, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(vel4, b.vel, bytes, cudaMemcpyDeviceToHost, s);
+    if (wc) cudaMemcpyAsync(vhalf4, b.vhalf, bytes, cudaMemcpyDeviceToHost, s);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(x, e, "state download");
+    return SPH_OK;
 }
 
 extern "C" {
@@ -1067,7 +1128,10 @@ int sph_create(const sph_params* params, sph_ctx** out) {
     x->own_stream = true;
     if (cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&x->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&x->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&x->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&x->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->ev_copy, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->ev_vel, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();   /* then everything runs on the main stream */
         release_side(x);
     }
@@ -1093,6 +1157,7 @@ int sph_destroy(sph_ctx* x) {
     cudaFree(x->frame_buf);
     if (x->own_stream && x->stream) cudaStreamDestroy(x->stream);
     if (x->side) cudaStreamSynchronize(x->side);
+    if (x->copy_stream) cudaStreamSynchronize(x->copy_stream);
     release_side(x);
     delete x;
     return SPH_OK;
@@ -1299,7 +1364,7 @@ int sph_simulate(sph_ctx* x, int nsteps) {
         drop_graph(x);
         x->inject = 0;
         x->c.barrier_extra = 1;
-        const int rc = enqueue_step(x, x->c.pci_max_iter);
+        const int rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
         x->c.barrier_extra = 0;
         if (rc != SPH_OK) return rc;
         return sph_simulate(x, nsteps - 1);
@@ -1312,7 +1377,7 @@ int sph_simulate(sph_ctx* x, int nsteps) {
         if (x->gexec) {
             SPH_CUDA(x, cudaGraphLaunch(x->gexec, x->stream));
         } else {
-            int rc = enqueue_step(x, x->c.pci_max_iter);
+            int rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
             if (rc != SPH_OK) return rc;
         }
     }
@@ -1338,7 +1403,7 @@ int sph_profile_step(sph_ctx* x, int nsteps, float* ms_out, int max_groups, int*
         ev.clear();
         x->prof_names.clear();
         x->prof = &ev;
-        rc = enqueue_step(x, x->c.pci_max_iter);
+        rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
         x->prof = nullptr;
         if (rc != SPH_OK) break;
         cudaError_t e = cudaStreamSynchronize(x->stream);
@@ -1393,6 +1458,53 @@ int sph_run_stage(sph_ctx* x, int stage) {
     if (check_ctx(x)) return SPH_E_INVALID;
     if (!x->has_state) return fail(x, SPH_E_STATE, "no particles added");
     return run_stage_impl(x, stage);
+}
+
+int sph_simulate_host(sph_ctx* x, float* pos4, float* vel4, float* vhalf4, int nsteps) {
+    NvtxRange range("sph_simulate_host");
+    if (check_ctx(x)) return SPH_E_INVALID;
+    if (nsteps < 0) return fail(x, SPH_E_INVALID, "nsteps < 0");
+    if (!x->has_state || x->N <= 0 || nsteps == 0) return SPH_OK;
+    if (!pos4 || !vel4 || (x->p.method == SPH_WCSPH && !vhalf4))
+        return fail(x, SPH_E_INVALID, "sph_simulate_host: pos4, vel4 (and vhalf4 for WCSPH) are required");
+    if (x->inject == SPH_FAULT_BARRIER_STALL) return fail(x, SPH_E_STATE, "sph_simulate_host: a fault is armed");
+    const void* key[3] = {pos4, vel4, vhalf4};
+    const bool same = x->host_key[0] == key[0] && x->host_key[1] == key[1] && x->host_key[2] == key[2];
+    if (x->p.use_graph && x->host_graph_ok && (!x->host_gexec || !same)) {
+        /* one graph per set of host buffers: the copies' pointers are part of it (a capture
+         * that fails, e.g. on pageable buffers, leaves the stream-ordered path) */
+        if (x->host_gexec) {
+            cudaGraphExecDestroy(x->host_gexec);
+            x->host_gexec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? enqueue_host_step(x, pos4, vel4, vhalf4) : SPH_E_CUDA;
+        if (e == cudaSuccess) e = cudaStreamEndCapture(x->stream, &g);
+        if (rc == SPH_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&x->host_gexec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (rc != SPH_OK || e != cudaSuccess || !x->host_gexec) {
+            cudaGetLastError();
+            x->err.clear();
+            x->host_gexec = nullptr;
+            x->host_graph_ok = false;
+        } else {
+            x->host_key[0] = key[0];
+            x->host_key[1] = key[1];
+            x->host_key[2] = key[2];
+        }
+    }
+    for (int k = 0; k < nsteps; ++k) {
+        if (x->host_gexec && same_or_built(x, key)) {
+            SPH_CUDA(x, cudaGraphLaunch(x->host_gexec, x->stream));
+        } else {
+            const int rc = enqueue_host_step(x, pos4, vel4, vhalf4);
+            if (rc != SPH_OK) return rc;
+        }
+    }
+    x->cur_keys = x->b.keys_sorted;
+    x->cur_mask = x->b.mask_sorted;
+    return SPH_OK;
 }
 
 int sph_step_kernel_launches(sph_ctx* x, int* launches) {

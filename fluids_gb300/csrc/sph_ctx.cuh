@@ -32,6 +32,13 @@ struct sph_ctx {
      * (the gated full sort of the step's incremental sort) */
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    /* sph_simulate_host: the stream and events of the velocity uploads, and the step graph
+     * with its copies for one set of host buffers */
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy = nullptr, ev_vel = nullptr;
+    cudaGraphExec_t host_gexec = nullptr;
+    const void* host_key[3] = {nullptr, nullptr, nullptr};
+    bool host_graph_ok = true;
     int device = 0, num_sms = 1;
     std::string err;
     float lim[3] = {0.f, 0.f, 0.f};

@@ -122,7 +122,7 @@ __global__ void k_gather(int n, const int32_t* __restrict__ perm, const float4* 
     if (i >= n) return;
     const int src = perm[i];
     as[i] = __ldg(&a[src]);
-    bs[i] = __ldg(&b[src]);
+    if (b) bs[i] = __ldg(&b[src]);
     if (c3) cs[i] = __ldg(&c3[src]);
     if (ids) ids_s[i] = __ldg(&ids[src]);
 }
@@ -188,7 +188,7 @@ __global__ void k_gather_ranges(Const c, int n, const int32_t* __restrict__ perm
     const int src = __ldg(&perm[i]);
     const float4 p = __ldg(&a[src]);
     as[i] = p;
-    bs[i] = __ldg(&b[src]);
+    if (b) bs[i] = __ldg(&b[src]);   /* null: the velocities are gathered later */
     if (c3) cs[i] = __ldg(&c3[src]);
     if (ids) ids_s[i] = __ldg(&ids[src]);
     int* t = reinterpret_cast<int*>(tab);

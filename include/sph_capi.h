@@ -202,6 +202,16 @@ int sph_boundary_particle_count(const sph_ctx* ctx);
 /* FluidSimulation::simulate (fluidsimulation.h:36) called nsteps times; asynchronous on the
  * context stream (a CUDA graph per step when use_graph = 1). */
 int sph_simulate(sph_ctx* ctx, int nsteps);
+/* nsteps steps with the particle state on the host: each step uploads pos4, vel4 and (WCSPH)
+ * vhalf4 -- 4 floats per particle in the context's current particle order, the layout of the
+ * POS, VEL and VEL_HALF fields -- runs the step of sph_simulate and downloads the three back
+ * into the same buffers.  The velocity uploads run beside the step's binning, sort and list
+ * pass, which do not read them.  Asynchronous on the context stream like sph_simulate; the
+ * buffers must stay valid until it completes.  With use_graph = 1 and page-locked buffers
+ * the step and its copies are one CUDA graph per set of buffers.  Same results as
+ * sph_set_field_async, sph_simulate(ctx, 1) and sph_get_field_async per step.  No
+ * counterpart in the reference, whose state stays on the device between steps. */
+int sph_simulate_host(sph_ctx* ctx, float* pos4, float* vel4, float* vhalf4, int nsteps);
 /* Runs one stage (one reference launch point) on the current state. */
 int sph_run_stage(sph_ctx* ctx, int stage);
 /* Runs nsteps steps of the same kernel sequence as sph_simulate, without the graph, with a
