@@ -13,6 +13,7 @@
  *   - boundary handling: BoundaryHandler (boundaryhandler.cpp:95-349); static bodies are
  *     transformed, sorted and given their Psi once, not re-sorted every step.
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -446,9 +447,23 @@ void mark(sph_ctx* x, const char* name) {
     x->prof_names.push_back(name);
 }
 
+/* The host buffers of sph_simulate_host; chunked: the force pass's parts download their
+ * particles' new state as they finish (single-scene WCSPH with the copy stream). */
+struct HostState {
+    float *pos4, *vel4, *vhalf4;
+    bool chunked;
+};
+static void download_range(sph_ctx* x, const HostState& h, size_t i0, size_t i1, cudaStream_t st) {
+    const size_t off = 4 * i0, bytes = 16 * (i1 - i0);
+    cudaMemcpyAsync(h.pos4 + off, x->b.pos + i0, bytes, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(h.vel4 + off, x->b.vel + i0, bytes, cudaMemcpyDeviceToHost, st);
+    if (h.vhalf4) cudaMemcpyAsync(h.vhalf4 + off, x->b.vhalf + i0, bytes, cudaMemcpyDeviceToHost, st);
+}
+
 /* vel_ready: null, or an event after which the unsorted velocities are in place (the host
- * step's uploads); the step then gathers them after the list pass, which does not read them. */
-int enqueue_step(sph_ctx* x, int pci_max_iter, cudaEvent_t vel_ready) {
+ * step's uploads); the step then gathers them after the list pass, which does not read them.
+ * out: null, or the host buffers the step's new state goes to. */
+int enqueue_step(sph_ctx* x, int pci_max_iter, cudaEvent_t vel_ready, const HostState* out) {
     if (x->N <= 0) return SPH_OK;
     Bufs& b = x->b;
     const Const& c = x->c;
@@ -513,7 +528,28 @@ int enqueue_step(sph_ctx* x, int pci_max_iter, cudaEvent_t vel_ready) {
             if (x->any_dynamic) sph::launch_body_integrate(s, c, b, (int)x->bodies.size());
             mark(x, "k_bnd_forces");
         }
-        sph::launch_wc_forces(s, c, b, lists, true, false, bs, pack);
+        if (out && out->chunked) {
+            /* the force pass (with the integration) in parts, each part's new state downloaded
+             * on the copy stream while the next part computes */
+            const int nb = (x->N + bs - 1) / bs;
+            const int K = sph_ctx::kOutChunks;
+            for (int k = 0; k < K; ++k) {
+                const int b0 = (int)((long long)nb * k / K), b1 = (int)((long long)nb * (k + 1) / K);
+                if (b1 <= b0) continue;
+                sph::Const ck = c;
+                ck.block0 = b0;
+                ck.blocks = b1 - b0;
+                sph::launch_wc_forces(s, ck, b, lists, true, false, bs, pack);
+                const size_t i0 = (size_t)b0 * bs, i1 = std::min((size_t)b1 * bs, (size_t)x->N);
+                cudaEventRecord(x->ev_chunk[k], s);
+                cudaStreamWaitEvent(x->copy_stream, x->ev_chunk[k], 0);
+                download_range(x, *out, i0, i1, x->copy_stream);
+            }
+            cudaEventRecord(x->ev_copy, x->copy_stream);
+            cudaStreamWaitEvent(s, x->ev_copy, 0);
+        } else {
+            sph::launch_wc_forces(s, c, b, lists, true, false, bs, pack);
+        }
         mark(x, "k_wc_forces");
     } else {
         if (!c.compat && !c.batched) {
@@ -564,7 +600,7 @@ int build_graph(sph_ctx* x) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) { x->graph_ok = false; cudaGetLastError(); return SPH_OK; }
-    int rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
+    int rc = enqueue_step(x, x->c.pci_max_iter, nullptr, nullptr);
     e = cudaStreamEndCapture(x->stream, &g);
     if (rc != SPH_OK || e != cudaSuccess || !g) {
         if (g) cudaGraphDestroy(g);
@@ -787,7 +823,7 @@ int rebuild(sph_ctx* x, bool keep) {
 int relax(sph_ctx* x) {
     if (x->p.method != SPH_PCISPH || !x->p.relax_on_add || x->N <= 0) return SPH_OK;
     int relax_iter = x->p.pcisph_relax_max_iterations > 0 ? x->p.pcisph_relax_max_iterations : 10000;
-    int rc = enqueue_step(x, relax_iter, nullptr);
+    int rc = enqueue_step(x, relax_iter, nullptr, nullptr);
     if (rc != SPH_OK) return rc;
     SPH_CUDA(x, cudaMemsetAsync(x->b.vel, 0, 16 * (size_t)x->N, x->stream));
     return SPH_OK;
@@ -892,6 +928,10 @@ static void release_side(sph_ctx* x) {
     if (x->copy_stream) cudaStreamDestroy(x->copy_stream);
     if (x->ev_copy) cudaEventDestroy(x->ev_copy);
     if (x->ev_vel) cudaEventDestroy(x->ev_vel);
+    for (auto& e : x->ev_chunk) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
     x->side = x->copy_stream = nullptr;
     x->ev_fork = x->ev_join = x->ev_copy = x->ev_vel = nullptr;
 }
@@ -920,11 +960,13 @@ static int enqueue_host_step(sph_ctx* x, float* pos4, float* vel4, float* vhalf4
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(x, e, "velocity upload");
-    int rc = enqueue_step(x, x->c.pci_max_iter, vel_ready);
+    HostState out{pos4, vel4, wc ? vhalf4 : nullptr, false};
+    /* the WCSPH force pass of a single-scene context ends the step: its parts download as
+     * they finish */
+    out.chunked = vel_ready != nullptr && x->p.method == SPH_WCSPH && !x->c.batched;
+    int rc = enqueue_step(x, x->c.pci_max_iter, vel_ready, &out);
     if (rc != SPH_OK) return rc;
-    cudaMemcpyAsync(pos4, b.pos, bytes, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(vel4, b.vel, bytes, cudaMemcpyDeviceToHost, s);
-    if (wc) cudaMemcpyAsync(vhalf4, b.vhalf, bytes, cudaMemcpyDeviceToHost, s);
+    if (!out.chunked) download_range(x, out, 0, (size_t)x->N, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(x, e, "state download");
     return SPH_OK;
@@ -1131,7 +1173,12 @@ int sph_create(const sph_params* params, sph_ctx** out) {
         cudaEventCreateWithFlags(&x->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&x->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&x->ev_copy, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&x->ev_vel, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&x->ev_vel, cudaEventDisableTiming) != cudaSuccess ||
+        [&]() {
+            for (auto& e : x->ev_chunk)
+                if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return true;
+            return false;
+        }()) {
         cudaGetLastError();   /* then everything runs on the main stream */
         release_side(x);
     }
@@ -1364,7 +1411,7 @@ int sph_simulate(sph_ctx* x, int nsteps) {
         drop_graph(x);
         x->inject = 0;
         x->c.barrier_extra = 1;
-        const int rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
+        const int rc = enqueue_step(x, x->c.pci_max_iter, nullptr, nullptr);
         x->c.barrier_extra = 0;
         if (rc != SPH_OK) return rc;
         return sph_simulate(x, nsteps - 1);
@@ -1377,7 +1424,7 @@ int sph_simulate(sph_ctx* x, int nsteps) {
         if (x->gexec) {
             SPH_CUDA(x, cudaGraphLaunch(x->gexec, x->stream));
         } else {
-            int rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
+            int rc = enqueue_step(x, x->c.pci_max_iter, nullptr, nullptr);
             if (rc != SPH_OK) return rc;
         }
     }
@@ -1403,7 +1450,7 @@ int sph_profile_step(sph_ctx* x, int nsteps, float* ms_out, int max_groups, int*
         ev.clear();
         x->prof_names.clear();
         x->prof = &ev;
-        rc = enqueue_step(x, x->c.pci_max_iter, nullptr);
+        rc = enqueue_step(x, x->c.pci_max_iter, nullptr, nullptr);
         x->prof = nullptr;
         if (rc != SPH_OK) break;
         cudaError_t e = cudaStreamSynchronize(x->stream);

@@ -36,6 +36,8 @@ struct sph_ctx {
      * with its copies for one set of host buffers */
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copy = nullptr, ev_vel = nullptr;
+    static constexpr int kOutChunks = 4;   /* force pass parts whose results download early */
+    cudaEvent_t ev_chunk[kOutChunks] = {};
     cudaGraphExec_t host_gexec = nullptr;
     const void* host_key[3] = {nullptr, nullptr, nullptr};
     bool host_graph_ok = true;

@@ -41,6 +41,8 @@ struct Const {
     int monaghan;        /* COMPAT with the Monaghan kernels (sph_params::kernels) */
     int ntiles;          /* batched: entries of the scene tile table (SceneTile) */
     int tile_blocks;     /* batched: CTAs of a persistent launch over the tiles */
+    int block0, blocks;  /* single-scene passes launched in parts: blocks [block0, block0 + blocks)
+                            of the whole pass (0, 0: the whole pass in one launch) */
 };
 
 /* One scene of a batched context: its grid (origin, dimensions, offset of its cells in the
@@ -112,7 +114,7 @@ __device__ __forceinline__ void for_each_particle(const Const& c0, const SceneTi
             }
         }
     } else {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        const int i = (c0.block0 + (int)blockIdx.x) * (int)blockDim.x + (int)threadIdx.x;
         if (i < c0.n) f(c0, 0LL, i);
     }
 }

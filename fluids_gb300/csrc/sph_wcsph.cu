@@ -385,7 +385,7 @@ static inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
 template <bool BATCH>
 static inline int grid_for(const Const& c, int bs) {
     if constexpr (BATCH) return c.tile_blocks > 0 ? c.tile_blocks : 1;
-    return nblk(c.n, bs);
+    return c.blocks > 0 ? c.blocks : nblk(c.n, bs);
 }
 /* a batched pass's tile counter, zeroed on the stream before its launch (slot: 0 density,
  * 1 list build, 2 normals, 3 forces) */
