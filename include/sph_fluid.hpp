@@ -393,6 +393,12 @@ class CudaFluidSimulation : public FluidSimulation {
     void simulate() override { check(sph_simulate(ctx_, 1), ctx_); }
     /* n steps in one call (one graph replay each, no host round trip in between) */
     void simulate(int steps) { check(sph_simulate(ctx_, steps), ctx_); }
+    /* steps with the state in host buffers (4 floats per particle each, updated in place;
+     * vhalf4 may be null for PCISPH), the copies beside the step's work; waits for them */
+    void simulate_host(float* pos4, float* vel4, float* vhalf4, int steps = 1) {
+        check(sph_simulate_host(ctx_, pos4, vel4, vhalf4, steps), ctx_);
+        check(sph_synchronize(ctx_), ctx_);
+    }
     void reset(const PhysicsSettings& ph, const SimulationSettings& si) override {
         params_ = to_params(ph, si, opt_);
         check(sph_reset(ctx_, &params_), ctx_);
