@@ -294,17 +294,18 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
  *                buckets below t) + its rank, a stayed particle of stayed rank a to a + (moved
  *                particles of the buckets below t) + (bucket particles below it).
  *   k_inc_keep   after an overflow, keeps the full sort's keys as prev; marks prev valid.
- * A bucket holds kIncBucket particles.  When one overflows, or there is no previous result
- * (the first call), the overflow word opens the gated full onesweep sort of all keys (its
- * kernels read the word and leave at once while it is 0; they run on a side stream beside
- * k_inc_merge, which then leaves at once).  Moved particles are 1-2 % of a flowing scene per
+ * A bucket holds kIncBucket particles.  When one overflows, when more than a sixth of the
+ * particles moved (their searches would cost more than a full sort), or when there is no
+ * previous result (the first call), the overflow word opens the gated full onesweep sort of
+ * all keys (its kernels read the word and leave at once while it is 0; they run on a side
+ * stream beside k_inc_merge, which then leaves at once).  Moved particles are 1-2 % of a flowing scene per
  * step: the passes over all particles then read 8 bytes and write 12 bytes per particle.
  * ------------------------------------------------------------------------------------- */
 namespace {
 static_assert(kIncTile == kThreads * kIncItems, "2048 positions = 64 ballot words");
 constexpr int kIncShift = 11;
 constexpr int kIncWords = kIncTile / 32;
-constexpr int kIncBucket = 256;                  /* moved particles per merge tile before overflow */
+constexpr int kIncBucket = 1024;                 /* moved particles per merge tile before overflow */
 
 struct IncLayout {
     size_t valid, prev, first, sub, bits, list, store, zero, over, lcount, done, bcnt, tcnt, tpre, boff, vscr, total,
@@ -416,11 +417,16 @@ __global__ void __launch_bounds__(kThreads) k_inc_place(const int2* __restrict__
     __shared__ uint32_t s_scan[kWarps];
     __shared__ bool s_last;
     if (*valid == 0u) return;   /* no previous result: the full sort runs */
+    const int m = (int)*lcount;
+    if (m > n / 6) {
+        /* past a sixth of the particles moved, the searches cost more than the full sort */
+        if (blockIdx.x == 0 && threadIdx.x == 0) *over = 1u;
+        return;
+    }
     const bool staged = tiles <= kIncSmemTiles;
     if (staged)
         for (int t = threadIdx.x; t < tiles; t += blockDim.x) s_first[t] = __ldg(&first[t]);
     __syncthreads();
-    const int m = (int)*lcount;
     const int words = (n + 31) >> 5;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
         const int2 e = __ldg(&list[r]);
@@ -526,8 +532,8 @@ __global__ void __launch_bounds__(kThreads) k_inc_merge(const uint32_t* __restri
                                                         uint32_t* __restrict__ kout, int32_t* __restrict__ vout,
                                                         uint32_t* __restrict__ prev, uint32_t* __restrict__ first,
                                                         uint32_t* __restrict__ sub) {
-    __shared__ uint32_t s_k[kIncBucket];
-    __shared__ int32_t s_i[kIncBucket], s_p[kIncBucket];
+    __shared__ uint32_t s_k[kIncBucket], s_gk[kIncBucket];
+    __shared__ int32_t s_i[kIncBucket], s_p[kIncBucket], s_g[kIncBucket], s_gi[kIncBucket];
     __shared__ uint32_t s_at[kIncTile + 1];   /* bucket particles inserted at each position */
     __shared__ uint32_t s_word[kIncWords], s_wpre[kIncWords];
     __shared__ uint32_t s_scan[kWarps];
@@ -560,7 +566,7 @@ __global__ void __launch_bounds__(kThreads) k_inc_merge(const uint32_t* __restri
         s_k[e] = (uint32_t)v.x;
         s_i[e] = v.y;
         s_p[e] = v.z;
-        atomicAdd(&s_at[v.z - tbase], 1u);   /* p in [tbase, tbase + tlen] */
+        s_g[e] = (int)atomicAdd(&s_at[v.z - tbase], 1u);   /* p in [tbase, tbase + tlen]; its place in p's group */
     }
     uint32_t wrun = 0;
 #pragma unroll
@@ -585,15 +591,24 @@ __global__ void __launch_bounds__(kThreads) k_inc_merge(const uint32_t* __restri
 #pragma unroll
     for (int k = 0; k < kIncItems; ++k) s_at[tid * kIncItems + k] = before + loc[k];
     __syncthreads();
-    /* the bucket's particles: those with a smaller insertion point are below; equal points
-     * compare by (key, index) */
+    /* the bucket's particles: those with a smaller insertion point are below; those with the
+     * same point (grouped by it, in any order) compare by (key, index) */
+    for (int e = tid; e < c; e += kThreads) {
+        const int lp = s_p[e] - tbase;
+        const int excl = lp > 0 ? (int)s_at[lp - 1] : 0;
+        s_gk[excl + s_g[e]] = s_k[e];
+        s_gi[excl + s_g[e]] = s_i[e];
+    }
+    __syncthreads();
     for (int e = tid; e < c; e += kThreads) {
         const uint32_t k = s_k[e];
         const int32_t i = s_i[e];
         const int p = s_p[e];
         const int lp = p - tbase;
-        int r = lp > 0 ? (int)s_at[lp - 1] : 0;
-        for (int f = 0; f < c; ++f) r += (s_p[f] == p && pair_less(s_k[f], s_i[f], k, i)) ? 1 : 0;
+        const int excl = lp > 0 ? (int)s_at[lp - 1] : 0;
+        const int gend = lp < kIncTile ? (int)s_at[lp] : c;
+        int r = excl;
+        for (int f = excl; f < gend; ++f) r += pair_less(s_gk[f], s_gi[f], k, i) ? 1 : 0;
         uint32_t mb = tile_pre + tile_moved;   /* p at the tile's end */
         if (lp < tlen) {
             const int lw = lp >> 5;
@@ -688,7 +703,7 @@ void sort_pairs_incremental(cudaStream_t s, const uint32_t* keys, int n, int key
         k_inc_flags<<<L.tiles, kThreads, 0, s>>>(keys, prev, n, valid, bits, tcnt, over, list, lcount);
     }
     const size_t fsm = L.tiles <= kIncSmemTiles ? 4 * (size_t)L.tiles : 0;
-    k_inc_place<<<2 * num_sms, kThreads, fsm, s>>>(list, lcount, prev, first, sub, n, L.tiles, valid, bcnt, store,
+    k_inc_place<<<4 * num_sms, kThreads, fsm, s>>>(list, lcount, prev, first, sub, n, L.tiles, valid, bcnt, store,
                                                    over, done, tcnt, tpre, boff);
     /* the gated full sort of (keys, identity) on the side stream, beside the merge (one of
      * the two writes the result); prev is its scratch and its last pass writes kout / vout */
