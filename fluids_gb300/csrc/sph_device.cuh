@@ -359,12 +359,16 @@ __device__ __forceinline__ int* list_slot(char* row, int k, unsigned n4) {
  * before the current U visits, so their latency overlaps the visits: measured on GB300 it
  * speeds up both walks that use it two entries deep: the normal pass 0.310 -> 0.291 ms at
  * 4M four deep and 0.272 ms two deep (eight deep 0.471 ms at 66 registers), the force pass
- * 0.699 -> 0.667 ms two deep (four deep its registers spill).  The visits run in list order
- * either way, so every sum keeps the list's order. */
+ * 0.699 -> 0.667 ms two deep.  PRED (with PIPE) drops the separate tail: a last, partial
+ * batch loads the particle itself in place of the missing entries and skips their visits;
+ * the force pass walks that way four deep, 0.628 -> 0.600 ms (the normal pass 0.320 ms four
+ * deep, so it stays two deep without PRED).  The visits run in list order either way, so
+ * every sum keeps the list's order. */
 #ifndef SPH_LIST_UNROLL
 #define SPH_LIST_UNROLL 4
 #endif
-template <int U = SPH_LIST_UNROLL, bool PIPE = false, class F>
+
+template <int U = SPH_LIST_UNROLL, bool PIPE = false, bool PRED = false, class F>
 __device__ __forceinline__ void list_neighbors(int i, int n, const int* __restrict__ list, int len,
                                                const float4* __restrict__ npos, float px, float py, float pz,
                                                F&& f) {
@@ -384,6 +388,28 @@ __device__ __forceinline__ void list_neighbors(int i, int n, const int* __restri
             for (int u = 0; u < U; ++u)
                 f(j[u], q[u], __fsub_rn(px, q[u].x), __fsub_rn(py, q[u].y), __fsub_rn(pz, q[u].z));
         }
+    } else if (PRED) {
+        /* batches of U; a last, partial batch loads its missing entries as the particle
+         * itself (a valid index) and does not visit them */
+        int jn[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) jn[u] = u < len ? __ldg(p + u * sn) : i;
+#pragma unroll 1
+        for (; k < len; k += U) {
+            int j[U];
+            float4 q[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) j[u] = jn[u];
+#pragma unroll
+            for (int u = 0; u < U; ++u) q[u] = __ldg(&npos[j[u]]);
+            p += U * sn;
+#pragma unroll
+            for (int u = 0; u < U; ++u) jn[u] = k + U + u < len ? __ldg(p + u * sn) : i;
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (k + u < len) f(j[u], q[u], __fsub_rn(px, q[u].x), __fsub_rn(py, q[u].y), __fsub_rn(pz, q[u].z));
+        }
+        return;
     } else if (len >= U) {
         int jn[U];
 #pragma unroll
@@ -425,9 +451,9 @@ struct Neigh {
     const int* list;
     const int* len;
     const float4* npos;
-    template <bool PIPE = false, int U = SPH_LIST_UNROLL, class F>
+    template <bool PIPE = false, int U = SPH_LIST_UNROLL, bool PRED = false, class F>
     __device__ __forceinline__ void visit(const Const& c, int i, float px, float py, float pz, F&& f) const {
-        if (LIST) list_neighbors<U, PIPE>(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
+        if (LIST) list_neighbors<U, PIPE, PRED>(i, c.n, list, __ldg(&len[i]), npos, px, py, pz, f);
         else scan_neighbors<EXACT>(c, px, py, pz, tab, npos, f);
     }
 };
