@@ -255,6 +255,12 @@ __device__ __forceinline__ void wc_integrate_one(const Const& c, float4 p, float
     bad = !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(vx) && isfinite(vy) && isfinite(vz));
 }
 
+/* the single-scene force walk's depth: measured on GB300 at 4M, 0.600 ms four deep at 4
+ * blocks/SM (64 registers) against 0.707 six deep (spills), and at 3 blocks/SM 0.689, 0.671
+ * and 0.663 ms four, six and eight deep */
+#ifndef SPH_FORCES_WALK
+#define SPH_FORCES_WALK 4
+#endif
 #ifndef SPH_FORCES_MIN_BLOCKS
 #define SPH_FORCES_MIN_BLOCKS 4
 #endif
@@ -296,7 +302,7 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
     /* list walk two entries deep with the next two entries loaded during the visits: 0.667 ms
      * vs 0.699 ms for four deep without that prefetch (and vs spills at four deep with it) */
     /* four deep with the predicated last batch single-scene; the batched kernel keeps two */
-    fl.template visit<true, BATCH ? 2 : 4, !BATCH>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy,
+    fl.template visit<true, BATCH ? 2 : SPH_FORCES_WALK, !BATCH>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy,
                                                                               float dz) {
         const float r2 = dx * dx + dy * dy + dz * dz;
         /* loaded ahead of the guard so that the list loop can issue them early */
