@@ -280,6 +280,9 @@ __device__ __forceinline__ int scan_neighbors(const Const& c, float px, float py
 #ifndef SPH_BUILD_UNROLL
 #define SPH_BUILD_UNROLL 2
 #endif
+#ifndef SPH_BUILD_PAIRS
+#define SPH_BUILD_PAIRS 1
+#endif
 constexpr int kBuildUnroll = SPH_BUILD_UNROLL;
 /* CELL_NEIGH_OFFSET order as (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4, one byte per offset. */
 #define SPH_NEIGH_CODES                                                                                  \
@@ -324,6 +327,28 @@ __device__ __forceinline__ int build_scan(const Const& c, float px, float py, fl
         const int2 r = __ldg(&tab[id]);
         if (cnt + (r.y - r.x) <= c.cap) {
             const float4* __restrict__ q = npos + r.x;
+#if SPH_BUILD_PAIRS
+            /* two candidates a trip, loaded together, then an odd last one */
+            int j = r.x;
+#pragma unroll 1
+            for (; j + 1 < r.y; j += 2, q += 2) {
+                const float4 pa = __ldg(q), pb = __ldg(q + 1);
+                const float ra = r2_exact(__fsub_rn(px, pa.x), __fsub_rn(py, pa.y), __fsub_rn(pz, pa.z));
+                const float rb = r2_exact(__fsub_rn(px, pb.x), __fsub_rn(py, pb.y), __fsub_rn(pz, pb.z));
+                const bool ha = ra < h2, hb = rb < h2;
+                f(ha, j, ra, cnt);
+                cnt += ha ? 1 : 0;
+                f(hb, j + 1, rb, cnt);
+                cnt += hb ? 1 : 0;
+            }
+            if (j < r.y) {
+                const float4 pj = __ldg(q);
+                const float r2 = r2_exact(__fsub_rn(px, pj.x), __fsub_rn(py, pj.y), __fsub_rn(pz, pj.z));
+                const bool hit = r2 < h2;
+                f(hit, j, r2, cnt);
+                cnt += hit ? 1 : 0;
+            }
+#else
 #pragma unroll kBuildUnroll
             for (int j = r.x; j < r.y; ++j, ++q) {
                 const float4 pj = __ldg(q);
@@ -332,6 +357,7 @@ __device__ __forceinline__ int build_scan(const Const& c, float px, float py, fl
                 f(hit, j, r2, cnt);
                 cnt += hit ? 1 : 0;
             }
+#endif
         } else {
 #pragma unroll 1
             for (int j = r.x; j < r.y && cnt < c.cap; ++j) {

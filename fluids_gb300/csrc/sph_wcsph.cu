@@ -77,11 +77,13 @@ __global__ void __launch_bounds__(256) k_wc_density(Const c0, Neigh<LIST, COMPAT
 /* compute_neigh_list (kernels/grid.cl:145-182, fluid and boundary) fused with
  * compute_density_pressure: the density sums run over exactly the pairs written to the
  * lists, in list order, so the step needs no separate density pass. */
-/* 6 blocks/SM gives the builder 36 registers: measured on GB300 at 4M, 1.045 ms against
- * 1.052 ms at 7 or 8 blocks/SM (32 registers) and 1.147 ms unbounded (an older builder);
- * inner-loop unrolling by 1, 3 or 4 instead of 2 was 4-10 % slower. */
+/* 8 blocks/SM holds the builder at 32 registers, with its candidate loop written two
+ * candidates a trip: measured on GB300 at 4M, 1.028 ms against 1.036 ms for the compiler's
+ * unrolling by 2 at 6 blocks/SM (36 registers; 1.045 vs 1.052 ms at 8 blocks/SM) and 1.040
+ * ms at 4 blocks/SM; unrolling by 1, 3 or 4 was 4-10 % slower; 3 % fewer warp
+ * instructions (2.466e8 vs 2.544e8 at 1M). */
 #ifndef SPH_LISTS_MIN_BLOCKS
-#define SPH_LISTS_MIN_BLOCKS 6
+#define SPH_LISTS_MIN_BLOCKS 8
 #endif
 /* REMAP (the adjoint's tape, which keeps particles in id order): the list of sorted particle
  * i is written as row remap[i] with entries remap[j], and its density, pressure and aux go to
