@@ -243,6 +243,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.pci_c = cv.take<float>(n);
     b.aux = cv.take<float4>(n);
     b.nrec = cv.take<float4>(2 * n);
+    b.prho = cv.take<float4>(n);
     b.keys = cv.take<uint32_t>(n); b.keys_alt = cv.take<uint32_t>(n);
     b.mask = cv.take<int32_t>(n); b.mask_alt = cv.take<int32_t>(n);
     b.ids = cv.take<int32_t>(n); b.ids_s = cv.take<int32_t>(n);
@@ -520,7 +521,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter, cudaEvent_t vel_ready, const Host
         gather_vel();
         const bool pack = lists && c.sigma != 0.f;
         if (c.sigma != 0.f) {
-            sph::launch_normals(s, c, b, lists, bs, pack);
+            sph::launch_normals(s, c, b, lists, bs, pack, lists);   /* k_lists_density wrote prho */
             mark(x, "k_normals");
         }
         if (x->any_massive) {
@@ -568,7 +569,7 @@ int enqueue_step(sph_ctx* x, int pci_max_iter, cudaEvent_t vel_ready, const Host
          * (velocity, normal, 1/rho) that the force pass reads */
         const bool pack = c.sigma != 0.f;
         if (pack) {
-            sph::launch_normals(s, c, b, true, bs, true);
+            sph::launch_normals(s, c, b, true, bs, true, !c.compat && !c.batched);   /* after k_lists_density_pci */
             mark(x, "k_normals");
         }
         sph::launch_pci_init_forces(s, c, b, bs, pack);

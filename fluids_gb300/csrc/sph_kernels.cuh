@@ -19,6 +19,8 @@ struct Bufs {
     float* pci_c;                          /* PCISPH loop: p / rho^2 of each particle this iteration */
     float4* aux;                           /* per particle (p/rho^2, 1/rho, rho, p) */
     float4* nrec;                          /* 2 per particle: (v, p/rho^2), (normal, 1/rho) for the force pass */
+    float4* prho;                          /* per particle (x, y, z, rho), written by the list + density pass of
+                                              the step for the normal pass (one load per neighbour) */
     uint32_t *keys, *keys_alt;
     int32_t *mask, *mask_alt;
     uint32_t* keys_sorted;                 /* where the sort left the keys */
@@ -121,7 +123,10 @@ void launch_neigh_lists(cudaStream_t s, const Const& c, const float4* spos, cons
 void launch_wc_density(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs);
 /* pack: also write nrec (the force pass then reads 2 adjacent float4 per neighbour instead of
  * velocity, aux and normal); only the fused step uses it */
-void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs, bool pack = false);
+/* prho: the step's list + density pass wrote b.prho, which the walk then reads for both the
+ * neighbour's position and its density */
+void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs, bool pack = false,
+                    bool prho = false);
 void launch_wc_forces(cudaStream_t s, const Const& c, const Bufs& b, bool lists, bool fuse_integrate,
                       bool write_acc, int bs, bool pack = false);
 void launch_wc_integrate(cudaStream_t s, const Const& c, const Bufs& b, int bs);

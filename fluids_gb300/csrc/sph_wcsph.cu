@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
                                                        const int32_t* __restrict__ remap = nullptr,
                                                        unsigned* __restrict__ flags = nullptr,
                                                        const uint8_t* __restrict__ bnear = nullptr,
-                                                       const int32_t* __restrict__ noff = nullptr) {
+                                                       const int32_t* __restrict__ noff = nullptr,
+                                                       float4* __restrict__ prho = nullptr) {
   for_each_particle<BATCH>(c0, tiles, scenes, next, [&](const Const& c, long long base, int i) {
     const int2* __restrict__ ftab = tab0 + base;
     const int2* __restrict__ fbtab = btab0 + base;
@@ -155,12 +156,14 @@ __global__ void __launch_bounds__(256, SPH_LISTS_MIN_BLOCKS) k_lists_density(Con
     if (PCI) {
         const float d = c.default_eval * ((di * c.mass_def) + bdi);
         dens[row] = d;
+        if (prho) prho[row] = make_float4(pi.x, pi.y, pi.z, d);
         pres[row] = 0.f;
         aux[row] = make_float4(0.f, 1.0f / d, d, 0.f);
         return;
     }
     di += c.poly6_eval * bdi;
     dens[row] = di;
+    if (prho) prho[row] = make_float4(pi.x, pi.y, pi.z, di);   /* the normal pass's neighbour records */
     const float pv = c.kgas * (pown7(di / c.rho0) - 1.0f);
     const float p = (0.f < pv) ? pv : 0.f;
     pres[row] = p;
@@ -178,7 +181,7 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
 
 /* MON: compute_normals with the Monaghan kernels, GRAD_W_DEFAULT(r, r.r, h) / rho_j
  * (normals.cl:66; the kernel text passes r^2 where the function takes |r|). */
-template <bool LIST, bool EXACT, bool BATCH, bool MON = false>
+template <bool LIST, bool EXACT, bool BATCH, bool MON = false, bool PRHO = false>
 __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl0, const float4* __restrict__ aux,
                                                  const float* __restrict__ dens, float4* __restrict__ normal,
                                                  const SceneDev* __restrict__ scenes,
@@ -192,11 +195,12 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
     /* two entries deep with the next two loaded during the visits (0.272 ms vs 0.291 four deep) */
-    fl.template visit<true, 2>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy, float dz) {
-        /* 1/rho_j from the dense density array (8 particles per 32-byte sector instead of 2
-         * for aux; the pass is bound by L1 throughput); __frcp_rn is the correctly rounded
-         * reciprocal, the value aux holds */
-        const float inv_rho = __frcp_rn(__ldg(&dens[j]));
+    fl.template visit<true, 2>(c, i, pi.x, pi.y, pi.z, [&](int j, float4 q, float dx, float dy, float dz) {
+        /* 1/rho_j: PRHO, from the w of the neighbour record the walk loaded with its position
+         * (npos = prho); otherwise from the dense density array (8 particles per 32-byte
+         * sector instead of 2 for aux; the pass is bound by L1 throughput); __frcp_rn is the
+         * correctly rounded reciprocal, the value aux holds */
+        const float inv_rho = __frcp_rn(PRHO ? q.w : __ldg(&dens[j]));
         if constexpr (MON) {
             float gx, gy, gz;
             grad_w_monaghan(dx, dy, dz, dx * dx + dy * dy + dz * dz, H, H, gx, gy, gz);
@@ -448,14 +452,14 @@ static void lists_density_launch(cudaStream_t s, const Const& c, const Bufs& b, 
     k_lists_density<COMPAT, BATCH><<<grid_for<BATCH>(c, bs), bs, 0, s>>>(c, b.pos_s, b.tab, b.bpos_s, b.btab,
                                                                 b.bphi_s, b.nlist, b.nlen, b.sblist, b.sblen,
                                                                 b.density, b.pressure, b.aux, b.scenes, b.tiles,
-                                                                next, nullptr, nullptr, b.bnear, b.noff);
+                                                                next, nullptr, nullptr, b.bnear, b.noff, b.prho);
 }
 
 void launch_lists_density_pci(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     if (c.n <= 0) return;
     k_lists_density<false, false, false, true><<<nblk(c.n, bs), bs, 0, s>>>(
         c, b.pos_s, b.tab, b.bpos_s, b.btab, b.bphi_s, b.nlist, b.nlen, b.sblist, b.sblen, b.density, b.pressure,
-        b.aux, b.scenes, b.tiles, nullptr, nullptr, nullptr, b.bnear, b.noff);
+        b.aux, b.scenes, b.tiles, nullptr, nullptr, nullptr, b.bnear, b.noff, b.prho);
 }
 void launch_lists_density_remap(cudaStream_t s, const Const& c, const Bufs& b, const int32_t* remap, int bs) {
     if (c.n <= 0) return;
@@ -476,7 +480,7 @@ void launch_aux(cudaStream_t s, const Const& c, const Bufs& b, int bs) {
     k_aux<<<nblk(c.n, bs), bs, 0, s>>>(c.n, b.density, b.pressure, b.aux);
 }
 
-void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs, bool pack) {
+void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, int bs, bool pack, bool prho) {
     if (c.n <= 0) return;
     const int g = nblk(c.n, bs), gt = grid_for<true>(c, bs);
     float4* nrec = pack ? b.nrec : nullptr;
@@ -491,12 +495,23 @@ void launch_normals(cudaStream_t s, const Const& c, const Bufs& b, bool lists, i
         return;
     }
     if (lists) {
-        if (c.batched)
-            k_normals<true, true, true><<<gt, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,
-                                                          b.scenes, b.tiles, next, b.vel_s, nrec);
-        else
-            k_normals<true, true, false><<<g, bs, 0, s>>>(c, fluid_src<true, true>(b), b.aux, b.density, b.normal,
-                                                          b.scenes, b.tiles, next, b.vel_s, nrec);
+        auto fl = fluid_src<true, true>(b);
+        if (prho) fl.npos = b.prho;
+        if (c.batched) {
+            if (prho)
+                k_normals<true, true, true, false, true><<<gt, bs, 0, s>>>(c, fl, b.aux, b.density, b.normal,
+                                                                         b.scenes, b.tiles, next, b.vel_s, nrec);
+            else
+                k_normals<true, true, true><<<gt, bs, 0, s>>>(c, fl, b.aux, b.density, b.normal, b.scenes, b.tiles,
+                                                              next, b.vel_s, nrec);
+        } else {
+            if (prho)
+                k_normals<true, true, false, false, true><<<g, bs, 0, s>>>(c, fl, b.aux, b.density, b.normal,
+                                                                          b.scenes, b.tiles, next, b.vel_s, nrec);
+            else
+                k_normals<true, true, false><<<g, bs, 0, s>>>(c, fl, b.aux, b.density, b.normal, b.scenes, b.tiles,
+                                                              next, b.vel_s, nrec);
+        }
     } else if (c.compat) {
         k_normals<false, true, false><<<g, bs, 0, s>>>(c, fluid_src<false, true>(b), b.aux, b.density, b.normal,
                                                        b.scenes, b.tiles, next);
