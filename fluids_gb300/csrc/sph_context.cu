@@ -241,6 +241,7 @@ void carve(sph_ctx* x, Carver& cv) {
     b.f_other = cv.take<float4>(n); b.f_press = cv.take<float4>(n);
     b.density = cv.take<float>(n); b.pressure = cv.take<float>(n); b.dens_var = cv.take<float>(n);
     b.pci_c = cv.take<float>(n);
+    b.pci_pc = cv.take<float4>(n);
     b.aux = cv.take<float4>(n);
     b.nrec = cv.take<float4>(2 * n);
     b.prho = cv.take<float4>(n);

@@ -17,6 +17,7 @@ struct Bufs {
     float4 *normal, *accel, *pos_pred, *f_other, *f_press;
     float *density, *pressure, *dens_var;
     float* pci_c;                          /* PCISPH loop: p / rho^2 of each particle this iteration */
+    float4* pci_pc;                        /* PCISPH loop: (x, y, z, p / rho^2), the force phase's neighbour record */
     float4* aux;                           /* per particle (p/rho^2, 1/rho, rho, p) */
     float4* nrec;                          /* 2 per particle: (v, p/rho^2), (normal, 1/rho) for the force pass */
     float4* prho;                          /* per particle (x, y, z, rho), written by the list + density pass of

@@ -156,11 +156,6 @@ __device__ __forceinline__ void walk_list(const int* __restrict__ e, size_t n, i
             if (k + u < len) visit(q[u]);
     }
 }
-struct PosQ {
-    float4 p;
-    float q;
-};
-
 template <bool COMPAT>
 __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, int i) {
     const float4 pi = b.pos_pred[i];
@@ -205,13 +200,17 @@ __device__ __forceinline__ float pci_update_one(const Const& c, const Bufs& b, i
     const float p = __fadd_rn(b.pressure[i], __fmul_rn(dv, c.delta));
     b.pressure[i] = p;
     const float di = __ldg(&b.density[i]);
-    b.pci_c[i] = p / (di * di);
+    const float q = p / (di * di);
+    b.pci_c[i] = q;
+    const float4 ps = __ldg(&b.pos_s[i]);
+    b.pci_pc[i] = make_float4(ps.x, ps.y, ps.z, q);   /* one record per neighbour for the force phase */
     return dv;
 }
 
 /* compute_pressure_force for one particle (initial density, updated pressure):
- * (p_i / rho_i^2 + p_j / rho_j^2) per pair with both quotients from pci_c (written by this
- * kernel's update phase, so plain loads); walked two entries deep like the update phase. */
+ * (p_i / rho_i^2 + p_j / rho_j^2) per pair with the quotients of pci_c; each neighbour's
+ * position and quotient come as one record from pci_pc (both written by the update phase
+ * of this kernel, so plain loads). */
 template <bool MON = false>
 __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Bufs& b, int i) {
     const float4 pi = __ldg(&b.pos_s[i]);
@@ -246,8 +245,8 @@ __device__ __forceinline__ void pci_pressure_force_one(const Const& c, const Buf
         fy += q * ((dy * il) * t);
         fz += q * ((dz * il) * t);
     };
-    walk_list<SPH_PCI_WALK_DEPTH>(e, n, len, i, [&](int j) { return PosQ{__ldg(&b.pos_s[j]), b.pci_c[j]}; },
-                                  [&](const PosQ& v) { visit(v.p, v.q); });
+    walk_list<SPH_PCI_WALK_DEPTH>(e, n, len, i, [&](int j) { return b.pci_pc[j]; },
+                                  [&](const float4& v) { visit(v, v.w); });
     const float sf = (-(c.mass_def * c.mass_def)) * c.spiky_grad;
     fx *= sf; fy *= sf; fz *= sf;
     const int blen = __ldg(&b.sblen[i]);
@@ -449,7 +448,10 @@ __global__ void __launch_bounds__(256) k_pci_quotient(Const c, Bufs b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const float di = b.density[i];
-    b.pci_c[i] = b.pressure[i] / (di * di);
+    const float q = b.pressure[i] / (di * di);
+    b.pci_c[i] = q;
+    const float4 ps = __ldg(&b.pos_s[i]);
+    b.pci_pc[i] = make_float4(ps.x, ps.y, ps.z, q);
 }
 
 __global__ void __launch_bounds__(256) k_pci_pressure_force(Const c, Bufs b) {
