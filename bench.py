@@ -44,7 +44,7 @@ ALG_BYTES = {
     "k_cell_ranges": 16 + 8 + 4 + 8,         # sorted pos, 2 keys, cell id out, range writes (per cell)
     "k_gather_ranges": 4 + 3 * 16 * 2 + 4 * 2 + 8 + 4 + 8,   # the gather + keys, cell id out, range writes
     "k_wc_density": 16 + 8,                  # own position; density and pressure out
-    "k_lists_density": 16 + 8 + 16,          # own position; density, pressure, aux out (+ the lists it writes)
+    "k_lists_density": 16 + 8 + 16 + 16,     # own position; density, pressure, aux, (x, y, z, rho) out (+ lists)
     "k_normals": 16 + 16,                    # own position; normal out (+ the fluid list it reads)
     "k_wc_forces": 16 * 3 + 4 + 4 + 16 + 4 + 16 * 3 + 4,   # pos,vel,vhalf,rho,p,normal,id in; pos,vel,vhalf,id out
 }
