@@ -19,7 +19,13 @@
  * the flag word, treats the missing count as 0 and finishes (the result is then wrong);
  * with in-order tile ids the wait always ends.  A context's step sorts into the context's
  * flag word, which sph_device_flags reads (SPH_FLAG_TIMEOUT); the standalone entry points
- * sph_sort_pairs and sph_sort_pairs_noalloc do not read their flag word back.
+ * sph_sort_pairs and sph_sort_pairs_noalloc do not read their flag word back.  A grid
+ * smaller than the tile count loops over tiles (the gated use below).
+ *
+ * The step's sort (sort_pairs_incremental, second half of this file) computes the same
+ * permutation as an update of the previous step's sorted keys: only the particles whose key
+ * changed are searched for and merged; the onesweep runs, gated, when there is no previous
+ * result or too many particles moved.
  */
 #include "sph_kernels.cuh"
 
