@@ -179,6 +179,15 @@ __global__ void __launch_bounds__(256) k_aux(int n, const float* __restrict__ de
     aux[i] = make_aux(dens[i], pres[i]);
 }
 
+/* the normal walk's depth: measured on GB300 at 4M with the (x, y, z, rho) records, 0.225 ms
+ * two deep against 0.240 three deep, 0.232 four deep, and with the predicated last batch
+ * 0.235 two deep and 0.255 four deep */
+#ifndef SPH_NORMALS_WALK
+#define SPH_NORMALS_WALK 2
+#endif
+#ifndef SPH_NORMALS_PRED
+#define SPH_NORMALS_PRED 0
+#endif
 /* MON: compute_normals with the Monaghan kernels, GRAD_W_DEFAULT(r, r.r, h) / rho_j
  * (normals.cl:66; the kernel text passes r^2 where the function takes |r|). */
 template <bool LIST, bool EXACT, bool BATCH, bool MON = false, bool PRHO = false>
@@ -194,8 +203,9 @@ __global__ void __launch_bounds__(256) k_normals(Const c0, Neigh<LIST, EXACT> fl
     const float4 pi = __ldg(&fl.npos[i]);
     const float H = c.h_def, HH = H * H;
     float nx = 0.f, ny = 0.f, nz = 0.f;
-    /* two entries deep with the next two loaded during the visits (0.272 ms vs 0.291 four deep) */
-    fl.template visit<true, 2>(c, i, pi.x, pi.y, pi.z, [&](int j, float4 q, float dx, float dy, float dz) {
+    /* two entries deep with the next two loaded during the visits */
+    fl.template visit<true, SPH_NORMALS_WALK, SPH_NORMALS_PRED != 0>(c, i, pi.x, pi.y, pi.z,
+                                                                     [&](int j, float4 q, float dx, float dy, float dz) {
         /* 1/rho_j: PRHO, from the w of the neighbour record the walk loaded with its position
          * (npos = prho); otherwise from the dense density array (8 particles per 32-byte
          * sector instead of 2 for aux; the pass is bound by L1 throughput); __frcp_rn is the
