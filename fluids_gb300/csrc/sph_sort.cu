@@ -286,26 +286,35 @@ void sort_pairs(cudaStream_t s, uint32_t* k0, int32_t* v0, uint32_t* k1, int32_t
  * holds for any non-decreasing prev.  prev is the workspace's own copy of the last result
  * (written beside the output, so that writes to the output from outside cannot unsort it).
  *
- *   k_inc_flags  per tile of kIncTile positions: the moved flags as ballot words (bits) and
- *                the tile's count of moved particles.
+ *   k_inc_flags  per tile of kIncTile positions: the moved flags as ballot words (bits), the
+ *                tile's count of moved particles, and the moved (index, key) pairs appended
+ *                to a list (one atomic per tile; the list's order does not matter).  The
+ *                step's hash kernel does the same pass on the keys it computes
+ *                (k_hashes_flags, sph_grid.cu).
  *   k_inc_place  per moved particle (k, i): p = the first position whose (prev[p], p) is
  *                not below (k, i), by binary searches over each tile's first prev key (a
  *                table staged in shared memory), then each word's first prev key within
  *                the tile, then prev within the word.  (k, i, p) goes to bucket p / kIncTile.
  *                The stayed particles at positions [t kIncTile, (t + 1) kIncTile) are all
  *                above the moved particles of the buckets below t and below those of the
- *                buckets above t, so only bucket t's need comparing with them.
- *   k_inc_merge  per tile t: the bucket's particles ranked among themselves in shared
- *                memory; a moved particle goes to (stayed before p) + (moved particles of the
- *                buckets below t) + its rank, a stayed particle of stayed rank a to a + (moved
- *                particles of the buckets below t) + (bucket particles below it).
+ *                buckets above t, so only bucket t's need comparing with them.  The last
+ *                CTA turns the tile and bucket counts into prefix sums.
+ *   k_inc_merge  per tile t: a bucket particle e is below the stayed particle at position j
+ *                exactly when p_e <= j, so a prefix sum of the bucket's insertion points
+ *                over the tile gives every stayed particle its count of bucket particles
+ *                below it; the bucket's particles are ranked by p and, for equal p, by
+ *                (key, index).  A moved particle goes to (stayed before p) + (moved
+ *                particles of the buckets below t) + its rank, a stayed particle of stayed
+ *                rank a to a + (moved particles of the buckets below t) + (bucket particles
+ *                below it).
  *   k_inc_keep   after an overflow, keeps the full sort's keys as prev; marks prev valid.
  * A bucket holds kIncBucket particles.  When one overflows, when more than a sixth of the
  * particles moved (their searches would cost more than a full sort), or when there is no
  * previous result (the first call), the overflow word opens the gated full onesweep sort of
  * all keys (its kernels read the word and leave at once while it is 0; they run on a side
- * stream beside k_inc_merge, which then leaves at once).  Moved particles are 1-2 % of a flowing scene per
- * step: the passes over all particles then read 8 bytes and write 12 bytes per particle.
+ * stream beside k_inc_merge, which then leaves at once).  Moved particles are 1-2 % of a
+ * flowing scene per step: the passes over all particles then read 8 bytes and write 12
+ * bytes per particle.
  * ------------------------------------------------------------------------------------- */
 namespace {
 static_assert(kIncTile == kThreads * kIncItems, "2048 positions = 64 ballot words");
