@@ -315,11 +315,11 @@ __global__ void __launch_bounds__(256, SPH_FORCES_MIN_BLOCKS) k_wc_forces(Const 
     float pax = 0.f, pay = 0.f, paz = 0.f, vax = 0.f, vay = 0.f, vaz = 0.f;
     float cux = 0.f, cuy = 0.f, cuz = 0.f, cox = 0.f, coy = 0.f, coz = 0.f;
     const float rmin2 = c.rmin2_wc, two_rho0 = 2.0f * c.rho0;
-    /* list walk two entries deep with the next two entries loaded during the visits: 0.667 ms
-     * vs 0.699 ms for four deep without that prefetch (and vs spills at four deep with it) */
-    /* four deep with the predicated last batch single-scene; the batched kernel keeps two */
-    fl.template visit<true, BATCH ? 2 : SPH_FORCES_WALK, !BATCH>(c, i, pi.x, pi.y, pi.z, [&](int j, float4, float dx, float dy,
-                                                                              float dz) {
+    /* the list walk SPH_FORCES_WALK (four) entries deep with the next entries loaded during
+     * the visits and a predicated last batch, single-scene; the batched kernel walks two deep
+     * with a serial tail (measured faster there) */
+    fl.template visit<true, BATCH ? 2 : SPH_FORCES_WALK, !BATCH>(c, i, pi.x, pi.y, pi.z,
+                                                                 [&](int j, float4, float dx, float dy, float dz) {
         const float r2 = dx * dx + dy * dy + dz * dz;
         /* loaded ahead of the guard so that the list loop can issue them early */
         float4 aj, vj, nj = make_float4(0.f, 0.f, 0.f, 0.f);
